@@ -1,0 +1,422 @@
+"""Benchmark: vertex relocations/s of the GB300 smoothing path.
+
+Workload (default): the sphere mesh -- 80^3 grid clipped to the unit ball,
+~1.6M Kuhn tets, 283k vertices -- under SphereBoundary with the metric-wise
+measurer, the sine-graded metric s^2 diag(1 + 9 sin^2(4 pi x), 1, 1) (s = 1/h)
+and metric-conformity quality: five gradient-descent passes then five
+spawn-search passes, with a full quality evaluation after every pass, as
+AbstractSmoother's pass loop does.  One step = that whole schedule from the
+same input mesh.
+
+  value   relocations/s with the mesh resident in HBM (CUDA events)
+  e2e     the same through the C ABI with host buffers: pinned-host upload of
+          the positions, the schedule, and the read-back of positions and the
+          per-pass quality histograms, all inside the timed region
+  --impl reference  the reference's CPU algorithm (the FP64 oracle port),
+          all host threads, on a bounded sample of the same workload
+
+Run under torchrun with N > 1: every rank runs an independent replica (the
+path has no exchange step); value is the sum over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "vertex relocations/s"
+UNIT = "relocations/s"
+
+# FP32 operations per element-quality evaluation (an add, multiply or
+# transcendental counts 1, an FMA counts 2), counted from the measures in
+# gpumesh_gb300/csrc/gm_device.cuh; see DESIGN.md "Relocation roofline".
+FLOPS_PER_ELEM_EVAL = {
+    ("mean_ratio", "tet"): 80,
+    ("mean_ratio", "hex"): 8 * 45 + 36 + 36,
+    ("metric_conformity", "tet"): 330,
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="C2")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-eval-roofline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_init(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if n > 0 else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = [r.split(", ") for r in self.out.strip().splitlines() if r.strip()]
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def prepare(workload_name):
+    from gpumesh_gb300 import mesh as M
+    from gpumesh_gb300 import workloads
+
+    w = workloads.WORKLOADS[workload_name]
+    raw = w.mesh()
+    perm, groups = M.node_groups_build(raw)
+    raw = M.permute_mesh(raw, perm)
+    return w, raw, groups
+
+
+def relocations_per_step(raw, w):
+    return int(np.count_nonzero(raw.cid >= 0)) * w.passes()
+
+
+def run_schedule(dev, w, torch, stream, ev_pass=None):
+    """The whole schedule with an evaluation after every pass (slot k)."""
+    slot = 0
+    dev.evaluate_async(slot)
+    slot += 1
+    for smoother, passes, params in w.schedule:
+        for _ in range(passes):
+            if ev_pass is not None:
+                ev_pass.append((smoother, torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)))
+                ev_pass[-1][1].record(stream)
+            dev.smooth_pass(smoother, params)
+            if ev_pass is not None:
+                ev_pass[-1][2].record(stream)
+            dev.evaluate_async(slot)
+            slot += 1
+    return slot
+
+
+def l2_flush(torch, buf, stream):
+    with torch.cuda.stream(stream):
+        buf.zero_()
+
+
+def flops_per_elem(w, raw):
+    key = (w.evaluator, "tet" if raw.tets.shape[0] else "hex")
+    return FLOPS_PER_ELEM_EVAL.get(key)
+
+
+def eval_roofline(torch, stream, hbm_peak, steps=10):
+    """HBM roofline of the evaluation kernel on the 128^3 hex mesh, L2 flushed
+    between launches: algorithmic bytes = 32 B/hex connectivity + 16 B/vertex."""
+    from gpumesh_gb300 import mesh as M
+    from gpumesh_gb300 import meshgen
+
+    raw = meshgen.box_mesh(128, "hex", 0.15, 2, gaussian=True)
+    dev = M.DeviceMesh(raw, None)
+    dev.set_stream(stream.cuda_stream)
+    dev.set_crew("uniform", "metric_free", "mean_ratio")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        dev.evaluate_async(0)
+    times = []
+    for _ in range(steps):
+        l2_flush(torch, flush, stream)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        dev.evaluate_async(0)
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b) * 1e-3)
+    algo = raw.hexs.shape[0] * 32 + raw.nv * 16
+    t = statistics.median(times)
+    achieved = algo / t / 1e9
+    h = dev.read_quality(0)
+    dev.close()
+    return {"bound": "hbm", "kernel": "evaluate_kernel (mean ratio, 128^3 hexes)", "achieved": round(achieved, 1),
+            "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": None,
+            "algorithmic_bytes": algo, "us_per_launch": round(t * 1e6, 2),
+            "min": h.minimumQuality(), "mean": h.harmonicMean(), "note": "of measured"}
+
+
+def cpu_sample_run(w, raw, groups, seconds, threads):
+    """Time the FP64 oracle (the reference's algorithm) on a bounded sample:
+    the first fraction f of every colour, the whole schedule, all threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    crew = w.crew(raw)
+    orc = pyoracle.OracleMesh.from_raw(raw, **crew)
+    gb = groups.group_base
+
+    def sample(frac):
+        base, mem = [0], []
+        for g in range(groups.count()):
+            m = groups.members[gb[g]:gb[g + 1]]
+            k = max(1, int(round(frac * m.size))) if m.size else 0
+            mem.append(m[:k])
+            base.append(base[-1] + k)
+        return np.array(base, np.int64), np.concatenate(mem).astype(np.uint32)
+
+    def timed(frac):
+        b, m = sample(frac)
+        orc.pos = raw.pos
+        t0 = time.perf_counter()
+        for smoother, passes, params in w.schedule:
+            for _ in range(passes):
+                orc.smooth_pass(smoother, b, m, params=params, nthreads=threads)
+        return time.perf_counter() - t0, int(m.size) * w.passes()
+
+    t, n = timed(0.002)
+    frac = min(1.0, 0.002 * seconds / max(t, 1e-3))
+    t, n = timed(frac)
+    return n / t, frac, n, t
+
+
+# ---------------------------------------------------------------------------
+def bench_reference(args, rank, world):
+    if rank != 0:
+        return
+    w, raw, groups = prepare(args.workload)
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, args.cpu_seconds / max(1, args.steps))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        rate, frac, n, t = cpu_sample_run(w, raw, groups, per_step if i >= args.warmup else 1.0, threads)
+        if i >= args.warmup:
+            vals.append(rate)
+    value = statistics.median(vals)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "vertices": raw.nv, "tets": int(raw.tets.shape[0]),
+                       "parallelism": "cpu threads"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"first {frac:.4f} of every colour, full schedule ({n} relocations per step)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def bench_gpu(args, rank, world, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    from gpumesh_gb300 import _native as N
+    from gpumesh_gb300 import mesh as M
+
+    peaks = {}
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        with open(pp) as f:
+            peaks = json.load(f)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+
+    w, raw, groups = prepare(args.workload)
+    crew = w.crew(raw)
+    stream = torch.cuda.Stream()
+    dev = M.DeviceMesh(raw, groups, stream=stream.cuda_stream)
+    dev.set_crew(**crew)
+    dev.save_positions()
+    dev.sync()
+    reloc = relocations_per_step(raw, w)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def one_step(record=None):
+        dev.restore_positions()
+        return run_schedule(dev, w, torch, stream, record)
+
+    for _ in range(args.warmup):
+        one_step()
+    dev.sync()
+    dev.counters(reset=True)
+
+    pass_events = []
+    step_times = []
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            l2_flush(torch, flush, stream)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            nslots = one_step(pass_events)
+            b.record(stream)
+            b.synchronize()
+            step_times.append(a.elapsed_time(b) * 1e-3)
+        torch.cuda.synchronize()
+    barrier(world)
+    total = max_over_ranks(sum(step_times), world)
+    value = reloc * args.steps * world / total
+    ctr = dev.counters(reset=True)
+    final = dev.read_quality(nslots - 1)
+    first = dev.read_quality(0)
+
+    # dominant relocation kernel family: the smoother with the most pass time
+    per = {}
+    for sm, e0, e1 in pass_events:
+        per.setdefault(sm, []).append(e0.elapsed_time(e1) * 1e-3)
+    dom = max(per, key=lambda k: sum(per[k]))
+    fpe = flops_per_elem(w, raw)
+    fp32 = __import__("ctypes").c_double(0)
+    N.check(N.lib().gm_probe_fp32_tflops(__import__("ctypes").byref(fp32)))
+    # element evaluations of the dominant smoother's passes: measured by a
+    # dedicated counted pass of that smoother from the same input
+    dev.restore_positions()
+    for smoother, passes, params in w.schedule:
+        if smoother == dom:
+            dev.counters(reset=True)
+            dev.smooth_pass(smoother, params)
+            dc = dev.counters(reset=True)
+            break
+        for _ in range(passes):
+            dev.smooth_pass(smoother, params)
+    dom_pass_s = statistics.median(per[dom])
+    achieved = dc["elem_evals"] * fpe / dom_pass_s / 1e12 if fpe else None
+    roofline = {"bound": "fp32", "kernel": f"relocate_kernel ({dom}, {w.evaluator})",
+                "achieved": round(achieved, 3) if achieved else None, "peak": round(fp32.value, 2),
+                "unit": "TFLOP/s", "frac": round(achieved / fp32.value, 4) if achieved else None, "traffic": None,
+                "flops_per_element_eval": fpe, "element_evals_per_pass": dc["elem_evals"],
+                "ms_per_pass": round(dom_pass_s * 1e3, 3),
+                "note": "peak = FFMA probe measured in this run (no FP32 entry in MEASURED_PEAKS.json)"}
+
+    # ---- e2e through the C ABI with host buffers ----
+    host = torch.empty((raw.nv, 4), dtype=torch.float32, pin_memory=True)
+    hv = host.numpy()
+    hv[:, :3] = raw.pos
+    hv[:, 3] = 0
+    out = torch.empty((raw.nv, 4), dtype=torch.float32, pin_memory=True).numpy()
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev.upload_gpu_verts(hv)
+        n = run_schedule(dev, w, torch, stream)
+        dev.fetch_gpu_verts(out)
+        hist = [dev.read_quality(s) for s in range(n)]
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_times.append(t1 - t0)
+    e2e_total = max_over_ranks(sum(e2e_times), world)
+    e2e = {"value": reloc * args.steps * world / e2e_total, "unit": UNIT, "h2d_bytes_per_step": raw.nv * 16,
+           "d2h_bytes_per_step": raw.nv * 16 + n * 208}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w.name, "vertices": raw.nv, "tets": int(raw.tets.shape[0]),
+                       "colours": groups.count(), "passes": w.passes(), "relocations_per_step": reloc,
+                       "parallelism": f"replicas x{world}", "l2": "flushed (256 MiB write) before every step"},
+            "quality": {"initial_min": first.minimumQuality(), "initial_mean": first.harmonicMean(),
+                        "final_min": final.minimumQuality(), "final_mean": final.harmonicMean()},
+            "gpu_launches": None, "roofline": roofline, "e2e": e2e, "clocks": clocks.summary(),
+            "counters": ctr}
+    # launches in the timed region: per pass, relocation + FP64 acceptance per colour,
+    # one counter reset, evaluation (2) after every pass, plus the initial evaluation and restore
+    ng = groups.count()
+    launches_per_step = 2 + w.passes() * (2 * ng + 2)
+    if any(s == "getme" for s, _, _ in w.schedule):
+        launches_per_step += sum(p for s, p, _ in w.schedule if s == "getme")
+    line["gpu_launches"] = launches_per_step * args.steps
+    if not args.no_eval_roofline and rank == 0:
+        line["roofline_eval"] = eval_roofline(torch, stream, hbm_peak)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, frac, n, t = cpu_sample_run(w, raw, groups, args.cpu_seconds, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": f"first {frac:.4f} of every colour, full schedule, {n} relocations "
+                                          f"in {t:.1f} s"}
+    dev.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_init(args.gpus)
+    if args.impl == "reference":
+        bench_reference(args, rank, world)
+    else:
+        bench_gpu(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,851 @@
+// C ABI of libgpumesh_gb300.so (include/gpumesh_gb300.h): device-resident
+// meshes, uploads in the reference's buffer layouts, evaluation and
+// relocation launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <exception>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gpumesh_gb300.h"
+#include "gm_internal.h"
+#include "gm_launch.h"
+
+namespace gm {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+struct ApiError : std::runtime_error
+{
+    gm_status status;
+    ApiError(gm_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define GM_CUDA(call)                                                                                      \
+    do                                                                                                     \
+    {                                                                                                      \
+        cudaError_t e_ = (call);                                                                           \
+        if (e_ != cudaSuccess)                                                                             \
+            throw ApiError(e_ == cudaErrorMemoryAllocation ? GM_ERR_OUT_OF_MEMORY : GM_ERR_CUDA,           \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+    } while (0)
+
+static void require(bool ok, const std::string& msg)
+{
+    if (!ok) throw ApiError(GM_ERR_INVALID_ARG, msg);
+}
+
+template <class F>
+static gm_status guarded(F&& f)
+{
+    try
+    {
+        f();
+        return GM_OK;
+    }
+    catch (const ApiError& e)
+    {
+        set_error(e.what());
+        return e.status;
+    }
+    catch (const std::bad_alloc&)
+    {
+        set_error("host allocation failed");
+        return GM_ERR_OUT_OF_MEMORY;
+    }
+    catch (const std::exception& e)
+    {
+        set_error(e.what());
+        return GM_ERR_STATE;
+    }
+}
+
+// growable device buffer
+template <class T>
+struct DBuf
+{
+    T* p = nullptr;
+    size_t cap = 0;
+    void reserve(size_t n)
+    {
+        if (n <= cap && p) return;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+        GM_CUDA(cudaMalloc(&p, bytes));
+        cap = std::max<size_t>(n, 1);
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+template <class T>
+static void upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s)
+{
+    b.reserve(n);
+    if (n) GM_CUDA(cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+}  // namespace gm
+
+using namespace gm;
+
+struct gm_mesh
+{
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = 0;
+    uint32_t nv = 0, nt = 0, np = 0, nh = 0;
+    DBuf<float4> pos;
+    DBuf<uint4> tets;
+    DBuf<uint32_t> pris;
+    DBuf<uint4> hexs;
+    DBuf<uint32_t> ve_off, ve, vv_off, vv;
+    DBuf<int32_t> cid;
+    DBuf<Constraint> con;
+    int ncon = 0;
+    DBuf<uint32_t> members;
+    uint32_t n_members = 0;
+    std::vector<uint32_t> group_base;
+    DBuf<Quality> quality;
+    uint32_t n_quality_slots = 0;
+    DBuf<EvalPartial> parts;
+    DBuf<float4> corners;
+    DBuf<float4> saved;
+    DBuf<Counters> ctr;
+    // FP64 acceptance hand-over: per-member slots and one counter per group
+    DBuf<uint32_t> def_v;
+    DBuf<float4> def_old, def_new;
+    DBuf<uint32_t> def_count;
+    Crew crew{};
+    int ks = 4;
+    int maxe = 32;
+    int warps_per_block = 4;
+    std::vector<float4> staging;  // host conversion buffer
+
+    MeshView view() const
+    {
+        MeshView v;
+        v.nv = nv;
+        v.nt = nt;
+        v.np = np;
+        v.nh = nh;
+        v.pos = pos.p;
+        v.tets = tets.p;
+        v.pris = pris.p;
+        v.hexs = hexs.p;
+        v.ve_off = ve_off.p;
+        v.ve = ve.p;
+        v.vv_off = vv_off.p;
+        v.vv = vv.p;
+        v.cid = cid.p;
+        v.con = con.p;
+        v.ncon = ncon;
+        return v;
+    }
+
+    // evaluator x measurer variant of the vertex kernels
+    int variant() const
+    {
+        if (crew.evaluator == GM_EVALUATOR_METRIC_CONFORMITY) return kVarMC;
+        return crew.measurer == GM_MEASURER_METRIC_WISE ? kVarMRWise : kVarMRFree;
+    }
+    // variant of the GETMe element pass, whose volumes also follow the measurer
+    int element_variant() const
+    {
+        if (crew.evaluator == GM_EVALUATOR_METRIC_CONFORMITY)
+            return crew.measurer == GM_MEASURER_METRIC_WISE ? kVarMCWise : kVarMC;
+        return variant();
+    }
+    int maxk() const { return (np || nh) ? 8 : 4; }
+};
+
+namespace {
+
+void set_crew(gm_mesh* m, int sampler, int measurer, int evaluator, double scaling, double aspect)
+{
+    require(sampler >= 0 && sampler <= 2, "unknown sampler");
+    require(measurer >= 0 && measurer <= 1, "unknown measurer");
+    require(evaluator >= 0 && evaluator <= 1, "unknown evaluator");
+    Crew& c = m->crew;
+    c.sampler = sampler;
+    c.measurer = measurer;
+    c.evaluator = evaluator;
+    c.scaling = scaling;
+    c.scaling2 = c.scaling * scaling;
+    c.scaling3 = c.scaling2 * scaling;
+    c.aspect = aspect;
+    // AbstractSampler's fixed rotation (Samplers/AbstractSampler.cpp:30-40):
+    // pi/4 about +z, then pi/4 about -y, composed on the right
+    auto rot = [](const double* m3, double ang, double ax, double ay, double az, double* out) {
+        double c_ = std::cos(ang), s_ = std::sin(ang);
+        double n = 1.0 / std::sqrt(ax * ax + ay * ay + az * az);
+        double a[3] = {ax * n, ay * n, az * n};
+        double t[3] = {(1 - c_) * a[0], (1 - c_) * a[1], (1 - c_) * a[2]};
+        double R[9];  // column-major
+        R[0] = c_ + t[0] * a[0];
+        R[1] = t[0] * a[1] + s_ * a[2];
+        R[2] = t[0] * a[2] - s_ * a[1];
+        R[3] = t[1] * a[0] - s_ * a[2];
+        R[4] = c_ + t[1] * a[1];
+        R[5] = t[1] * a[2] + s_ * a[0];
+        R[6] = t[2] * a[0] + s_ * a[1];
+        R[7] = t[2] * a[1] - s_ * a[0];
+        R[8] = c_ + t[2] * a[2];
+        for (int j = 0; j < 3; ++j)
+            for (int r = 0; r < 3; ++r)
+                out[j * 3 + r] = m3[0 * 3 + r] * R[j * 3 + 0] + m3[1 * 3 + r] * R[j * 3 + 1] + m3[2 * 3 + r] * R[j * 3 + 2];
+    };
+    double I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, A[9];
+    const double pi = 3.14159265358979323846;
+    rot(I, pi / 4.0, 0, 0, 1, A);
+    rot(A, pi / 4.0, 0, -1, 0, c.rot);
+    for (int j = 0; j < 3; ++j)
+        for (int r = 0; r < 3; ++r) c.rotinv[j * 3 + r] = c.rot[r * 3 + j];
+}
+
+void update_patch_shape(gm_mesh* m, const uint32_t* ve_off_host)
+{
+    uint32_t mx = 0;
+    for (uint32_t v = 0; v < m->nv; ++v) mx = std::max(mx, ve_off_host[v + 1] - ve_off_host[v]);
+    m->maxe = std::max<int>(32, (int)((mx + 31) / 32 * 32));
+    m->ks = (m->nh || m->np) ? 8 : 4;
+    size_t per = patch_smem_per_warp(m->ks, m->maxe);
+    int wpb = 4;
+    while (wpb > 1 && per * wpb > 96 * 1024) wpb >>= 1;
+    if (per * wpb > 200 * 1024)
+        throw ApiError(GM_ERR_UNSUPPORTED, "a vertex has " + std::to_string(mx) +
+                                               " incident elements, more than the relocation kernels stage");
+    m->warps_per_block = wpb;
+}
+
+void upload_csr(gm_mesh* m, const std::vector<uint32_t>& ve_off, const std::vector<uint32_t>& ve,
+                const std::vector<uint32_t>& vv_off, const std::vector<uint32_t>& vv)
+{
+    upload(m->ve_off, ve_off.data(), ve_off.size(), m->stream);
+    upload(m->ve, ve.data(), ve.size(), m->stream);
+    upload(m->vv_off, vv_off.data(), vv_off.size(), m->stream);
+    upload(m->vv, vv.data(), vv.size(), m->stream);
+    update_patch_shape(m, ve_off.data());
+}
+
+void check_conn(const uint32_t* c, size_t n, uint32_t nv, const char* what)
+{
+    for (size_t i = 0; i < n; ++i)
+        if (c[i] >= nv) throw ApiError(GM_ERR_INVALID_ARG, std::string(what) + " references vertex " +
+                                                                std::to_string(c[i]) + " >= vertex count");
+}
+
+void upload_positions(gm_mesh* m, uint32_t nv, const double* xyz)
+{
+    m->staging.resize(nv);
+    for (uint32_t v = 0; v < nv; ++v)
+    {
+        double x = xyz[3 * (size_t)v], y = xyz[3 * (size_t)v + 1], z = xyz[3 * (size_t)v + 2];
+        if (!(std::isfinite(x) && std::isfinite(y) && std::isfinite(z)))
+            throw ApiError(GM_ERR_INVALID_ARG, "vertex " + std::to_string(v) + " has a non-finite position");
+        m->staging[v] = make_float4((float)x, (float)y, (float)z, 0.f);
+    }
+    upload(m->pos, m->staging.data(), nv, m->stream);
+    m->nv = nv;
+}
+
+template <int K>
+void upload_conn(gm_mesh* m, uint32_t n, const uint32_t* words, uint32_t stride, std::vector<uint32_t>& packed)
+{
+    require(stride >= (uint32_t)K, "element stride shorter than the element");
+    packed.resize((size_t)n * K);
+    for (uint32_t i = 0; i < n; ++i)
+        for (int k = 0; k < K; ++k) packed[(size_t)i * K + k] = words[(size_t)i * stride + k];
+}
+
+SmoothParams parse_params(int smoother, const double* p)
+{
+    SmoothParams sp{};
+    sp.alpha = 1.f;
+    sp.beta = 0.5f;
+    sp.gamma = 2.f;
+    sp.convergence = 1e-4f;
+    sp.accept_q = 1e-3f;
+    switch (smoother)
+    {
+    case GM_SMOOTH_NELDER_MEAD:
+        sp.shift = (float)(p ? p[0] : 1.0 / 24.0);
+        sp.cycles = p ? (int)p[1] : 12;
+        sp.convergence = (float)(p ? p[2] : 1e-4);
+        sp.alpha = (float)(p ? p[3] : 1.0);
+        sp.beta = (float)(p ? p[4] : 0.5);
+        sp.gamma = (float)(p ? p[5] : 2.0);
+        break;
+    case GM_SMOOTH_GRADIENT_DESCENT:
+        sp.shift = (float)(p ? p[0] : 1.0 / 75.0);
+        sp.cycles = p ? (int)p[1] : 5;
+        break;
+    case GM_SMOOTH_SPAWN_SEARCH:
+        sp.shift = (float)(p ? p[0] : 1.0 / 20.0);
+        sp.cycles = p ? (int)p[1] : 2;
+        break;
+    case GM_SMOOTH_GETME:
+        sp.lambda = (float)(p ? p[0] : 0.78);
+        break;
+    default:
+        throw ApiError(GM_ERR_INVALID_ARG, "unknown smoother " + std::to_string(smoother));
+    }
+    if (p && p[7] > 0) sp.accept_q = (float)p[7];
+    require(sp.cycles >= 0 && sp.cycles <= 4096, "cycle count out of range");
+    return sp;
+}
+
+void require_mesh(const gm_mesh* m)
+{
+    require(m != nullptr, "null mesh");
+    require(m->nv > 0 && m->pos.p, "mesh has no vertices");
+    require(m->cid.p != nullptr, "mesh has no topology");
+}
+
+void require_groups(const gm_mesh* m) { require(!m->group_base.empty(), "mesh has no independent groups"); }
+
+void ensure_deferred(gm_mesh* m)
+{
+    require(m->n_members > 0 || !m->group_base.empty(), "mesh has no independent groups");
+    m->def_v.reserve(m->n_members);
+    m->def_old.reserve(m->n_members);
+    m->def_new.reserve(m->n_members);
+    m->def_count.reserve(m->group_base.size() + 2);
+}
+
+// one group: the FP32 relocation (or GETMe update) launch, then the FP64
+// acceptance launch for the vertices it handed over
+void relocate_group(gm_mesh* m, int smoother, const SmoothParams& sp, uint32_t base, uint32_t count, uint32_t slot)
+{
+    if (count == 0) return;
+    RelocLaunch L;
+    L.variant = m->variant();
+    L.maxk = m->maxk();
+    L.m = m->view();
+    L.crew = m->crew;
+    L.sp = sp;
+    L.members = m->members.p + base;
+    L.count = count;
+    L.maxe = m->maxe;
+    L.warps_per_block = m->warps_per_block;
+    L.ctr = m->ctr.p;
+    L.def = Deferred{m->def_v.p, m->def_old.p, m->def_new.p, m->def_count.p + slot};
+    L.slot_base = base;
+    L.stream = m->stream;
+    switch (smoother)
+    {
+    case GM_SMOOTH_NELDER_MEAD: GM_CUDA(launch_relocate_nm(L)); break;
+    case GM_SMOOTH_GRADIENT_DESCENT: GM_CUDA(launch_relocate_gd(L)); break;
+    case GM_SMOOTH_SPAWN_SEARCH: GM_CUDA(launch_relocate_spawn(L)); break;
+    default: GM_CUDA(launch_getme_update(L, m->corners.p)); break;
+    }
+    GM_CUDA(launch_accept(L));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gm_last_error(void) { return g_last_error.c_str(); }
+
+const char* gm_status_string(gm_status s)
+{
+    switch (s)
+    {
+    case GM_OK: return "ok";
+    case GM_ERR_INVALID_ARG: return "invalid argument";
+    case GM_ERR_CUDA: return "CUDA error";
+    case GM_ERR_OUT_OF_MEMORY: return "out of memory";
+    case GM_ERR_UNSUPPORTED: return "unsupported";
+    case GM_ERR_TIMEOUT: return "timeout";
+    case GM_ERR_STATE: return "invalid state";
+    default: return "unknown status";
+    }
+}
+
+const char* gm_version(void) { return "gpumesh_gb300 sm_103a " __DATE__; }
+
+gm_status gm_node_groups_build(uint32_t nv, const int32_t* cid, uint32_t nt, const uint32_t* tets, uint32_t np,
+                               const uint32_t* pris, uint32_t nh, const uint32_t* hexs, int32_t permute, uint32_t* perm,
+                               uint32_t* group_base, uint32_t* members, uint32_t* ranges, uint32_t* ngroups)
+{
+    return guarded([&] {
+        require(nv > 0 && cid && perm && group_base && members && ngroups, "null argument");
+        check_conn(tets, (size_t)nt * 4, nv, "tet");
+        check_conn(pris, (size_t)np * 6, nv, "prism");
+        check_conn(hexs, (size_t)nh * 8, nv, "hex");
+        HostMeshView in;
+        in.nv = nv;
+        in.nt = nt;
+        in.np = np;
+        in.nh = nh;
+        in.cid = cid;
+        in.tets = tets;
+        in.pris = pris;
+        in.hexs = hexs;
+        Topology t = build_topology(in, permute != 0);
+        std::copy(t.perm.begin(), t.perm.end(), perm);
+        std::copy(t.group_base.begin(), t.group_base.end(), group_base);
+        std::copy(t.members.begin(), t.members.end(), members);
+        if (ranges) std::copy(t.ranges.begin(), t.ranges.end(), ranges);
+        *ngroups = (uint32_t)(t.group_base.size() - 1);
+    });
+}
+
+gm_status gm_mesh_create(gm_mesh** out)
+{
+    return guarded([&] {
+        require(out != nullptr, "null output");
+        gm_mesh* m = new gm_mesh();
+        try
+        {
+            GM_CUDA(cudaGetDevice(&m->device));
+            GM_CUDA(cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device));
+            m->ctr.reserve(1);
+            GM_CUDA(cudaMemset(m->ctr.p, 0, sizeof(Counters)));
+            set_crew(m, GM_SAMPLER_UNIFORM, GM_MEASURER_METRIC_FREE, GM_EVALUATOR_MEAN_RATIO, 1.0, 1.0);
+        }
+        catch (...)
+        {
+            delete m;
+            throw;
+        }
+        *out = m;
+    });
+}
+
+gm_status gm_mesh_destroy(gm_mesh* m)
+{
+    return guarded([&] {
+        if (!m) return;
+        cudaStreamSynchronize(m->stream);
+        m->pos.release();
+        m->tets.release();
+        m->pris.release();
+        m->hexs.release();
+        m->ve_off.release();
+        m->ve.release();
+        m->vv_off.release();
+        m->vv.release();
+        m->cid.release();
+        m->con.release();
+        m->members.release();
+        m->quality.release();
+        m->parts.release();
+        m->corners.release();
+        m->saved.release();
+        m->ctr.release();
+        m->def_v.release();
+        m->def_old.release();
+        m->def_new.release();
+        m->def_count.release();
+        delete m;
+    });
+}
+
+gm_status gm_mesh_set_stream(gm_mesh* m, void* stream)
+{
+    return guarded([&] {
+        require(m != nullptr, "null mesh");
+        m->stream = (cudaStream_t)stream;
+    });
+}
+
+gm_status gm_mesh_sync(gm_mesh* m)
+{
+    return guarded([&] {
+        require(m != nullptr, "null mesh");
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+gm_status gm_mesh_upload(gm_mesh* m, uint32_t nv, const double* xyz, const int32_t* cid, uint32_t nt,
+                         const uint32_t* tets, uint32_t np, const uint32_t* pris, uint32_t nh, const uint32_t* hexs)
+{
+    return guarded([&] {
+        require(m && xyz && cid && nv > 0, "null argument");
+        require((nt == 0 || tets) && (np == 0 || pris) && (nh == 0 || hexs), "null connectivity");
+        require((uint64_t)nt + np + nh <= kMaxElemId, "too many elements");
+        check_conn(tets, (size_t)nt * 4, nv, "tet");
+        check_conn(pris, (size_t)np * 6, nv, "prism");
+        check_conn(hexs, (size_t)nh * 8, nv, "hex");
+        HostMeshView in;
+        in.nv = nv;
+        in.nt = nt;
+        in.np = np;
+        in.nh = nh;
+        in.cid = cid;
+        in.tets = tets;
+        in.pris = pris;
+        in.hexs = hexs;
+        std::vector<uint32_t> ve_off, ve, vv_off, vv;
+        build_csr(in, ve_off, ve, vv_off, vv);
+        upload_positions(m, nv, xyz);
+        upload(m->cid, cid, nv, m->stream);
+        m->nt = nt;
+        m->np = np;
+        m->nh = nh;
+        upload(m->tets, reinterpret_cast<const uint4*>(tets), nt, m->stream);
+        upload(m->pris, pris, (size_t)np * 6, m->stream);
+        upload(m->hexs, reinterpret_cast<const uint4*>(hexs), (size_t)nh * 2, m->stream);
+        upload_csr(m, ve_off, ve, vv_off, vv);
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+gm_status gm_mesh_upload_verts(gm_mesh* m, uint32_t nv, const double* xyz)
+{
+    return guarded([&] {
+        require(m && xyz, "null argument");
+        require(m->nv == 0 || m->nv == nv, "vertex count differs from the uploaded topology");
+        upload_positions(m, nv, xyz);
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+gm_status gm_mesh_upload_gpu_verts(gm_mesh* m, uint32_t nv, const void* gpu_verts)
+{
+    return guarded([&] {
+        require(m && gpu_verts, "null argument");
+        require(m->nv == 0 || m->nv == nv, "vertex count differs from the uploaded topology");
+        upload(m->pos, reinterpret_cast<const float4*>(gpu_verts), nv, m->stream);
+        m->nv = nv;
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+#define GM_UPLOAD_ELEMS(NAME, K, FIELD, COUNT, VEC)                                                       \
+    gm_status NAME(gm_mesh* m, uint32_t n, const uint32_t* words, uint32_t stride)                       \
+    {                                                                                                    \
+        return guarded([&] {                                                                             \
+            require(m && (n == 0 || words), "null argument");                                            \
+            std::vector<uint32_t> packed;                                                                \
+            upload_conn<K>(m, n, words, stride, packed);                                                 \
+            if (m->nv) check_conn(packed.data(), packed.size(), m->nv, #FIELD);                          \
+            upload(m->FIELD, reinterpret_cast<const VEC*>(packed.data()), packed.size() * 4 / (sizeof(VEC)), \
+                   m->stream);                                                                           \
+            m->COUNT = n;                                                                                \
+            GM_CUDA(cudaStreamSynchronize(m->stream));                                                   \
+        });                                                                                              \
+    }
+GM_UPLOAD_ELEMS(gm_mesh_upload_tets, 4, tets, nt, uint4)
+GM_UPLOAD_ELEMS(gm_mesh_upload_pris, 6, pris, np, uint32_t)
+GM_UPLOAD_ELEMS(gm_mesh_upload_hexs, 8, hexs, nh, uint4)
+#undef GM_UPLOAD_ELEMS
+
+gm_status gm_mesh_upload_topo(gm_mesh* m, uint32_t nv, const int32_t* topo5, uint32_t n_nv, const uint32_t* neig_verts,
+                              uint32_t n_ne, const int32_t* neig_elems3)
+{
+    return guarded([&] {
+        require(m && topo5 && (n_nv == 0 || neig_verts) && (n_ne == 0 || neig_elems3), "null argument");
+        require(m->nv == 0 || m->nv == nv, "vertex count differs from the uploaded vertices");
+        std::vector<int32_t> cid(nv);
+        std::vector<uint32_t> ve_off((size_t)nv + 1, 0), vv_off((size_t)nv + 1, 0), ve, vv;
+        ve.reserve(n_ne);
+        vv.reserve(n_nv);
+        for (uint32_t v = 0; v < nv; ++v)
+        {
+            const int32_t* t = topo5 + 5 * (size_t)v;
+            cid[v] = t[0];
+            uint32_t vb = (uint32_t)t[1], vc = (uint32_t)t[2], eb = (uint32_t)t[3], ec = (uint32_t)t[4];
+            require((uint64_t)vb + vc <= n_nv && (uint64_t)eb + ec <= n_ne, "topology range out of bounds");
+            for (uint32_t i = 0; i < vc; ++i)
+            {
+                require(neig_verts[vb + i] < nv, "neighbour vertex out of range");
+                vv.push_back(neig_verts[vb + i]);
+            }
+            for (uint32_t i = 0; i < ec; ++i)
+            {
+                const int32_t* ne = neig_elems3 + 3 * (size_t)(eb + i);
+                require(ne[1] == GM_TET || ne[1] == GM_PRI || ne[1] == GM_HEX, "unsupported neighbour element type");
+                require(ne[2] >= 0 && ne[2] < 8 && (uint32_t)ne[0] <= kMaxElemId, "neighbour element out of range");
+                ve.push_back(pack_elem_ref(ne[1], ne[2], (uint32_t)ne[0]));
+            }
+            vv_off[v + 1] = (uint32_t)vv.size();
+            ve_off[v + 1] = (uint32_t)ve.size();
+        }
+        upload(m->cid, cid.data(), nv, m->stream);
+        m->nv = nv;
+        upload_csr(m, ve_off, ve, vv_off, vv);
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+gm_status gm_mesh_upload_groups(gm_mesh* m, uint32_t n_members, const uint32_t* members, uint32_t ngroups,
+                                const uint32_t* group_base)
+{
+    return guarded([&] {
+        require(m && (n_members == 0 || members) && group_base, "null argument");
+        require(group_base[0] == 0 && group_base[ngroups] == n_members, "group bases must span the members");
+        for (uint32_t g = 0; g < ngroups; ++g) require(group_base[g] <= group_base[g + 1], "group bases must ascend");
+        for (uint32_t i = 0; i < n_members; ++i) require(members[i] < m->nv, "group member out of range");
+        upload(m->members, members, n_members, m->stream);
+        m->n_members = n_members;
+        m->group_base.assign(group_base, group_base + ngroups + 1);
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+gm_status gm_mesh_set_constraints(gm_mesh* m, uint32_t n, const int32_t* kind, const double* params)
+{
+    return guarded([&] {
+        require(m && kind && params && n > 0, "null argument");
+        std::vector<Constraint> table(n);
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            Constraint& c = table[i];
+            std::memset(&c, 0, sizeof(c));
+            c.kind = kind[i];
+            require(c.kind >= GM_CON_VOLUME && c.kind <= GM_CON_POINT, "unknown constraint kind");
+            const double* p = params + 6 * (size_t)i;
+            double a[3] = {p[0], p[1], p[2]}, b[3] = {p[3], p[4], p[5]}, u[3] = {0, 0, 0}, len = 0;
+            if (c.kind == GM_CON_PLANE)
+            {
+                // PlaneConstraint normalizes its normal (FaceConstraint.cpp:172-176)
+                double s = 1.0 / std::sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+                for (int k = 0; k < 3; ++k) b[k] *= s;
+            }
+            else if (c.kind == GM_CON_SEGMENT)
+            {
+                // SegmentConstraint keeps the unit direction and length (EdgeConstraint.cpp:176-181)
+                double d[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+                double l2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                double s = 1.0 / std::sqrt(l2);
+                for (int k = 0; k < 3; ++k) u[k] = d[k] * s;
+                len = std::sqrt(l2);
+            }
+            for (int k = 0; k < 3; ++k)
+            {
+                c.a[k] = (float)a[k];
+                c.b[k] = (float)b[k];
+                c.u[k] = (float)u[k];
+                c.ad[k] = a[k];
+                c.bd[k] = b[k];
+                c.ud[k] = u[k];
+            }
+            c.len = (float)len;
+            c.lend = len;
+        }
+        upload(m->con, table.data(), n, m->stream);
+        m->ncon = (int)n;
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+gm_status gm_mesh_set_crew(gm_mesh* m, int32_t sampler, int32_t measurer, int32_t evaluator, double scaling,
+                           double aspect_ratio)
+{
+    return guarded([&] {
+        require(m != nullptr, "null mesh");
+        set_crew(m, sampler, measurer, evaluator, scaling, aspect_ratio);
+    });
+}
+
+gm_status gm_mesh_save_positions(gm_mesh* m)
+{
+    return guarded([&] {
+        require_mesh(m);
+        m->saved.reserve(m->nv);
+        GM_CUDA(cudaMemcpyAsync(m->saved.p, m->pos.p, m->nv * sizeof(float4), cudaMemcpyDeviceToDevice, m->stream));
+    });
+}
+
+gm_status gm_mesh_restore_positions(gm_mesh* m)
+{
+    return guarded([&] {
+        require_mesh(m);
+        require(m->saved.p != nullptr && m->saved.cap >= m->nv, "no saved positions");
+        GM_CUDA(cudaMemcpyAsync(m->pos.p, m->saved.p, m->nv * sizeof(float4), cudaMemcpyDeviceToDevice, m->stream));
+    });
+}
+
+gm_status gm_mesh_fetch_verts(gm_mesh* m, uint32_t nv, double* xyz)
+{
+    return guarded([&] {
+        require(m && xyz, "null argument");
+        require(nv == m->nv, "vertex count mismatch");
+        m->staging.resize(nv);
+        GM_CUDA(cudaMemcpyAsync(m->staging.data(), m->pos.p, nv * sizeof(float4), cudaMemcpyDeviceToHost, m->stream));
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+        for (uint32_t v = 0; v < nv; ++v)
+        {
+            xyz[3 * (size_t)v] = m->staging[v].x;
+            xyz[3 * (size_t)v + 1] = m->staging[v].y;
+            xyz[3 * (size_t)v + 2] = m->staging[v].z;
+        }
+    });
+}
+
+gm_status gm_mesh_fetch_gpu_verts(gm_mesh* m, uint32_t nv, void* gpu_verts)
+{
+    return guarded([&] {
+        require(m && gpu_verts, "null argument");
+        require(nv == m->nv, "vertex count mismatch");
+        GM_CUDA(cudaMemcpyAsync(gpu_verts, m->pos.p, nv * sizeof(float4), cudaMemcpyDeviceToHost, m->stream));
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+gm_status gm_evaluate_async(gm_mesh* m, uint32_t slot)
+{
+    return guarded([&] {
+        require_mesh(m);
+        require(slot < 65536, "quality slot out of range");
+        if (slot >= m->n_quality_slots)
+        {
+            // grow, keeping the recorded slots
+            uint32_t n = std::max<uint32_t>(slot + 1, 2 * m->n_quality_slots);
+            Quality* fresh = nullptr;
+            GM_CUDA(cudaMalloc(&fresh, n * sizeof(Quality)));
+            if (m->quality.p && m->n_quality_slots)
+                GM_CUDA(cudaMemcpyAsync(fresh, m->quality.p, m->n_quality_slots * sizeof(Quality),
+                                        cudaMemcpyDeviceToDevice, m->stream));
+            GM_CUDA(cudaStreamSynchronize(m->stream));
+            m->quality.release();
+            m->quality.p = fresh;
+            m->quality.cap = n;
+            m->n_quality_slots = n;
+        }
+        uint32_t total = m->nt + m->np + m->nh;
+        int nb = evaluate_blocks(total, m->sm_count);
+        m->parts.reserve(nb);
+        GM_CUDA(launch_evaluate(m->variant(), m->maxk(), m->view(), m->crew, m->parts.p, nb, m->quality.p + slot,
+                                m->stream));
+    });
+}
+
+gm_status gm_quality_read(gm_mesh* m, uint32_t slot, gm_quality* out)
+{
+    return guarded([&] {
+        require(m && out, "null argument");
+        require(slot < m->n_quality_slots, "quality slot never evaluated");
+        static_assert(sizeof(Quality) == sizeof(gm_quality), "quality layout");
+        GM_CUDA(cudaMemcpyAsync(out, m->quality.p + slot, sizeof(Quality), cudaMemcpyDeviceToHost, m->stream));
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+gm_status gm_evaluate(gm_mesh* m, gm_quality* out)
+{
+    gm_status s = gm_evaluate_async(m, 0);
+    if (s != GM_OK) return s;
+    return gm_quality_read(m, 0, out);
+}
+
+gm_status gm_smooth_group(gm_mesh* m, int32_t smoother, const double* params, uint32_t base, uint32_t count)
+{
+    return guarded([&] {
+        require_mesh(m);
+        require((uint64_t)base + count <= m->n_members, "group slice outside the uploaded members");
+        require(smoother != GM_SMOOTH_GETME, "GETMe relocates through gm_getme_elements / gm_getme_update_group");
+        SmoothParams sp = parse_params(smoother, params);
+        ensure_deferred(m);
+        uint32_t slot = (uint32_t)m->group_base.size();
+        GM_CUDA(cudaMemsetAsync(m->def_count.p + slot, 0, sizeof(uint32_t), m->stream));
+        relocate_group(m, smoother, sp, base, count, slot);
+    });
+}
+
+gm_status gm_getme_elements(gm_mesh* m, const double* params)
+{
+    return guarded([&] {
+        require_mesh(m);
+        SmoothParams sp = parse_params(GM_SMOOTH_GETME, params);
+        m->corners.reserve(4 * (size_t)m->nt + 6 * (size_t)m->np + 8 * (size_t)m->nh);
+        GM_CUDA(launch_getme_elements(m->element_variant(), m->view(), m->crew, sp.lambda, m->corners.p, m->sm_count,
+                                      m->stream));
+    });
+}
+
+gm_status gm_getme_update_group(gm_mesh* m, const double* params, uint32_t base, uint32_t count)
+{
+    return guarded([&] {
+        require_mesh(m);
+        require(m->corners.p != nullptr, "gm_getme_elements must run before the vertex update");
+        require((uint64_t)base + count <= m->n_members, "group slice outside the uploaded members");
+        SmoothParams sp = parse_params(GM_SMOOTH_GETME, params);
+        ensure_deferred(m);
+        uint32_t slot = (uint32_t)m->group_base.size();
+        GM_CUDA(cudaMemsetAsync(m->def_count.p + slot, 0, sizeof(uint32_t), m->stream));
+        relocate_group(m, GM_SMOOTH_GETME, sp, base, count, slot);
+    });
+}
+
+gm_status gm_smooth_pass(gm_mesh* m, int32_t smoother, const double* params)
+{
+    return guarded([&] {
+        require_mesh(m);
+        require_groups(m);
+        SmoothParams sp = parse_params(smoother, params);
+        ensure_deferred(m);
+        size_t ng = m->group_base.size() - 1;
+        GM_CUDA(cudaMemsetAsync(m->def_count.p, 0, (ng + 2) * sizeof(uint32_t), m->stream));
+        if (smoother == GM_SMOOTH_GETME)
+        {
+            m->corners.reserve(4 * (size_t)m->nt + 6 * (size_t)m->np + 8 * (size_t)m->nh);
+            GM_CUDA(launch_getme_elements(m->element_variant(), m->view(), m->crew, sp.lambda, m->corners.p,
+                                          m->sm_count, m->stream));
+        }
+        for (size_t g = 0; g < ng; ++g)
+            relocate_group(m, smoother, sp, m->group_base[g], m->group_base[g + 1] - m->group_base[g], (uint32_t)g);
+    });
+}
+
+gm_status gm_mesh_counters(gm_mesh* m, uint64_t* out5, int32_t reset)
+{
+    return guarded([&] {
+        require(m && out5, "null argument");
+        Counters c;
+        GM_CUDA(cudaMemcpyAsync(&c, m->ctr.p, sizeof(c), cudaMemcpyDeviceToHost, m->stream));
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+        out5[0] = c.patch_evals;
+        out5[1] = c.elem_evals[0];
+        out5[2] = c.elem_evals[2];
+        out5[3] = c.elem_evals[3];
+        out5[4] = c.fp64_vertices;
+        if (reset) GM_CUDA(cudaMemsetAsync(m->ctr.p, 0, sizeof(Counters), m->stream));
+    });
+}
+
+gm_status gm_probe_fp32_tflops(double* tflops)
+{
+    return guarded([&] {
+        require(tflops != nullptr, "null output");
+        int dev = 0, sms = 0;
+        GM_CUDA(cudaGetDevice(&dev));
+        GM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        float* sink = nullptr;
+        GM_CUDA(cudaMalloc(&sink, sizeof(float) * 1024));
+        cudaEvent_t a, b;
+        GM_CUDA(cudaEventCreate(&a));
+        GM_CUDA(cudaEventCreate(&b));
+        const int iters = 1 << 14, blocks = sms * 8, threads = 256;
+        GM_CUDA(launch_ffma_probe(blocks, threads, iters, sink, 0));  // warm-up
+        GM_CUDA(cudaEventRecord(a, 0));
+        GM_CUDA(launch_ffma_probe(blocks, threads, iters, sink, 0));
+        GM_CUDA(cudaEventRecord(b, 0));
+        GM_CUDA(cudaEventSynchronize(b));
+        float ms = 0;
+        GM_CUDA(cudaEventElapsedTime(&ms, a, b));
+        // 8 independent FFMA chains per thread, 2 flops each
+        double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
+        *tflops = flops / (ms * 1e-3) / 1e12;
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        cudaFree(sink);
+    });
+}
+
+}  // extern "C"

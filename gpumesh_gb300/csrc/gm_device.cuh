@@ -1,0 +1,565 @@
+// Device-side data views, geometry and quality measures for sm_103a.
+//
+// Every measure is a template on the arithmetic type: the relocation and
+// evaluation kernels run them in FP32, and the acceptance test on
+// near-degenerate patches re-runs them in FP64.  The formulas restate the
+// reference's CPU measures:
+//   mean ratio       Evaluators/MeanRatioEvaluator.cpp:22-167
+//   metric conform.  Evaluators/MetricConformityEvaluator.cpp:25-224
+//   measurers        Measurers/MetricFreeMeasurer.cpp:27-105,
+//                    Measurers/MetricWiseMeasurer.cpp:64-188
+//   samplers         Samplers/UniformSampler.cpp:45, AbstractSampler.cpp:190-208
+//   projections      Boundaries/Constraints/{Face,Edge,Vertex,Volume}Constraint.cpp,
+//                    Boundaries/SphereBoundary.cpp:42-45
+// Positive element qualities are carried as reciprocals (1/q), which is all
+// a harmonic mean needs, so the common path has no division.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gm {
+
+constexpr int kTet = 0;
+constexpr int kPri = 2;
+constexpr int kHex = 3;
+
+enum : int { kSamplerUniform = 0, kSamplerAnalytic = 1, kSamplerSine = 2 };
+enum : int { kMeasurerMetricFree = 0, kMeasurerMetricWise = 1 };
+enum : int { kEvalMeanRatio = 0, kEvalMetricConformity = 1 };
+enum : int { kConVolume = 0, kConPlane = 1, kConSegment = 2, kConSphere = 3, kConPoint = 4 };
+
+// smoothing-wide parameters, passed by value to every kernel
+struct Crew
+{
+    int sampler, measurer, evaluator, pad;
+    double scaling, scaling2, scaling3, aspect;
+    double rot[9], rotinv[9];  // column-major, AbstractSampler::_rotMat / _rotInv
+};
+
+// one boundary constraint (index = constraint id)
+struct Constraint
+{
+    int kind;
+    float a[3];  // plane point / segment start / point
+    float b[3];  // plane normal (normalized) / segment end
+    float u[3];  // segment direction (normalized)
+    float len;   // segment length
+    double ad[3], bd[3], ud[3];
+    double lend;
+};
+
+// read-only device view of one mesh
+struct MeshView
+{
+    uint32_t nv, nt, np, nh;
+    float4* pos;
+    const uint4* tets;
+    const uint32_t* pris;  // 6 per prism
+    const uint4* hexs;     // 2 per hex
+    const uint32_t* ve_off;
+    const uint32_t* ve;    // packed (type, local, id)
+    const uint32_t* vv_off;
+    const uint32_t* vv;
+    const int32_t* cid;
+    const Constraint* con;
+    int ncon;
+};
+
+__device__ __forceinline__ int ref_type(uint32_t r) { return (int)(r >> 30); }
+__device__ __forceinline__ int ref_local(uint32_t r) { return (int)((r >> 27) & 7u); }
+__device__ __forceinline__ uint32_t ref_id(uint32_t r) { return r & ((1u << 27) - 1); }
+
+// ---------------------------------------------------------------------------
+// small vector algebra
+// ---------------------------------------------------------------------------
+template <class R>
+struct V3
+{
+    R x, y, z;
+};
+template <class R> __device__ __forceinline__ V3<R> mk(R x, R y, R z) { return V3<R>{x, y, z}; }
+template <class R> __device__ __forceinline__ V3<R> operator+(V3<R> a, V3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class R> __device__ __forceinline__ V3<R> operator-(V3<R> a, V3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class R> __device__ __forceinline__ V3<R> operator-(V3<R> a) { return {-a.x, -a.y, -a.z}; }
+template <class R> __device__ __forceinline__ V3<R> operator*(V3<R> a, R s) { return {a.x * s, a.y * s, a.z * s}; }
+template <class R> __device__ __forceinline__ R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class R> __device__ __forceinline__ V3<R> cross(V3<R> a, V3<R> b)
+{
+    return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+}
+template <class R> __device__ __forceinline__ R det3(V3<R> c0, V3<R> c1, V3<R> c2)
+{
+    // determinant of the matrix with columns c0, c1, c2
+    return c0.x * (c1.y * c2.z - c2.y * c1.z) - c1.x * (c0.y * c2.z - c2.y * c0.z) + c2.x * (c0.y * c1.z - c1.y * c0.z);
+}
+template <class R> __device__ __forceinline__ R rsqrt_(R x);
+template <> __device__ __forceinline__ float rsqrt_<float>(float x) { return rsqrtf(x); }
+template <> __device__ __forceinline__ double rsqrt_<double>(double x) { return rsqrt(x); }
+template <class R> __device__ __forceinline__ R sqrt_(R x);
+template <> __device__ __forceinline__ float sqrt_<float>(float x) { return sqrtf(x); }
+template <> __device__ __forceinline__ double sqrt_<double>(double x) { return sqrt(x); }
+template <class R> __device__ __forceinline__ V3<R> normalize(V3<R> a) { return a * rsqrt_<R>(dot(a, a)); }
+template <class R> __device__ __forceinline__ R length(V3<R> a) { return sqrt_<R>(dot(a, a)); }
+
+// |x|^(-2/3) for x != 0, and |x|^(2/3)
+__device__ __forceinline__ float pow_m23(float x) { return exp2f(-0.666666666666666667f * __log2f(fabsf(x))); }
+__device__ __forceinline__ double pow_m23(double x) { return pow(fabs(x), -2.0 / 3.0); }
+__device__ __forceinline__ float pow_23(float x) { return exp2f(0.666666666666666667f * __log2f(fabsf(x))); }
+__device__ __forceinline__ double pow_23(double x) { return pow(fabs(x), 2.0 / 3.0); }
+__device__ __forceinline__ float cbrt_(float x) { return cbrtf(x); }
+__device__ __forceinline__ double cbrt_(double x) { return cbrt(x); }
+
+template <class R> __device__ __forceinline__ R sgn(R x) { return (R)((R(0) < x) - (x < R(0))); }
+
+// symmetric 3x3 metric
+template <class R>
+struct Sym3
+{
+    R xx, yy, zz, xy, xz, yz;
+};
+
+template <class R> __device__ __forceinline__ V3<R> to(float4 p) { return {(R)p.x, (R)p.y, (R)p.z}; }
+
+// ---------------------------------------------------------------------------
+// samplers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float sinpi_(float x) { return sinpif(x); }
+__device__ __forceinline__ double sinpi_(double x) { return sinpi(x); }
+
+// AbstractSampler::vertMetric (Samplers/AbstractSampler.cpp:190-208):
+// R^T diag(sx^2, s^2, s^2) R with sx = s * a^(((1 - cos(2.5 pi (Rp).x))/2)^a)
+template <class R>
+__device__ __noinline__ Sym3<R> analytic_metric(const Crew& c, V3<R> p)
+{
+    const double* m = c.rot;
+    R rx = (R)m[0] * p.x + (R)m[3] * p.y + (R)m[6] * p.z;
+    R x = rx * R(2.5 * 3.14159265358979323846);
+    R a = (R)c.aspect;
+    R cc = (R(1) - cos(x)) / R(2);
+    R sizeX = (R)c.scaling * pow(a, pow(cc, a));
+    R Mx = sizeX * sizeX, My = (R)c.scaling2;
+    // rows of R are (m[0],m[3],m[6]), (m[1],m[4],m[7]), (m[2],m[5],m[8]); M = sum_i d_i r_i r_i^T
+    R r0[3] = {(R)m[0], (R)m[3], (R)m[6]};
+    R r1[3] = {(R)m[1], (R)m[4], (R)m[7]};
+    R r2[3] = {(R)m[2], (R)m[5], (R)m[8]};
+    Sym3<R> M;
+    M.xx = Mx * r0[0] * r0[0] + My * (r1[0] * r1[0] + r2[0] * r2[0]);
+    M.yy = Mx * r0[1] * r0[1] + My * (r1[1] * r1[1] + r2[1] * r2[1]);
+    M.zz = Mx * r0[2] * r0[2] + My * (r1[2] * r1[2] + r2[2] * r2[2]);
+    M.xy = Mx * r0[0] * r0[1] + My * (r1[0] * r1[1] + r2[0] * r2[1]);
+    M.xz = Mx * r0[0] * r0[2] + My * (r1[0] * r1[2] + r2[0] * r2[2]);
+    M.yz = Mx * r0[1] * r0[2] + My * (r1[1] * r1[2] + r2[1] * r2[2]);
+    return M;
+}
+
+template <class R>
+__device__ __forceinline__ Sym3<R> metric_at(const Crew& c, V3<R> p)
+{
+    if (c.sampler == kSamplerSine)
+    {
+        // s^2 * diag(1 + 9 sin^2(4 pi x), 1, 1)
+        R s = sinpi_(R(4) * p.x);
+        R s2 = (R)c.scaling2;
+        return {s2 * (R(1) + R(9) * s * s), s2, s2, R(0), R(0), R(0)};
+    }
+    if (c.sampler == kSamplerAnalytic) return analytic_metric(c, p);
+    R s2 = (R)c.scaling2;
+    return {s2, s2, s2, R(0), R(0), R(0)};
+}
+
+template <class R> __device__ __forceinline__ R quad_form(const Sym3<R>& M, V3<R> v)
+{
+    return v.x * (M.xx * v.x + M.xy * v.y + M.xz * v.z) + v.y * (M.xy * v.x + M.yy * v.y + M.yz * v.z) +
+           v.z * (M.xz * v.x + M.yz * v.y + M.zz * v.z);
+}
+
+// ---------------------------------------------------------------------------
+// measurers
+// ---------------------------------------------------------------------------
+
+// MetricWiseMeasurer::riemannianDistance, localized segment division
+// (Measurers/MetricWiseMeasurer.cpp:64-116), with the subdivision depth
+// bounded at 2^16 segments so that a pathological metric cannot loop forever.
+template <class R>
+__device__ __noinline__ R metric_wise_distance(const Crew& c, V3<R> a, V3<R> b)
+{
+    int curr = 0, base = 2;
+    R len = 0;
+    V3<R> d = b - a;
+    V3<R> bv = d * (R(1) / (R)base);
+    for (int guard = 0; curr < base && guard < 4096; ++guard)
+    {
+        R p0 = (R(curr) + R(0.5)) / (R)base;
+        R p1 = (R(curr) + R(1.5)) / (R)base;
+        R l0 = sqrt_<R>(quad_form(metric_at(c, a + d * p0), bv));
+        R l1 = sqrt_<R>(quad_form(metric_at(c, a + d * p1), bv));
+        R sum = l0 + l1;
+        R diff = fabs(l0 - l1) / (sum / R(2));
+        if (diff < R(0.01) || base >= (1 << 16))
+        {
+            len += sum;
+            curr += 2;
+            if ((curr & 2) == 0)
+            {
+                base >>= 1;
+                curr >>= 1;
+            }
+            bv = d * (R(1) / (R)base);
+        }
+        else
+        {
+            base <<= 1;
+            curr <<= 1;
+            bv = bv * R(0.5);
+        }
+    }
+    return len;
+}
+
+// crew variants the kernels are specialised on: evaluator x measurer
+enum : int { kVarMRFree = 0, kVarMRWise = 1, kVarMC = 2, kVarMCWise = 3 };
+template <int VAR> struct VarTraits
+{
+    static constexpr bool mean_ratio = VAR == kVarMRFree || VAR == kVarMRWise;
+    static constexpr bool metric_wise = VAR == kVarMRWise || VAR == kVarMCWise;
+};
+
+template <int VAR, class R>
+__device__ __forceinline__ V3<R> segment(const Crew& c, V3<R> a, V3<R> b)
+{
+    if (VarTraits<VAR>::metric_wise) return normalize(b - a) * metric_wise_distance(c, a, b);
+    return (b - a) * (R)c.scaling;
+}
+
+// ---------------------------------------------------------------------------
+// element quality.  EQ carries 1/q when the element is valid (q > 0) and q
+// itself otherwise.
+// ---------------------------------------------------------------------------
+template <class R>
+struct EQ
+{
+    R v;       // 1/q if pos, else q
+    bool pos;  // q > 0
+};
+
+// mean-ratio corner: q = sign(det) 3 |det|^(2/3) / |F|^2
+template <class R>
+__device__ __forceinline__ void mr_corner(V3<R> c0, V3<R> c1, V3<R> c2, R& rq, R& q, bool& pos)
+{
+    R det = det3(c0, c1, c2);
+    R f2 = dot(c0, c0) + dot(c1, c1) + dot(c2, c2);
+    pos = det > R(0);
+    if (pos)
+        rq = f2 * pow_m23(det) * R(1.0 / 3.0);
+    else
+        q = sgn(det) * R(3) * pow_23(det) / f2;
+}
+
+// Fr_TET_INV applied on the right of [e03 e13 e23] (AbstractEvaluator.cpp:28-31)
+template <class R>
+__device__ __forceinline__ void tet_frame(V3<R> e03, V3<R> e13, V3<R> e23, V3<R>& c0, V3<R>& c1, V3<R>& c2)
+{
+    c0 = e03;
+    c1 = e03 * R(-0.5773502691896257645091) + e13 * R(1.154700538379251529018);
+    c2 = e03 * R(-0.4082482904638630163662) + e13 * R(-0.4082482904638630163662) + e23 * R(1.224744871391589049099);
+}
+// Fr_PRI_INV (AbstractEvaluator.cpp:32-35)
+template <class R>
+__device__ __forceinline__ void pri_frame(V3<R> a, V3<R> b, V3<R> e, V3<R>& c0, V3<R>& c1, V3<R>& c2)
+{
+    c0 = a;
+    c1 = a * R(-0.5773502691896257645091) + b * R(1.154700538379251529018);
+    c2 = e;
+}
+
+template <class R>
+__device__ __forceinline__ EQ<R> combine(const R* rq, const R* q, const bool* pos, int n)
+{
+    bool all = true;
+    for (int i = 0; i < n; ++i) all = all && pos[i];
+    EQ<R> r;
+    if (all)
+    {
+        R s = 0;
+        for (int i = 0; i < n; ++i) s += rq[i];
+        r.v = s / R(n);
+        r.pos = true;
+    }
+    else
+    {
+        // min over corners; valid corners need their q = 1/rq
+        R mn = pos[0] ? R(1) / rq[0] : q[0];
+        for (int i = 1; i < n; ++i)
+        {
+            R qi = pos[i] ? R(1) / rq[i] : q[i];
+            mn = qi < mn ? qi : mn;
+        }
+        r.v = mn;
+        r.pos = mn > R(0);
+        if (r.pos) r.v = R(1) / mn;
+    }
+    return r;
+}
+
+template <int VAR, class R>
+__device__ __forceinline__ EQ<R> mr_tet(const Crew& c, const V3<R>* p)
+{
+    V3<R> c0, c1, c2;
+    tet_frame(segment<VAR, R>(c, p[0], p[3]), segment<VAR, R>(c, p[1], p[3]), segment<VAR, R>(c, p[2], p[3]), c0, c1, c2);
+    R rq = 0, q = 0;
+    bool pos;
+    mr_corner(c0, c1, c2, rq, q, pos);
+    return EQ<R>{pos ? rq : q, pos};
+}
+
+template <int VAR, class R>
+__device__ __forceinline__ EQ<R> mr_pri(const Crew& c, const V3<R>* p)
+{
+    V3<R> e03 = segment<VAR, R>(c, p[0], p[3]), e14 = segment<VAR, R>(c, p[1], p[4]), e25 = segment<VAR, R>(c, p[2], p[5]);
+    V3<R> e01 = segment<VAR, R>(c, p[0], p[1]), e12 = segment<VAR, R>(c, p[1], p[2]), e20 = segment<VAR, R>(c, p[2], p[0]);
+    V3<R> e34 = segment<VAR, R>(c, p[3], p[4]), e45 = segment<VAR, R>(c, p[4], p[5]), e53 = segment<VAR, R>(c, p[5], p[3]);
+    R rq[6], q[6];
+    bool pos[6];
+    V3<R> a, b, d;
+    pri_frame(-e01, e20, e03, a, b, d); mr_corner(a, b, d, rq[0], q[0], pos[0]);
+    pri_frame(-e12, e01, e14, a, b, d); mr_corner(a, b, d, rq[1], q[1], pos[1]);
+    pri_frame(-e20, e12, e25, a, b, d); mr_corner(a, b, d, rq[2], q[2], pos[2]);
+    pri_frame(-e34, e53, e03, a, b, d); mr_corner(a, b, d, rq[3], q[3], pos[3]);
+    pri_frame(-e45, e34, e14, a, b, d); mr_corner(a, b, d, rq[4], q[4], pos[4]);
+    pri_frame(-e53, e45, e25, a, b, d); mr_corner(a, b, d, rq[5], q[5], pos[5]);
+    return combine(rq, q, pos, 6);
+}
+
+template <int VAR, class R>
+__device__ __forceinline__ EQ<R> mr_hex(const Crew& c, const V3<R>* p)
+{
+    V3<R> e01 = segment<VAR, R>(c, p[0], p[1]), e03 = segment<VAR, R>(c, p[0], p[3]), e04 = segment<VAR, R>(c, p[0], p[4]);
+    V3<R> e12 = segment<VAR, R>(c, p[1], p[2]), e15 = segment<VAR, R>(c, p[1], p[5]), e23 = segment<VAR, R>(c, p[2], p[3]);
+    V3<R> e26 = segment<VAR, R>(c, p[2], p[6]), e37 = segment<VAR, R>(c, p[3], p[7]), e45 = segment<VAR, R>(c, p[4], p[5]);
+    V3<R> e47 = segment<VAR, R>(c, p[4], p[7]), e56 = segment<VAR, R>(c, p[5], p[6]), e67 = segment<VAR, R>(c, p[6], p[7]);
+    R rq[8], q[8];
+    bool pos[8];
+    mr_corner(e01, e04, -e03, rq[0], q[0], pos[0]);
+    mr_corner(e01, e12, e15, rq[1], q[1], pos[1]);
+    mr_corner(e12, e26, -e23, rq[2], q[2], pos[2]);
+    mr_corner(e03, e23, e37, rq[3], q[3], pos[3]);
+    mr_corner(e04, e45, e47, rq[4], q[4], pos[4]);
+    mr_corner(e15, -e56, e45, rq[5], q[5], pos[5]);
+    mr_corner(e26, e56, e67, rq[6], q[6], pos[6]);
+    mr_corner(e37, e67, -e47, rq[7], q[7], pos[7]);
+    return combine(rq, q, pos, 8);
+}
+
+// MetricConformityEvaluator::specifiedMetric: 5-point Keast rule
+template <class R>
+__device__ __forceinline__ Sym3<R> specified_metric(const Crew& c, V3<R> v0, V3<R> v1, V3<R> v2, V3<R> v3)
+{
+    const R H = R(0.5), Q = R((1.0 - 0.5) / 3.0);
+    Sym3<R> m0 = metric_at(c, (v0 + v1 + v2 + v3) * R(0.25));
+    Sym3<R> m1 = metric_at(c, v0 * H + v1 * Q + v2 * Q + v3 * Q);
+    Sym3<R> m2 = metric_at(c, v0 * Q + v1 * H + v2 * Q + v3 * Q);
+    Sym3<R> m3 = metric_at(c, v0 * Q + v1 * Q + v2 * H + v3 * Q);
+    Sym3<R> m4 = metric_at(c, v0 * Q + v1 * Q + v2 * Q + v3 * H);
+    const R a = R(-0.8), b = R(0.45);
+    Sym3<R> r;
+    r.xx = m0.xx * a + (m1.xx + m2.xx + m3.xx + m4.xx) * b;
+    r.yy = m0.yy * a + (m1.yy + m2.yy + m3.yy + m4.yy) * b;
+    r.zz = m0.zz * a + (m1.zz + m2.zz + m3.zz + m4.zz) * b;
+    r.xy = m0.xy * a + (m1.xy + m2.xy + m3.xy + m4.xy) * b;
+    r.xz = m0.xz * a + (m1.xz + m2.xz + m3.xz + m4.xz) * b;
+    r.yz = m0.yz * a + (m1.yz + m2.yz + m3.yz + m4.yz) * b;
+    return r;
+}
+
+template <class R>
+__device__ __forceinline__ Sym3<R> sym_inverse(const Sym3<R>& m)
+{
+    R c00 = m.yy * m.zz - m.yz * m.yz;
+    R c01 = m.xz * m.yz - m.xy * m.zz;
+    R c02 = m.xy * m.yz - m.xz * m.yy;
+    R det = m.xx * c00 + m.xy * c01 + m.xz * c02;
+    R id = R(1) / det;
+    Sym3<R> r;
+    r.xx = c00 * id;
+    r.xy = c01 * id;
+    r.xz = c02 * id;
+    r.yy = (m.xx * m.zz - m.xz * m.xz) * id;
+    r.yz = (m.xy * m.xz - m.xx * m.yz) * id;
+    r.zz = (m.xx * m.yy - m.xy * m.xy) * id;
+    return r;
+}
+
+// MetricConformityEvaluator::metricConformity: with F the corner matrix,
+// Mk^-1 = F F^T and Mk = (F F^T)^-1; tNc = Mk^-1 Ms + Ms^-1 Mk - 2I and
+// q = sign(det F) / sqrt(1 + |tNc|_F).  Returns 1/q for valid corners.
+template <class R>
+__device__ __forceinline__ void mc_corner(V3<R> c0, V3<R> c1, V3<R> c2, const Sym3<R>& Ms, R& rq, R& q, bool& pos)
+{
+    // A = F F^T, F has columns c0, c1, c2
+    Sym3<R> A;
+    A.xx = c0.x * c0.x + c1.x * c1.x + c2.x * c2.x;
+    A.yy = c0.y * c0.y + c1.y * c1.y + c2.y * c2.y;
+    A.zz = c0.z * c0.z + c1.z * c1.z + c2.z * c2.z;
+    A.xy = c0.x * c0.y + c1.x * c1.y + c2.x * c2.y;
+    A.xz = c0.x * c0.z + c1.x * c1.z + c2.x * c2.z;
+    A.yz = c0.y * c0.z + c1.y * c1.z + c2.y * c2.z;
+    R det = det3(c0, c1, c2);
+    Sym3<R> Mk = sym_inverse(A);
+    Sym3<R> Msi = sym_inverse(Ms);
+    // P = A Ms ; Qm = Msi Mk ; tNc = P + Qm - 2I
+    R t[9];
+#define GM_SYM(m, i, j) ((i) == (j) ? ((i) == 0 ? m.xx : (i) == 1 ? m.yy : m.zz) \
+    : (((i) + (j)) == 1 ? m.xy : ((i) + (j)) == 2 ? m.xz : m.yz))
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+        {
+            R pij = GM_SYM(A, i, 0) * GM_SYM(Ms, 0, j) + GM_SYM(A, i, 1) * GM_SYM(Ms, 1, j) + GM_SYM(A, i, 2) * GM_SYM(Ms, 2, j);
+            R qij = GM_SYM(Msi, i, 0) * GM_SYM(Mk, 0, j) + GM_SYM(Msi, i, 1) * GM_SYM(Mk, 1, j) + GM_SYM(Msi, i, 2) * GM_SYM(Mk, 2, j);
+            t[i * 3 + j] = pij + qij - (i == j ? R(2) : R(0));
+        }
+#undef GM_SYM
+    R f2 = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) f2 += t[i] * t[i];
+    if (isnan(f2))
+    {
+        pos = false;
+        q = R(0);
+        return;
+    }
+    R s = sgn(det);
+    pos = s > R(0);
+    R r = sqrt_<R>(R(1) + sqrt_<R>(f2));
+    if (pos) rq = r;
+    else q = s / r;
+}
+
+template <class R>
+__device__ __forceinline__ EQ<R> mc_tet(const Crew& c, const V3<R>* p)
+{
+    V3<R> c0, c1, c2;
+    tet_frame(p[3] - p[0], p[3] - p[1], p[3] - p[2], c0, c1, c2);
+    Sym3<R> Ms = specified_metric(c, p[0], p[1], p[2], p[3]);
+    R rq = 0, q = 0;
+    bool pos;
+    mc_corner(c0, c1, c2, Ms, rq, q, pos);
+    return EQ<R>{pos ? rq : q, pos};
+}
+
+template <class R>
+__device__ __noinline__ EQ<R> mc_pri(const Crew& c, const V3<R>* p)
+{
+    V3<R> e03 = p[3] - p[0], e14 = p[4] - p[1], e25 = p[5] - p[2];
+    V3<R> e01 = p[1] - p[0], e12 = p[2] - p[1], e20 = p[0] - p[2];
+    V3<R> e34 = p[4] - p[3], e45 = p[5] - p[4], e53 = p[3] - p[5];
+    R rq[6], q[6];
+    bool pos[6];
+    V3<R> a, b, d;
+    pri_frame(-e01, e20, e03, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[3]), rq[0], q[0], pos[0]);
+    pri_frame(-e12, e01, e14, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[4]), rq[1], q[1], pos[1]);
+    pri_frame(-e20, e12, e25, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[5]), rq[2], q[2], pos[2]);
+    pri_frame(-e34, e53, e03, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[3], p[4], p[5]), rq[3], q[3], pos[3]);
+    pri_frame(-e45, e34, e14, a, b, d); mc_corner(a, b, d, specified_metric(c, p[1], p[3], p[4], p[5]), rq[4], q[4], pos[4]);
+    pri_frame(-e53, e45, e25, a, b, d); mc_corner(a, b, d, specified_metric(c, p[2], p[3], p[4], p[5]), rq[5], q[5], pos[5]);
+    return combine(rq, q, pos, 6);
+}
+
+template <class R>
+__device__ __noinline__ EQ<R> mc_hex(const Crew& c, const V3<R>* p)
+{
+    V3<R> e01 = p[1] - p[0], e03 = p[3] - p[0], e04 = p[4] - p[0], e12 = p[2] - p[1];
+    V3<R> e15 = p[5] - p[1], e23 = p[3] - p[2], e26 = p[6] - p[2], e37 = p[7] - p[3];
+    V3<R> e45 = p[5] - p[4], e47 = p[7] - p[4], e56 = p[6] - p[5], e67 = p[7] - p[6];
+    R rq[8], q[8];
+    bool pos[8];
+    mc_corner(e01, e04, -e03, specified_metric(c, p[0], p[1], p[3], p[4]), rq[0], q[0], pos[0]);
+    mc_corner(e01, e12, e15, specified_metric(c, p[0], p[1], p[2], p[5]), rq[1], q[1], pos[1]);
+    mc_corner(e12, e26, -e23, specified_metric(c, p[1], p[2], p[3], p[6]), rq[2], q[2], pos[2]);
+    mc_corner(e03, e23, e37, specified_metric(c, p[0], p[2], p[3], p[7]), rq[3], q[3], pos[3]);
+    mc_corner(e04, e45, e47, specified_metric(c, p[0], p[4], p[5], p[7]), rq[4], q[4], pos[4]);
+    mc_corner(e15, -e56, e45, specified_metric(c, p[1], p[4], p[5], p[6]), rq[5], q[5], pos[5]);
+    mc_corner(e26, e56, e67, specified_metric(c, p[2], p[5], p[6], p[7]), rq[6], q[6], pos[6]);
+    mc_corner(e37, e67, -e47, specified_metric(c, p[3], p[4], p[6], p[7]), rq[7], q[7], pos[7]);
+    return combine(rq, q, pos, 8);
+}
+
+// quality of an element of the given type; MAXK = 4 means tets only
+template <int VAR, int MAXK, class R>
+__device__ __forceinline__ EQ<R> elem_quality(const Crew& c, int type, const V3<R>* p)
+{
+    if (!VarTraits<VAR>::mean_ratio)
+    {
+        if (MAXK == 4 || type == kTet) return mc_tet(c, p);
+        if (type == kPri) return mc_pri(c, p);
+        return mc_hex(c, p);
+    }
+    if (MAXK == 4 || type == kTet) return mr_tet<VAR, R>(c, p);
+    if (type == kPri) return mr_pri<VAR, R>(c, p);
+    return mr_hex<VAR, R>(c, p);
+}
+
+__device__ __forceinline__ int type_size(int type) { return type == kTet ? 4 : type == kPri ? 6 : 8; }
+
+// vertex ids of element (type, id)
+__device__ __forceinline__ void elem_vertices(const MeshView& m, int type, uint32_t id, uint32_t* v)
+{
+    if (type == kTet)
+    {
+        uint4 t = m.tets[id];
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    }
+    else if (type == kPri)
+    {
+        const uint2* p = reinterpret_cast<const uint2*>(m.pris + 6 * (size_t)id);
+        uint2 a = p[0], b = p[1], c = p[2];
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
+    }
+    else
+    {
+        uint4 a = m.hexs[2 * (size_t)id], b = m.hexs[2 * (size_t)id + 1];
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// boundary projection by constraint id (-1 fixed: never moved; 0 free)
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ V3<R> project(const Constraint* con, int ncon, int id, V3<R> p)
+{
+    if (id <= 0 || id >= ncon) return p;
+    const Constraint& k = con[id];
+    const bool dbl = sizeof(R) == 8;
+    switch (k.kind)
+    {
+    case kConPlane:
+    {
+        V3<R> a = dbl ? mk<R>((R)k.ad[0], (R)k.ad[1], (R)k.ad[2]) : mk<R>((R)k.a[0], (R)k.a[1], (R)k.a[2]);
+        V3<R> n = dbl ? mk<R>((R)k.bd[0], (R)k.bd[1], (R)k.bd[2]) : mk<R>((R)k.b[0], (R)k.b[1], (R)k.b[2]);
+        R l = dot(p - a, n);
+        return p - n * l;
+    }
+    case kConSegment:
+    {
+        V3<R> a = dbl ? mk<R>((R)k.ad[0], (R)k.ad[1], (R)k.ad[2]) : mk<R>((R)k.a[0], (R)k.a[1], (R)k.a[2]);
+        V3<R> u = dbl ? mk<R>((R)k.ud[0], (R)k.ud[1], (R)k.ud[2]) : mk<R>((R)k.u[0], (R)k.u[1], (R)k.u[2]);
+        R len = dbl ? (R)k.lend : (R)k.len;
+        V3<R> dist = p - a;
+        R l = dot(dist, u);
+        if (l < R(0)) return a;
+        if (l > len) return dbl ? mk<R>((R)k.bd[0], (R)k.bd[1], (R)k.bd[2]) : mk<R>((R)k.b[0], (R)k.b[1], (R)k.b[2]);
+        return p - (dist - u * l);
+    }
+    case kConSphere:
+        return normalize(p);
+    case kConPoint:
+        return dbl ? mk<R>((R)k.ad[0], (R)k.ad[1], (R)k.ad[2]) : mk<R>((R)k.a[0], (R)k.a[1], (R)k.a[2]);
+    default:
+        return p;
+    }
+}
+
+}  // namespace gm

@@ -1,0 +1,163 @@
+// GETMe element-wise smoothing: the element transform pass and the
+// per-group vertex update with the patch-quality acceptance test
+// (Smoothers/ElementWise/GetmeSmoother.cpp:55-374,
+//  Smoothers/ElementWise/AbstractElementWiseSmoother.cpp:406-444).
+//
+// The element pass writes each element's transformed corners and weight to
+// a per-(element, corner) buffer instead of accumulating them with atomics;
+// the update pass gathers a vertex's corners through its vertex->element
+// list, so the sums are deterministic.
+#include <cuda_runtime.h>
+
+#include "gm_relocate.cuh"
+
+namespace gm {
+
+template <int VAR, int N>
+__device__ __forceinline__ void getme_one(const MeshView& m, const Crew& crew, float lambda, int type, uint32_t id,
+                                          float4* out)
+{
+    uint32_t vi[8];
+    elem_vertices(m, type, id, vi);
+    V3<float> vp[N], vpp[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) vp[k] = to<float>(m.pos[vi[k]]);
+    float w = getme_transform<VAR, float, N>(m, crew, lambda, type, vi, vp, vpp);
+#pragma unroll
+    for (int k = 0; k < N; ++k) out[(size_t)id * N + k] = make_float4(vpp[k].x, vpp[k].y, vpp[k].z, w);
+}
+
+template <int VAR>
+__global__ void __launch_bounds__(256) getme_elements_kernel(MeshView m, Crew crew, float lambda, float4* corners)
+{
+    const uint32_t total = m.nt + m.np + m.nh;
+    float4* ctet = corners;
+    float4* cpri = corners + 4 * (size_t)m.nt;
+    float4* chex = cpri + 6 * (size_t)m.np;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
+    {
+        if (i < m.nt) getme_one<VAR, 4>(m, crew, lambda, kTet, i, ctet);
+        else if (i < m.nt + m.np) getme_one<VAR, 6>(m, crew, lambda, kPri, i - m.nt, cpri);
+        else getme_one<VAR, 8>(m, crew, lambda, kHex, i - m.nt - m.np, chex);
+    }
+}
+
+cudaError_t launch_getme_elements(int variant, const MeshView& m, const Crew& crew, float lambda, float4* corners,
+                                  int sm_count, cudaStream_t s)
+{
+    uint32_t total = m.nt + m.np + m.nh;
+    if (total == 0) return cudaSuccess;
+    long need = ((long)total + 255) / 256;
+    long cap = (long)sm_count * 8;
+    int blocks = (int)(need < cap ? need : cap);
+    switch (variant)
+    {
+    case kVarMRFree: getme_elements_kernel<kVarMRFree><<<blocks, 256, 0, s>>>(m, crew, lambda, corners); break;
+    case kVarMRWise: getme_elements_kernel<kVarMRWise><<<blocks, 256, 0, s>>>(m, crew, lambda, corners); break;
+    case kVarMC: getme_elements_kernel<kVarMC><<<blocks, 256, 0, s>>>(m, crew, lambda, corners); break;
+    default: getme_elements_kernel<kVarMCWise><<<blocks, 256, 0, s>>>(m, crew, lambda, corners); break;
+    }
+    return cudaGetLastError();
+}
+
+// weighted average of the vertex's transformed corners
+__device__ __forceinline__ bool getme_average(const MeshView& m, const float4* corners, uint32_t v, int lane,
+                                              V3<float>& out)
+{
+    const size_t base[4] = {0, 0, 4 * (size_t)m.nt, 4 * (size_t)m.nt + 6 * (size_t)m.np};
+    uint32_t b = m.ve_off[v], e = m.ve_off[v + 1];
+    float sx = 0, sy = 0, sz = 0, sw = 0;
+    for (uint32_t i = b + lane; i < e; i += kWarp)
+    {
+        uint32_t r = m.ve[i];
+        int type = ref_type(r);
+        float4 c = corners[base[type] + (size_t)ref_id(r) * type_size(type) + ref_local(r)];
+        sx += c.x * c.w;
+        sy += c.y * c.w;
+        sz += c.z * c.w;
+        sw += c.w;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        sz += __shfl_xor_sync(0xffffffffu, sz, o);
+        sw += __shfl_xor_sync(0xffffffffu, sw, o);
+    }
+    if (sw == 0.f) return false;
+    out = mk(sx / sw, sy / sw, sz / sw);
+    return true;
+}
+
+template <int VAR, int MAXK>
+__global__ void __launch_bounds__(128) getme_update_kernel(MeshView m, Crew crew, SmoothParams sp,
+                                                           const float4* corners, const uint32_t* members,
+                                                           uint32_t count, int maxe, Counters* ctr, Deferred def,
+                                                           uint32_t slot_base)
+{
+    extern __shared__ __align__(16) char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t w = blockIdx.x * (blockDim.x >> 5) + wib;
+    if (w >= count) return;
+    WarpPatch P = carve_patch(smem + wib * warp_patch_bytes(MAXK, maxe), MAXK, maxe);
+    const uint32_t v = members[w];
+    V3<float> prim;
+    if (!getme_average(m, corners, v, lane, prim)) return;
+    const int cid = m.cid[v];
+    if (cid != 0) prim = snap(m, cid, prim);
+    stage_patch(m, v, P, lane);
+    const float4 old = m.pos[v];
+    if (lane == 0)
+    {
+        P.cand[0] = old;
+        P.cand[1] = make_float4(prim.x, prim.y, prim.z, 0.f);
+    }
+    __syncwarp();
+    patch_multi<VAR, MAXK, float>(crew, P, 2, lane);
+    const float q = P.res[0], qp = P.res[1];
+    const bool defer = !(q >= sp.accept_q && qp >= sp.accept_q);
+    if (lane == 0)
+    {
+        float4 nw = make_float4(prim.x, prim.y, prim.z, old.w);
+        if (defer)
+        {
+            uint32_t k = atomicAdd(def.count, 1u);
+            def.v[slot_base + k] = v;
+            def.oldp[slot_base + k] = old;
+            def.newp[slot_base + k] = nw;
+        }
+        else if (!(qp < q))
+            m.pos[v] = nw;
+    }
+    count_work(ctr, 2, P.E, MAXK == 4 ? kTet : kHex, defer, lane);
+}
+
+template <int VAR, int MAXK>
+static cudaError_t launch_update_t(const RelocLaunch& L, const float4* corners)
+{
+    size_t smem = patch_smem_per_warp(MAXK, L.maxe) * L.warps_per_block;
+    if (smem > 48 * 1024)
+    {
+        cudaError_t e = cudaFuncSetAttribute(getme_update_kernel<VAR, MAXK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    unsigned blocks = (L.count + L.warps_per_block - 1) / L.warps_per_block;
+    getme_update_kernel<VAR, MAXK><<<blocks, 32 * L.warps_per_block, smem, L.stream>>>(
+        L.m, L.crew, L.sp, corners, L.members, L.count, L.maxe, L.ctr, L.def, L.slot_base);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_getme_update(const RelocLaunch& L, const float4* corners)
+{
+    if (L.count == 0) return cudaSuccess;
+    switch (L.variant)
+    {
+    case kVarMRFree: return L.maxk == 4 ? launch_update_t<kVarMRFree, 4>(L, corners)
+                                        : launch_update_t<kVarMRFree, 8>(L, corners);
+    case kVarMRWise: return launch_update_t<kVarMRWise, 8>(L, corners);
+    default: return L.maxk == 4 ? launch_update_t<kVarMC, 4>(L, corners) : launch_update_t<kVarMC, 8>(L, corners);
+    }
+}
+
+}  // namespace gm

@@ -1,0 +1,580 @@
+// Kernel bodies shared by the plain (one launch per colour) and batched
+// (persistent, work-queue) paths.
+#pragma once
+
+#include "gm_device.cuh"
+
+namespace gm {
+
+constexpr int kWarp = 32;
+enum : int { kSmoothNM = 0, kSmoothGD = 1, kSmoothSpawn = 2, kSmoothGetme = 3 };
+constexpr int kMaxCand = 64;  // spawn search evaluates 64 candidates at once
+
+// evaluation output (QualityHistogram, DataStructures/QualityHistogram.h:72-75)
+struct Quality
+{
+    double min;
+    double inv_sum;  // +inf once any element has q <= 0
+    unsigned long long count;
+    unsigned long long nbad;
+    unsigned long long buckets[20];
+};
+
+struct EvalPartial
+{
+    float min;
+    int nbad;
+    double rsum;
+    int hist[20];
+    int pad;
+};
+
+// relocation parameters (the reference's file-scope constants, now runtime)
+struct SmoothParams
+{
+    float shift;        // NM / GD: local size -> node shift; spawn: move coefficient
+    int cycles;         // NM / GD security cycle count; spawn iterations
+    float convergence;  // NM value convergence
+    float alpha, beta, gamma;
+    float lambda;       // GETMe
+    float accept_q;     // patches below this quality are relocated / accepted in FP64
+};
+
+// vertices whose old or new patch quality is below the acceptance threshold,
+// handed from the FP32 relocation kernel to the FP64 acceptance kernel
+struct Deferred
+{
+    uint32_t* v;
+    float4* oldp;
+    float4* newp;
+    uint32_t* count;
+};
+
+// per-launch counters for FLOP accounting
+struct Counters
+{
+    unsigned long long patch_evals;
+    unsigned long long elem_evals[4];  // by element type
+    unsigned long long fp64_vertices;
+};
+
+// ---------------------------------------------------------------------------
+// warp-level patch: the incident elements of one vertex staged in shared
+// memory as [slot][element] float4 (conflict-free: lane e reads element e)
+// ---------------------------------------------------------------------------
+struct WarpPatch
+{
+    float4* sp;    // ks * maxe
+    int* meta;     // maxe: type | local << 2
+    float4* cand;  // kMaxCand candidate positions
+    float* res;    // kMaxCand patch qualities
+    int maxe;
+    int E;
+};
+
+__device__ __forceinline__ size_t warp_patch_bytes(int ks, int maxe)
+{
+    return (size_t)ks * maxe * sizeof(float4) + (size_t)maxe * sizeof(int) + kMaxCand * sizeof(float4) +
+           kMaxCand * sizeof(float);
+}
+
+__device__ __forceinline__ WarpPatch carve_patch(char* base, int ks, int maxe)
+{
+    WarpPatch p;
+    p.sp = reinterpret_cast<float4*>(base);
+    base += (size_t)ks * maxe * sizeof(float4);
+    p.cand = reinterpret_cast<float4*>(base);
+    base += kMaxCand * sizeof(float4);
+    p.res = reinterpret_cast<float*>(base);
+    base += kMaxCand * sizeof(float);
+    p.meta = reinterpret_cast<int*>(base);
+    p.maxe = maxe;
+    p.E = 0;
+    return p;
+}
+
+__device__ __forceinline__ void stage_patch(const MeshView& m, uint32_t v, WarpPatch& P, int lane)
+{
+    uint32_t b = m.ve_off[v], e = m.ve_off[v + 1];
+    P.E = (int)(e - b);
+    for (int i = lane; i < P.E; i += kWarp)
+    {
+        uint32_t r = m.ve[b + i];
+        int type = ref_type(r), loc = ref_local(r);
+        uint32_t vid[8];
+        elem_vertices(m, type, ref_id(r), vid);
+        int n = type_size(type);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < n) P.sp[k * P.maxe + i] = m.pos[vid[k]];
+        P.meta[i] = type | (loc << 2);
+    }
+    __syncwarp();
+}
+
+// quality of staged element e with its moving vertex at c
+template <int VAR, int MAXK, class R>
+__device__ __forceinline__ EQ<R> staged_quality(const Crew& crew, const WarpPatch& P, int e, V3<R> c)
+{
+    int meta = P.meta[e];
+    int type = MAXK == 4 ? kTet : (meta & 3);
+    int loc = meta >> 2;
+    V3<R> p[MAXK];
+    int n = MAXK == 4 ? 4 : type_size(type);
+#pragma unroll
+    for (int k = 0; k < MAXK; ++k)
+    {
+        if (k < n) p[k] = (k == loc) ? c : to<R>(P.sp[k * P.maxe + e]);
+        else p[k] = c;
+    }
+    return elem_quality<VAR, MAXK, R>(crew, type, p);
+}
+
+// patch quality semantics of AbstractEvaluator::accumulatePatchQuality /
+// finalizePatchQuality (Evaluators/AbstractEvaluator.cpp:778-803): harmonic
+// mean when every element is valid, else the minimum element quality
+template <class R>
+struct PatchAcc
+{
+    R rsum;
+    R minq;
+    int nbad;
+};
+
+template <class R>
+__device__ __forceinline__ void acc_add(PatchAcc<R>& a, EQ<R> q)
+{
+    if (q.pos) a.rsum += q.v;
+    else
+    {
+        a.nbad += 1;
+        a.minq = q.v < a.minq ? q.v : a.minq;
+    }
+}
+
+template <class R>
+__device__ __forceinline__ R shfl_xor(R v, int o)
+{
+    return __shfl_xor_sync(0xffffffffu, v, o);
+}
+
+// reduce within aligned segments of S lanes (S a power of two)
+template <class R>
+__device__ __forceinline__ void acc_reduce(PatchAcc<R>& a, int S)
+{
+    for (int o = S >> 1; o > 0; o >>= 1)
+    {
+        a.rsum += shfl_xor(a.rsum, o);
+        R mq = shfl_xor(a.minq, o);
+        a.minq = mq < a.minq ? mq : a.minq;
+        a.nbad += __shfl_xor_sync(0xffffffffu, a.nbad, o);
+    }
+}
+
+template <class R>
+__device__ __forceinline__ R acc_final(const PatchAcc<R>& a, int E)
+{
+    if (a.nbad > 0) return a.minq;
+    if (E == 0) return R(0);
+    return R(E) / a.rsum;
+}
+
+// patch quality with the vertex at c (same c on every lane), whole warp
+template <int VAR, int MAXK, class R>
+__device__ __forceinline__ R patch_uniform(const Crew& crew, const WarpPatch& P, V3<R> c, int lane)
+{
+    PatchAcc<R> a{R(0), R(3.0e38), 0};
+    for (int e = lane; e < P.E; e += kWarp) acc_add(a, staged_quality<VAR, MAXK, R>(crew, P, e, c));
+    acc_reduce(a, kWarp);
+    return acc_final(a, P.E);
+}
+
+// patch quality of K candidates held in P.cand; results land in P.res
+template <int VAR, int MAXK, class R>
+__device__ __forceinline__ void patch_multi(const Crew& crew, WarpPatch& P, int K, int lane)
+{
+    int S = 32;
+    while (S > 1 && K * S > 32) S >>= 1;
+    int G = 32 / S;
+    int slot = lane / S, sub = lane & (S - 1);
+    for (int r = 0; r < K; r += G)
+    {
+        int c = r + slot;
+        PatchAcc<R> a{R(0), R(3.0e38), 0};
+        if (c < K)
+        {
+            float4 cf = P.cand[c];
+            V3<R> cp = to<R>(cf);
+            for (int e = sub; e < P.E; e += S) acc_add(a, staged_quality<VAR, MAXK, R>(crew, P, e, cp));
+        }
+        acc_reduce(a, S);
+        if (c < K && sub == 0) P.res[c] = (float)acc_final(a, P.E);
+    }
+    __syncwarp();
+}
+
+template <class R>
+__device__ __forceinline__ V3<R> snap(const MeshView& m, int cid, V3<R> p)
+{
+    return project<R>(m.con, m.ncon, cid, p);
+}
+
+// AbstractMeasurer::computeLocalElementSize (Measurers/AbstractMeasurer.cpp:137-155)
+template <class R>
+__device__ __forceinline__ R local_size(const MeshView& m, uint32_t v, V3<R> pos, int lane)
+{
+    uint32_t b = m.vv_off[v], e = m.vv_off[v + 1];
+    R s = 0;
+    for (uint32_t i = b + lane; i < e; i += kWarp) s += length(to<R>(m.pos[m.vv[i]]) - pos);
+    for (int o = 16; o > 0; o >>= 1) s += shfl_xor(s, o);
+    return s / R(e - b);
+}
+
+// ---------------------------------------------------------------------------
+// Nelder-Mead (Smoothers/VertexWise/NelderMeadSmoother.cpp:100-260), one warp
+// ---------------------------------------------------------------------------
+struct S4
+{
+    V3<float> p;
+    float w;
+};
+__device__ __forceinline__ void swp(S4& a, S4& b)
+{
+    S4 t = a;
+    a = b;
+    b = t;
+}
+
+template <int VAR, int MAXK>
+__device__ V3<float> nelder_mead(const MeshView& m, const Crew& crew, const SmoothParams& sp, WarpPatch& P,
+                                 uint32_t v, int cid, V3<float> pos, float q0, int lane, int& evals)
+{
+    const bool constrained = cid != 0;
+    const float nodeShift = local_size<float>(m, v, pos, lane) * sp.shift;
+    const S4 vo{pos, q0};
+    S4 s[4] = {{pos + mk(nodeShift, 0.f, 0.f), 0.f}, {pos + mk(0.f, nodeShift, 0.f), 0.f},
+               {pos + mk(0.f, 0.f, nodeShift), 0.f}, vo};
+    int cycle = 0;
+    bool reset = false, terminated = false;
+    while (!terminated)
+    {
+        for (int p = 0; p < 3; ++p)
+        {
+            V3<float> x = s[p].p;
+            if (constrained) x = snap(m, cid, x);
+            ++evals;
+            s[p] = S4{x, patch_uniform<VAR, MAXK, float>(crew, P, x, lane)};
+        }
+        if (s[0].w > s[1].w) swp(s[0], s[1]);
+        if (s[1].w > s[2].w) swp(s[1], s[2]);
+        if (s[2].w > s[3].w) swp(s[2], s[3]);
+        if (s[0].w > s[1].w) swp(s[0], s[1]);
+        if (s[1].w > s[2].w) swp(s[1], s[2]);
+        if (s[0].w > s[1].w) swp(s[0], s[1]);
+
+        for (; cycle < sp.cycles; ++cycle)
+        {
+            V3<float> c = (s[1].p + s[2].p + s[3].p) * (1.f / 3.f);
+            V3<float> x = c + (c - s[0].p) * sp.alpha;
+            if (constrained) x = snap(m, cid, x);
+            ++evals;
+            const float fr = patch_uniform<VAR, MAXK, float>(crew, P, x, lane);
+            float f = fr;
+            const V3<float> xr = x;
+            bool probe = true;
+            if (s[3].w < fr) x = c + (x - c) * sp.gamma;                      // expand
+            else if (s[1].w >= fr) x = c + ((fr > s[0].w ? xr : s[0].p) - c) * sp.beta;  // contract
+            else probe = false;                                                // accept reflection
+            if (probe)
+            {
+                if (constrained) x = snap(m, cid, x);
+                ++evals;
+                f = patch_uniform<VAR, MAXK, float>(crew, P, x, lane);
+                if (s[3].w < fr && f <= fr)
+                {
+                    x = xr;
+                    f = fr;
+                }
+            }
+            S4 vx{x, f};
+            if (vx.w > s[3].w) swp(s[3], vx);
+            if (vx.w > s[2].w) swp(s[2], vx);
+            if (vx.w > s[1].w) swp(s[1], vx);
+            if (vx.w > s[0].w) swp(s[0], vx);
+            if ((s[3].w - s[1].w) < sp.convergence)
+            {
+                terminated = true;
+                break;
+            }
+        }
+        if (terminated || (cycle >= sp.cycles && reset)) break;
+        s[0] = S4{vo.p - mk(nodeShift, 0.f, 0.f), vo.w};
+        s[1] = S4{vo.p - mk(0.f, nodeShift, 0.f), vo.w};
+        s[2] = S4{vo.p - mk(0.f, 0.f, nodeShift), vo.w};
+        s[3] = vo;
+        reset = true;
+        cycle = 0;
+    }
+    V3<float> out = s[3].p;
+    if (constrained) out = snap(m, cid, out);
+    return out;
+}
+
+// ---------------------------------------------------------------------------
+// Gradient descent (Smoothers/VertexWise/GradientDescentSmoother.cpp:73-202)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float gd_offset(int i)
+{
+    // -0.25, 0, 0.1, 0.2, 0.4, 0.8, 1.2, 1.6
+    return i == 0 ? -0.25f : i == 1 ? 0.f : i == 2 ? 0.1f : i == 3 ? 0.2f : i == 4 ? 0.4f : i == 5 ? 0.8f
+           : i == 6 ? 1.2f : 1.6f;
+}
+
+template <int VAR, int MAXK>
+__device__ V3<float> gradient_descent(const MeshView& m, const Crew& crew, const SmoothParams& sp, WarpPatch& P,
+                                      uint32_t v, int cid, V3<float> pos, int lane, int& evals)
+{
+    const bool constrained = cid != 0;
+    float nodeShift = local_size<float>(m, v, pos, lane) * sp.shift;
+    const float original = nodeShift;
+    for (int c = 0; c < sp.cycles; ++c)
+    {
+        if (lane < 6)
+        {
+            int axis = lane >> 1;
+            float d = (lane & 1) ? nodeShift : -nodeShift;
+            V3<float> g = pos + mk(axis == 0 ? d : 0.f, axis == 1 ? d : 0.f, axis == 2 ? d : 0.f);
+            if (constrained) g = snap(m, cid, g);
+            P.cand[lane] = make_float4(g.x, g.y, g.z, 0.f);
+        }
+        __syncwarp();
+        patch_multi<VAR, MAXK, float>(crew, P, 6, lane);
+        evals += 6;
+        V3<float> gradQ = mk(P.res[1] - P.res[0], P.res[3] - P.res[2], P.res[5] - P.res[4]);
+        float gn = length(gradQ);
+        __syncwarp();
+        if (gn == 0.f) break;
+        V3<float> shift = gradQ * (nodeShift / gn);
+        V3<float> mine = pos;
+        if (lane < 8)
+        {
+            V3<float> x = pos + shift * gd_offset(lane);
+            if (constrained) x = snap(m, cid, x);
+            P.cand[lane] = make_float4(x.x, x.y, x.z, 0.f);
+            mine = x;
+        }
+        __syncwarp();
+        patch_multi<VAR, MAXK, float>(crew, P, 8, lane);
+        evals += 8;
+        int best = 0;
+        float bestQ = -3.0e38f;
+        for (int p = 0; p < 8; ++p)
+        {
+            float q = P.res[p];
+            if (q > bestQ)
+            {
+                bestQ = q;
+                best = p;
+            }
+        }
+        pos.x = __shfl_sync(0xffffffffu, mine.x, best);
+        pos.y = __shfl_sync(0xffffffffu, mine.y, best);
+        pos.z = __shfl_sync(0xffffffffu, mine.z, best);
+        nodeShift *= fabsf(gd_offset(best));
+        __syncwarp();
+        if (nodeShift < original / 10.f) break;
+    }
+    return pos;
+}
+
+// ---------------------------------------------------------------------------
+// Spawn search (Smoothers/VertexWise/SpawnSearchSmoother.cpp:161-226)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ V3<float> spawn_offset(int p)
+{
+    // 4x4x4 lattice minus 1.5, offset 0 replaced by the origin
+    if (p == 0) return mk(0.f, 0.f, 0.f);
+    return mk((float)(p & 3) - 1.5f, (float)((p >> 2) & 3) - 1.5f, (float)(p >> 4) - 1.5f);
+}
+
+template <int VAR, int MAXK>
+__device__ V3<float> spawn_search(const MeshView& m, const Crew& crew, const SmoothParams& sp, WarpPatch& P,
+                                  uint32_t v, int cid, V3<float> pos, int lane, int& evals)
+{
+    const bool constrained = cid != 0;
+    float scale = local_size<float>(m, v, pos, lane) * sp.shift;
+    for (int it = 0; it < sp.cycles; ++it)
+    {
+        V3<float> mine[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+        {
+            int p = lane + 32 * h;
+            V3<float> x = pos + spawn_offset(p) * scale;
+            if (constrained) x = snap(m, cid, x);
+            mine[h] = x;
+            P.cand[p] = make_float4(x.x, x.y, x.z, 0.f);
+        }
+        __syncwarp();
+        patch_multi<VAR, MAXK, float>(crew, P, 64, lane);
+        evals += 64;
+        // argmax; the first maximum wins, as in the reference's strict '>' scan
+        float bestQ = P.res[lane];
+        int best = lane;
+        float q1 = P.res[lane + 32];
+        if (q1 > bestQ)
+        {
+            bestQ = q1;
+            best = lane + 32;
+        }
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            float oq = __shfl_xor_sync(0xffffffffu, bestQ, o);
+            int ob = __shfl_xor_sync(0xffffffffu, best, o);
+            if (oq > bestQ || (oq == bestQ && ob < best))
+            {
+                bestQ = oq;
+                best = ob;
+            }
+        }
+        V3<float> sel = (best >> 5) ? mine[1] : mine[0];
+        int src = best & 31;
+        pos.x = __shfl_sync(0xffffffffu, sel.x, src);
+        pos.y = __shfl_sync(0xffffffffu, sel.y, src);
+        pos.z = __shfl_sync(0xffffffffu, sel.z, src);
+        scale /= 3.f;
+        __syncwarp();
+    }
+    return pos;
+}
+
+// ---------------------------------------------------------------------------
+// GETMe element transform (Smoothers/ElementWise/GetmeSmoother.cpp:55-374)
+// ---------------------------------------------------------------------------
+template <int VAR, class R>
+__device__ __forceinline__ R tet_volume(const Crew& c, const V3<R>* vp)
+{
+    if (VarTraits<VAR>::metric_wise)
+        return det3(segment<VAR, R>(c, vp[0], vp[3]), segment<VAR, R>(c, vp[1], vp[3]), segment<VAR, R>(c, vp[2], vp[3])) / R(6);
+    return (R)c.scaling3 * det3(vp[3] - vp[0], vp[3] - vp[1], vp[3] - vp[2]) / R(6);
+}
+
+template <int VAR, class R>
+__device__ __forceinline__ R pri_volume(const Crew& c, const V3<R>* vp)
+{
+    V3<R> e02, e12, e32, e42, e52;
+    constexpr bool mw = VarTraits<VAR>::metric_wise;
+    if (mw)
+    {
+        e02 = segment<VAR, R>(c, vp[0], vp[2]); e12 = segment<VAR, R>(c, vp[1], vp[2]); e32 = segment<VAR, R>(c, vp[3], vp[2]);
+        e42 = segment<VAR, R>(c, vp[4], vp[2]); e52 = segment<VAR, R>(c, vp[5], vp[2]);
+    }
+    else
+    {
+        e02 = vp[2] - vp[0]; e12 = vp[2] - vp[1]; e32 = vp[2] - vp[3]; e42 = vp[2] - vp[4]; e52 = vp[2] - vp[5];
+    }
+    R d = det3(e32, e52, e42) + det3(e02, e32, e42) + det3(e12, e02, e42);
+    return mw ? d / R(6) : (R)c.scaling3 * d / R(6);
+}
+
+template <int VAR, class R>
+__device__ __forceinline__ R hex_volume(const Crew& c, const V3<R>* vp)
+{
+    if (VarTraits<VAR>::metric_wise)
+    {
+        R d = det3(segment<VAR, R>(c, vp[1], vp[0]), segment<VAR, R>(c, vp[4], vp[0]), segment<VAR, R>(c, vp[3], vp[0]));
+        d += det3(segment<VAR, R>(c, vp[1], vp[2]), segment<VAR, R>(c, vp[3], vp[2]), segment<VAR, R>(c, vp[6], vp[2]));
+        d += det3(segment<VAR, R>(c, vp[4], vp[5]), segment<VAR, R>(c, vp[1], vp[5]), segment<VAR, R>(c, vp[6], vp[5]));
+        d += det3(segment<VAR, R>(c, vp[4], vp[7]), segment<VAR, R>(c, vp[6], vp[7]), segment<VAR, R>(c, vp[3], vp[7]));
+        d += det3(segment<VAR, R>(c, vp[1], vp[4]), segment<VAR, R>(c, vp[6], vp[4]), segment<VAR, R>(c, vp[3], vp[4]));
+        return d / R(6);
+    }
+    R d = det3(vp[0] - vp[1], vp[0] - vp[4], vp[0] - vp[3]);
+    d += det3(vp[2] - vp[1], vp[2] - vp[3], vp[2] - vp[6]);
+    d += det3(vp[5] - vp[4], vp[5] - vp[1], vp[5] - vp[6]);
+    d += det3(vp[7] - vp[4], vp[7] - vp[6], vp[7] - vp[3]);
+    d += det3(vp[4] - vp[1], vp[4] - vp[6], vp[4] - vp[3]);
+    return (R)c.scaling3 * d / R(6);
+}
+
+template <int VAR, class R>
+__device__ __forceinline__ R quality_value(const Crew& c, int type, const V3<R>* p)
+{
+    EQ<R> q = elem_quality<VAR, 8, R>(c, type, p);
+    return q.pos ? R(1) / q.v : q.v;
+}
+
+// transformed corners and weight of one element; fixed corners keep their
+// position (their VertexConstraint), constrained corners are projected
+template <int VAR, class R, int N>
+__device__ __forceinline__ R getme_transform(const MeshView& m, const Crew& c, R lambda, int type, const uint32_t* vi,
+                                             const V3<R>* vp, V3<R>* vpp)
+{
+    V3<R> nrm[N];
+    if (N == 4)
+    {
+        nrm[0] = cross(vp[3] - vp[1], vp[2] - vp[1]);
+        nrm[1] = cross(vp[3] - vp[2], vp[0] - vp[2]);
+        nrm[2] = cross(vp[1] - vp[3], vp[0] - vp[3]);
+        nrm[3] = cross(vp[1] - vp[0], vp[2] - vp[0]);
+        for (int k = 0; k < N; ++k) vpp[k] = vp[k] + nrm[k] * (lambda * rsqrt_<R>(length(nrm[k])));
+    }
+    else if (N == 6)
+    {
+        V3<R> aux[5] = {(vp[0] + vp[1] + vp[2]) * R(1.0 / 3.0), (vp[0] + vp[1] + vp[4] + vp[3]) * R(0.25),
+                        (vp[1] + vp[2] + vp[5] + vp[4]) * R(0.25), (vp[2] + vp[0] + vp[3] + vp[5]) * R(0.25),
+                        (vp[3] + vp[4] + vp[5]) * R(1.0 / 3.0)};
+        nrm[0] = cross(aux[1] - aux[0], aux[3] - aux[0]);
+        nrm[1] = cross(aux[2] - aux[0], aux[1] - aux[0]);
+        nrm[2] = cross(aux[3] - aux[0], aux[2] - aux[0]);
+        nrm[3] = cross(aux[3] - aux[4], aux[1] - aux[4]);
+        nrm[4] = cross(aux[1] - aux[4], aux[2] - aux[4]);
+        nrm[5] = cross(aux[2] - aux[4], aux[3] - aux[4]);
+        R t = R(4.0 / 5.0) * (R(1) - pow(R(4.0 / 39.0), R(0.25)) * lambda);
+        R it = R(1) - t;
+        V3<R> bases[6] = {aux[0] * it + (aux[3] + aux[1]) * (t * R(0.5)), aux[0] * it + (aux[1] + aux[2]) * (t * R(0.5)),
+                          aux[0] * it + (aux[2] + aux[3]) * (t * R(0.5)), aux[4] * it + (aux[3] + aux[1]) * (t * R(0.5)),
+                          aux[4] * it + (aux[1] + aux[2]) * (t * R(0.5)), aux[4] * it + (aux[2] + aux[3]) * (t * R(0.5))};
+        for (int k = 0; k < N; ++k) vpp[k] = bases[k] + nrm[k] * (lambda * rsqrt_<R>(length(nrm[k])));
+    }
+    else
+    {
+        V3<R> aux[6] = {(vp[0] + vp[1] + vp[2] + vp[3]) * R(0.25), (vp[0] + vp[4] + vp[5] + vp[1]) * R(0.25),
+                        (vp[1] + vp[5] + vp[6] + vp[2]) * R(0.25), (vp[2] + vp[6] + vp[7] + vp[3]) * R(0.25),
+                        (vp[0] + vp[3] + vp[7] + vp[4]) * R(0.25), (vp[4] + vp[7] + vp[6] + vp[5]) * R(0.25)};
+        nrm[0] = cross(aux[1] - aux[0], aux[4] - aux[0]);
+        nrm[1] = cross(aux[2] - aux[0], aux[1] - aux[0]);
+        nrm[2] = cross(aux[3] - aux[0], aux[2] - aux[0]);
+        nrm[3] = cross(aux[4] - aux[0], aux[3] - aux[0]);
+        nrm[4] = cross(aux[4] - aux[5], aux[1] - aux[5]);
+        nrm[5] = cross(aux[1] - aux[5], aux[2] - aux[5]);
+        nrm[6] = cross(aux[2] - aux[5], aux[3] - aux[5]);
+        nrm[7] = cross(aux[3] - aux[5], aux[4] - aux[5]);
+        const int B[8][3] = {{0, 1, 4}, {0, 2, 1}, {0, 3, 2}, {0, 4, 3}, {5, 4, 1}, {5, 1, 2}, {5, 2, 3}, {5, 3, 4}};
+        for (int k = 0; k < N; ++k)
+        {
+            V3<R> base = (aux[B[k][0]] + aux[B[k][1]] + aux[B[k][2]]) * R(1.0 / 3.0);
+            vpp[k] = base + nrm[k] * (lambda * rsqrt_<R>(length(nrm[k])));
+        }
+    }
+    R vol, volp;
+    if (N == 4) { vol = tet_volume<VAR, R>(c, vp); volp = tet_volume<VAR, R>(c, vpp); }
+    else if (N == 6) { vol = pri_volume<VAR, R>(c, vp); volp = pri_volume<VAR, R>(c, vpp); }
+    else { vol = hex_volume<VAR, R>(c, vp); volp = hex_volume<VAR, R>(c, vpp); }
+    R var = cbrt_(fabs(vol / volp));
+    V3<R> center = vp[0];
+    for (int k = 1; k < N; ++k) center = center + vp[k];
+    center = center * (R(1) / R(N));
+    for (int k = 0; k < N; ++k)
+    {
+        vpp[k] = center + (vpp[k] - center) * var;
+        int id = m.cid[vi[k]];
+        if (id < 0) vpp[k] = vp[k];
+        else if (id > 0) vpp[k] = snap(m, id, vpp[k]);
+    }
+    R q = quality_value<VAR, R>(c, type, vp);
+    R qp = quality_value<VAR, R>(c, type, vpp);
+    return qp / (R(1) + q);
+}
+
+}  // namespace gm

@@ -1,0 +1,47 @@
+// Launchers of the device kernels (defined in the .cu files).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gm_kernels.cuh"
+
+namespace gm {
+
+size_t patch_smem_per_warp(int ks, int maxe);
+
+int evaluate_blocks(uint32_t total, int sm_count);
+cudaError_t launch_evaluate(int variant, int maxk, const MeshView& m, const Crew& crew, EvalPartial* parts,
+                            int nblocks, Quality* out, cudaStream_t s);
+
+// one relocation launch over one independent group
+struct RelocLaunch
+{
+    int variant;  // kVarMRFree / kVarMRWise / kVarMC
+    int maxk;     // 4: tets only, 8: any element type
+    MeshView m;
+    Crew crew;
+    SmoothParams sp;
+    const uint32_t* members;
+    uint32_t count;
+    int maxe;
+    int warps_per_block;
+    Counters* ctr;
+    Deferred def;
+    uint32_t slot_base;  // this group's region of the deferred arrays
+    cudaStream_t stream;
+};
+
+cudaError_t launch_relocate_nm(const RelocLaunch& L);
+cudaError_t launch_relocate_gd(const RelocLaunch& L);
+cudaError_t launch_relocate_spawn(const RelocLaunch& L);
+cudaError_t launch_getme_update(const RelocLaunch& L, const float4* corners);
+// FP64 acceptance of the vertices the preceding launch deferred
+cudaError_t launch_accept(const RelocLaunch& L);
+
+cudaError_t launch_getme_elements(int variant, const MeshView& m, const Crew& crew, float lambda, float4* corners,
+                                  int sm_count, cudaStream_t s);
+
+// FP32 peak probe: 8 independent FFMA chains per thread
+cudaError_t launch_ffma_probe(int blocks, int threads, int iters, float* sink, cudaStream_t s);
+
+}  // namespace gm

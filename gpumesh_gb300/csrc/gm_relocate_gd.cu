@@ -1,0 +1,8 @@
+// Relocation kernels of one smoother (see gm_relocate.cuh).
+#include "gm_relocate.cuh"
+
+namespace gm {
+
+cudaError_t launch_relocate_gd(const RelocLaunch& L) { return launch_relocate_smoother<kSmoothGD>(L); }
+
+}  // namespace gm

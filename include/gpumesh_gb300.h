@@ -1,0 +1,224 @@
+/*
+ * gpumesh_gb300.h -- C ABI of libgpumesh_gb300.so, the GB300 (sm_103a)
+ * implementation of GpuMesh's vertex-wise relocation smoothing and
+ * element-quality evaluation.
+ *
+ * The reference host code (GpuMesh's C++ Mesh / MeshCrew / NodeGroups and
+ * its AbstractSmoother / AbstractEvaluator plugins) calls CUDA through
+ * C++-linkage "driver" functions defined under resources/cuda/.  Every entry
+ * point below names the driver it replaces (file:line in the GpuMesh tree);
+ * a thin C++ shim with the legacy signatures forwards to these calls.
+ *
+ * Conventions
+ *  - Every function returns a gm_status; GM_OK is 0.  gm_last_error()
+ *    returns a message for the last failure on the calling thread.
+ *  - Arrays are plain host pointers with explicit counts.  Nothing here
+ *    takes ownership of caller memory.
+ *  - A gm_mesh owns its device buffers.  Work is issued on the mesh's
+ *    stream (gm_mesh_set_stream, default: the legacy default stream);
+ *    functions that return host results synchronise that stream.
+ *  - One process may hold any number of meshes (the reference keeps one
+ *    mesh in file-scope device globals, resources/cuda/Mesh.cu:9-31).
+ */
+#ifndef GPUMESH_GB300_H
+#define GPUMESH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int gm_status;
+#define GM_OK 0
+#define GM_ERR_INVALID_ARG 1
+#define GM_ERR_CUDA 2
+#define GM_ERR_OUT_OF_MEMORY 3
+#define GM_ERR_UNSUPPORTED 4
+#define GM_ERR_TIMEOUT 5
+#define GM_ERR_STATE 6
+
+/* element type codes = MeshTet/MeshPri/MeshHex::ELEMENT_TYPE (DataStructures/Mesh.h:89,171,213) */
+#define GM_TET 0
+#define GM_PRI 2
+#define GM_HEX 3
+
+/* samplers: UniformSampler (Samplers/UniformSampler.cpp:45), AnalyticSampler
+ * (Samplers/AbstractSampler.cpp:190-208) and the sine-graded anisotropic
+ * metric s^2 diag(1 + 9 sin^2(4 pi x), 1, 1) */
+#define GM_SAMPLER_UNIFORM 0
+#define GM_SAMPLER_ANALYTIC 1
+#define GM_SAMPLER_SINE 2
+/* measurers: MetricFreeMeasurer, MetricWiseMeasurer (Measurers/) */
+#define GM_MEASURER_METRIC_FREE 0
+#define GM_MEASURER_METRIC_WISE 1
+/* evaluators: MeanRatioEvaluator, MetricConformityEvaluator (Evaluators/) */
+#define GM_EVALUATOR_MEAN_RATIO 0
+#define GM_EVALUATOR_METRIC_CONFORMITY 1
+/* constraint kinds (Boundaries/Constraints/, Boundaries/SphereBoundary.cpp) */
+#define GM_CON_VOLUME 0
+#define GM_CON_PLANE 1
+#define GM_CON_SEGMENT 2
+#define GM_CON_SPHERE 3
+#define GM_CON_POINT 4
+/* smoothers */
+#define GM_SMOOTH_NELDER_MEAD 0
+#define GM_SMOOTH_GRADIENT_DESCENT 1
+#define GM_SMOOTH_SPAWN_SEARCH 2
+#define GM_SMOOTH_GETME 3
+
+#define GM_HIST_BUCKETS 20
+
+/* QualityHistogram (DataStructures/QualityHistogram.h): minimum, sum of
+ * 1/q (+inf once any q <= 0, so the harmonic mean count/inv_sum is 0),
+ * element count, elements with q <= 0, and 20 clamped buckets. */
+typedef struct gm_quality
+{
+    double min;
+    double inv_sum;
+    uint64_t count;
+    uint64_t nbad;
+    uint64_t buckets[GM_HIST_BUCKETS];
+} gm_quality;
+
+/* Smoother parameters.  params[] layout per smoother (defaults are the
+ * reference's file-scope constants):
+ *   NM    [local size -> node shift (1/24), security cycles (12),
+ *          value convergence (1e-4), alpha (1), beta (0.5), gamma (2)]
+ *          Smoothers/VertexWise/NelderMeadSmoother.cpp:17-23
+ *   GD    [local size -> node shift (1/75), security cycles (5)]
+ *          Smoothers/VertexWise/GradientDescentSmoother.cpp:14-15
+ *   spawn [move coefficient (1/20), iterations (2)]
+ *          Smoothers/VertexWise/SpawnSearchSmoother.cpp:14,181
+ *   GETMe [lambda (0.78)]  Smoothers/ElementWise/GetmeSmoother.cpp:22
+ * A NULL params pointer selects the defaults. */
+#define GM_PARAMS 8
+
+typedef struct gm_mesh gm_mesh;
+
+const char* gm_last_error(void);
+const char* gm_status_string(gm_status s);
+/* library build identification: "sm_103a <date>" */
+const char* gm_version(void);
+
+/* ---- host topology -------------------------------------------------------
+ * Replaces Mesh::compileTopology's neighbourhood pass and NodeGroups::build
+ * (DataStructures/Mesh.cpp:213-285, DataStructures/NodeGroups.cpp:104-122)
+ * for callers that do not run the reference host code.  Outputs are caller
+ * allocated:
+ *   perm[nv]          new vertex index -> input vertex index
+ *   group_base[nv+1]  colour g owns members[group_base[g] .. group_base[g+1])
+ *   members[nv]       colour-major relocation order (new indices)
+ *   ranges[6*nv]      per colour: boundary, subsurface, interior [begin,end)
+ *   *ngroups          number of colours
+ * Connectivity passed in uses input indices. */
+gm_status gm_node_groups_build(uint32_t nv, const int32_t* cid, uint32_t nt, const uint32_t* tets,
+                               uint32_t np, const uint32_t* pris, uint32_t nh, const uint32_t* hexs,
+                               int32_t permute, uint32_t* perm, uint32_t* group_base, uint32_t* members,
+                               uint32_t* ranges, uint32_t* ngroups);
+
+/* ---- device mesh ---------------------------------------------------------- */
+gm_status gm_mesh_create(gm_mesh** out);
+gm_status gm_mesh_destroy(gm_mesh* mesh);
+/* stream: a cudaStream_t; 0 is the legacy default stream */
+gm_status gm_mesh_set_stream(gm_mesh* mesh, void* stream);
+gm_status gm_mesh_sync(gm_mesh* mesh);
+
+/* Upload a whole mesh in the order given (no permutation): positions (FP64,
+ * 3 per vertex), constraint id per vertex (<0 fixed, 0 free, >0 constraint),
+ * connectivity.  Builds the vertex->element and vertex->vertex CSR on the
+ * host.  Replaces GpuMesh::updateCudaTopology + updateCudaVertices
+ * (DataStructures/GpuMesh.cpp:227-276). */
+gm_status gm_mesh_upload(gm_mesh* mesh, uint32_t nv, const double* xyz, const int32_t* cid, uint32_t nt,
+                         const uint32_t* tets, uint32_t np, const uint32_t* pris, uint32_t nh,
+                         const uint32_t* hexs);
+
+/* Replaces updateCudaVerts (resources/cuda/Mesh.cu:74).  xyz: FP64 x,y,z. */
+gm_status gm_mesh_upload_verts(gm_mesh* mesh, uint32_t nv, const double* xyz);
+/* Replaces updateCudaVerts with the reference's GpuVert layout
+ * {vec3 p; uint c} (16 bytes per vertex, DataStructures/GpuMesh.h:11-19). */
+gm_status gm_mesh_upload_gpu_verts(gm_mesh* mesh, uint32_t nv, const void* gpu_verts);
+/* Replace updateCudaTets / updateCudaPris / updateCudaHexs
+ * (resources/cuda/Mesh.cu:100,126,152).  stride_words = 32-bit words per
+ * element record: 4/6/8 for bare connectivity, 5/12/16 for GpuTet, GpuPri,
+ * GpuHex (DataStructures/GpuMesh.h:41-85), whose cache words are ignored. */
+gm_status gm_mesh_upload_tets(gm_mesh* mesh, uint32_t n, const uint32_t* words, uint32_t stride_words);
+gm_status gm_mesh_upload_pris(gm_mesh* mesh, uint32_t n, const uint32_t* words, uint32_t stride_words);
+gm_status gm_mesh_upload_hexs(gm_mesh* mesh, uint32_t n, const uint32_t* words, uint32_t stride_words);
+/* Replaces updateCudaTopo (resources/cuda/Mesh.cu:185): GpuTopo records
+ * {int type; uint neigVertBase, neigVertCount, neigElemBase, neigElemCount}
+ * (type: -1 fixed, 0 free, >0 constraint id), GpuNeigVert {uint v},
+ * GpuNeigElem {uint id; int type; int vId} (DataStructures/GpuMesh.h:87-141). */
+gm_status gm_mesh_upload_topo(gm_mesh* mesh, uint32_t nv, const int32_t* topo5, uint32_t n_neig_verts,
+                              const uint32_t* neig_verts, uint32_t n_neig_elems, const int32_t* neig_elems3);
+/* Replaces updateCudaGroupMembers (resources/cuda/Mesh.cu:259): the
+ * concatenated relocation order; group_base gives each colour's slice. */
+gm_status gm_mesh_upload_groups(gm_mesh* mesh, uint32_t n_members, const uint32_t* members, uint32_t ngroups,
+                                const uint32_t* group_base);
+/* Constraint table indexed by constraint id (id 0 = volume).  params: 6
+ * doubles per id -- plane: point, normal; segment: a, b; point: position.
+ * The reference's constraint objects (Boundaries/Constraints/) carry these
+ * as private members; the drop-in shim recovers them. */
+gm_status gm_mesh_set_constraints(gm_mesh* mesh, uint32_t n, const int32_t* kind, const double* params);
+/* Sampler / measurer / evaluator plugins and their uniforms.  Replaces the
+ * install* drivers (Evaluating/MeanRatio.cu:156, MetricConformity.cu:196,
+ * Measuring/MetricFree.cu:124, MetricWise.cu:168, Sampling/Analytic.cu:15,
+ * Uniform.cu:13) and setCudaMetricScaling/ScalingSqr/ScalingCube/AspectRatio,
+ * setCudaRotMat (Sampling/Base.cu:110-153); the rotation is the reference
+ * sampler's fixed one and is rebuilt here. */
+gm_status gm_mesh_set_crew(gm_mesh* mesh, int32_t sampler, int32_t measurer, int32_t evaluator, double scaling,
+                           double aspect_ratio);
+
+/* Keep a device copy of the current positions / restore it (no host
+ * traffic); used to replay a smoothing schedule from the same input. */
+gm_status gm_mesh_save_positions(gm_mesh* mesh);
+gm_status gm_mesh_restore_positions(gm_mesh* mesh);
+
+/* Replaces fetchCudaVerts (resources/cuda/Mesh.cu:56): FP64 x,y,z. */
+gm_status gm_mesh_fetch_verts(gm_mesh* mesh, uint32_t nv, double* xyz);
+gm_status gm_mesh_fetch_gpu_verts(gm_mesh* mesh, uint32_t nv, void* gpu_verts);
+
+/* ---- evaluation ----------------------------------------------------------
+ * Replaces evaluateCudaMeshQuality (resources/cuda/Evaluating/Evaluate.cu:55)
+ * and AbstractEvaluator::evaluateMeshQualityCuda
+ * (Evaluators/AbstractEvaluator.cpp:574-610).  Synchronous: fills *out. */
+gm_status gm_evaluate(gm_mesh* mesh, gm_quality* out);
+/* Asynchronous: leaves the result in device result slot `slot` (slots are
+ * allocated on demand, so a whole smoothing schedule can record one result
+ * per pass without a host round trip); gm_quality_read copies a slot back
+ * and synchronises the mesh's stream. */
+gm_status gm_evaluate_async(gm_mesh* mesh, uint32_t slot);
+gm_status gm_quality_read(gm_mesh* mesh, uint32_t slot, gm_quality* out);
+
+/* ---- relocation ----------------------------------------------------------
+ * One colour: replaces smoothCudaVertices (Smoothing/VertexWise/
+ * SmoothVertices.cu:28) and smoothCudaSpawnVertices (SpawnSearch.cu:220),
+ * i.e. one NodeGroups::GpuDispatch {gpuBufferBase, gpuBufferSize} slice of
+ * the uploaded members.  Relocates constrained (boundary) vertices too, with
+ * in-kernel projection.  Asynchronous. */
+gm_status gm_smooth_group(gm_mesh* mesh, int32_t smoother, const double* params, uint32_t member_base,
+                          uint32_t member_count);
+/* A whole relocation pass: every colour in order, one launch per colour, no
+ * host round trip.  For GETMe: the element pass then one vertex-update launch
+ * per colour.  Asynchronous. */
+gm_status gm_smooth_pass(gm_mesh* mesh, int32_t smoother, const double* params);
+/* GETMe halves for the drop-in: smoothCudaElements (Smoothing/ElementWise/
+ * SmoothElements.cu:41) and updateCudaSmoothedElementsVertices
+ * (UpdateVertices.cu:47). */
+gm_status gm_getme_elements(gm_mesh* mesh, const double* params);
+gm_status gm_getme_update_group(gm_mesh* mesh, const double* params, uint32_t member_base, uint32_t member_count);
+
+/* Work counters since the last reset: [patch evaluations, tet, prism, hex
+ * element evaluations, vertices relocated in FP64].  Synchronous. */
+gm_status gm_mesh_counters(gm_mesh* mesh, uint64_t* out5, int32_t reset);
+
+/* Device peak probe: a dependent-FFMA loop over every SM; *tflops receives
+ * the achieved FP32 rate (2 flops per FFMA).  The roofline denominator of
+ * the relocation kernels. */
+gm_status gm_probe_fp32_tflops(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPUMESH_GB300_H */

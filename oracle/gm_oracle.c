@@ -1,0 +1,1441 @@
+/*
+ * gm_oracle.c -- FP64 CPU restatement of GpuMesh's node-relocation smoothers
+ * and element-quality evaluators.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path.  Only tests/,
+ * __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm load
+ * it.  The product never calls it.
+ *
+ * Parity is pinned two ways: against the reference's regular-element
+ * known-answer test (Evaluators/AbstractEvaluator.cpp:281-338), and against
+ * the reference's own C++ compiled from its sources by oracle/Makefile into
+ * oracle/_ref (tests/test_oracle_vs_reference.py, tests/golden/).
+ *
+ * Conventions follow GLM as used by the reference: dmat3 is column-major,
+ * mat*vec / mat*mat sum columns left to right, normalize(v) = v*(1/sqrt(v.v)),
+ * sign() returns -1/0/+1.  Build with -ffp-contract=off.
+ */
+#include "gm_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------------ */
+/* small GLM-like vector / matrix algebra                                    */
+/* ------------------------------------------------------------------------ */
+
+typedef struct { double x, y, z; } v3;
+typedef struct { v3 c[3]; } m3; /* column-major, like glm::dmat3 */
+
+static inline v3 V(double x, double y, double z) { v3 r = {x, y, z}; return r; }
+static inline v3 add(v3 a, v3 b) { return V(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 sub(v3 a, v3 b) { return V(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 neg(v3 a) { return V(-a.x, -a.y, -a.z); }
+static inline v3 mul(v3 a, double s) { return V(a.x * s, a.y * s, a.z * s); }
+static inline v3 dvs(v3 a, double s) { return V(a.x / s, a.y / s, a.z / s); }
+static inline double dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline double length(v3 a) { return sqrt(dot(a, a)); }
+static inline v3 normalize(v3 a) { return mul(a, 1.0 / sqrt(dot(a, a))); }
+static inline v3 cross(v3 a, v3 b)
+{
+    return V(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+static inline double gsign(double x) { return (double)((0.0 < x) - (x < 0.0)); }
+static inline double gmin(double a, double b) { return (b < a) ? b : a; }
+
+static inline m3 M(v3 c0, v3 c1, v3 c2) { m3 r; r.c[0] = c0; r.c[1] = c1; r.c[2] = c2; return r; }
+static inline m3 mdiag(double a, double b, double c)
+{
+    return M(V(a, 0, 0), V(0, b, 0), V(0, 0, c));
+}
+static inline double el(const m3* m, int c, int r)
+{
+    const double* p = &m->c[c].x;
+    return p[r];
+}
+static inline v3 mmulv(m3 m, v3 v)
+{
+    return V(m.c[0].x * v.x + m.c[1].x * v.y + m.c[2].x * v.z,
+             m.c[0].y * v.x + m.c[1].y * v.y + m.c[2].y * v.z,
+             m.c[0].z * v.x + m.c[1].z * v.y + m.c[2].z * v.z);
+}
+static inline m3 mmul(m3 a, m3 b)
+{
+    return M(mmulv(a, b.c[0]), mmulv(a, b.c[1]), mmulv(a, b.c[2]));
+}
+static inline m3 madd(m3 a, m3 b) { return M(add(a.c[0], b.c[0]), add(a.c[1], b.c[1]), add(a.c[2], b.c[2])); }
+static inline m3 msub(m3 a, m3 b) { return M(sub(a.c[0], b.c[0]), sub(a.c[1], b.c[1]), sub(a.c[2], b.c[2])); }
+static inline m3 mscale(m3 a, double s) { return M(mul(a.c[0], s), mul(a.c[1], s), mul(a.c[2], s)); }
+static inline m3 mtranspose(m3 m)
+{
+    return M(V(m.c[0].x, m.c[1].x, m.c[2].x), V(m.c[0].y, m.c[1].y, m.c[2].y),
+             V(m.c[0].z, m.c[1].z, m.c[2].z));
+}
+static inline double mdet(m3 m)
+{
+#define E(c, r) el(&m, c, r)
+    return +E(0, 0) * (E(1, 1) * E(2, 2) - E(2, 1) * E(1, 2))
+           - E(1, 0) * (E(0, 1) * E(2, 2) - E(2, 1) * E(0, 2))
+           + E(2, 0) * (E(0, 1) * E(1, 2) - E(1, 1) * E(0, 2));
+}
+static inline m3 minverse(m3 m)
+{
+    double ood = 1.0 / (+E(0, 0) * (E(1, 1) * E(2, 2) - E(2, 1) * E(1, 2))
+                        - E(1, 0) * (E(0, 1) * E(2, 2) - E(2, 1) * E(0, 2))
+                        + E(2, 0) * (E(0, 1) * E(1, 2) - E(1, 1) * E(0, 2)));
+    m3 r;
+    r.c[0].x = +(E(1, 1) * E(2, 2) - E(2, 1) * E(1, 2)) * ood;
+    r.c[1].x = -(E(1, 0) * E(2, 2) - E(2, 0) * E(1, 2)) * ood;
+    r.c[2].x = +(E(1, 0) * E(2, 1) - E(2, 0) * E(1, 1)) * ood;
+    r.c[0].y = -(E(0, 1) * E(2, 2) - E(2, 1) * E(0, 2)) * ood;
+    r.c[1].y = +(E(0, 0) * E(2, 2) - E(2, 0) * E(0, 2)) * ood;
+    r.c[2].y = -(E(0, 0) * E(2, 1) - E(2, 0) * E(0, 1)) * ood;
+    r.c[0].z = +(E(0, 1) * E(1, 2) - E(1, 1) * E(0, 2)) * ood;
+    r.c[1].z = -(E(0, 0) * E(1, 2) - E(1, 0) * E(0, 2)) * ood;
+    r.c[2].z = +(E(0, 0) * E(1, 1) - E(1, 0) * E(0, 1)) * ood;
+#undef E
+    return r;
+}
+
+/* Rodrigues rotation applied on the right of m, the algebra of
+ * glm::rotate(dmat4, angle, axis) restricted to the 3x3 block. */
+static m3 mrotate(m3 m, double angle, v3 axis_in)
+{
+    double c = cos(angle), s = sin(angle);
+    v3 axis = normalize(axis_in);
+    v3 temp = mul(axis, 1.0 - c);
+    m3 R;
+    R.c[0].x = c + temp.x * axis.x;
+    R.c[0].y = temp.x * axis.y + s * axis.z;
+    R.c[0].z = temp.x * axis.z - s * axis.y;
+    R.c[1].x = temp.y * axis.x - s * axis.z;
+    R.c[1].y = c + temp.y * axis.y;
+    R.c[1].z = temp.y * axis.z + s * axis.x;
+    R.c[2].x = temp.z * axis.x + s * axis.y;
+    R.c[2].y = temp.z * axis.y - s * axis.x;
+    R.c[2].z = c + temp.z * axis.z;
+    m3 out;
+    for (int j = 0; j < 3; ++j)
+    {
+        const double* rj = &R.c[j].x;
+        out.c[j] = add(add(mul(m.c[0], rj[0]), mul(m.c[1], rj[1])), mul(m.c[2], rj[2]));
+    }
+    return out;
+}
+
+/* ------------------------------------------------------------------------ */
+/* mesh                                                                      */
+/* ------------------------------------------------------------------------ */
+
+typedef struct
+{
+    uint32_t id;
+    int32_t type;
+    int32_t vid;
+} neig_elem;
+
+struct om_mesh
+{
+    int64_t nv, nt, np, nh;
+    double* pos; /* nv*3 */
+    uint32_t* tets;
+    uint32_t* pris;
+    uint32_t* hexs;
+    int32_t* cid;
+
+    /* vertex -> element, in the order Mesh::compileNeighborhoods builds
+     * topos[v].neighborElems (DataStructures/Mesh.cpp:365-445) */
+    int64_t* ne_base;
+    neig_elem* ne;
+    /* vertex -> vertex, in MeshTopo::neighborVerts order (Mesh::addEdge,
+     * DataStructures/Mesh.cpp:447-460) */
+    int64_t* nvx_base;
+    uint32_t* nvx;
+
+    int32_t ncon;
+    int32_t* con_kind;
+    double* con_param; /* 6 per id */
+    /* derived segment data: u, length (EdgeConstraint.cpp:176-181) */
+    double* con_derived; /* 4 per id */
+
+    int32_t sampler, measurer, evaluator;
+    double scaling, scaling2, scaling3, aspect_ratio;
+    m3 rot, rotinv;
+
+    int64_t patch_evals;
+};
+
+static const m3* fr_tet_inv(void)
+{
+    /* AbstractEvaluator.cpp:28-31 */
+    static m3 m;
+    static int init = 0;
+    if (!init)
+    {
+        m = M(V(1, 0, 0), V(-0.5773502691896257645091, 1.154700538379251529018, 0),
+              V(-0.4082482904638630163662, -0.4082482904638630163662, 1.224744871391589049099));
+        init = 1;
+    }
+    return &m;
+}
+static const m3* fr_pri_inv(void)
+{
+    /* AbstractEvaluator.cpp:32-35 */
+    static m3 m;
+    static int init = 0;
+    if (!init)
+    {
+        m = M(V(1.0, 0.0, 0.0), V(-0.5773502691896257645091, 1.154700538379251529018, 0.0),
+              V(0.0, 0.0, 1.0));
+        init = 1;
+    }
+    return &m;
+}
+
+static inline v3 P(const om_mesh* m, uint32_t v)
+{
+    const double* p = m->pos + 3 * (int64_t)v;
+    return V(p[0], p[1], p[2]);
+}
+static inline void setP(om_mesh* m, uint32_t v, v3 p)
+{
+    double* q = m->pos + 3 * (int64_t)v;
+    q[0] = p.x;
+    q[1] = p.y;
+    q[2] = p.z;
+}
+
+/* Mesh::addEdge (Mesh.cpp:447-460): linear scan of the first vertex's list */
+typedef struct
+{
+    uint32_t* items;
+    int32_t n, cap;
+} ulist;
+static void ulist_push(ulist* l, uint32_t v)
+{
+    if (l->n == l->cap)
+    {
+        l->cap = l->cap ? l->cap * 2 : 16;
+        l->items = (uint32_t*)realloc(l->items, sizeof(uint32_t) * l->cap);
+    }
+    l->items[l->n++] = v;
+}
+static void add_edge(ulist* lists, uint32_t a, uint32_t b)
+{
+    ulist* l = &lists[a];
+    for (int32_t i = 0; i < l->n; ++i)
+        if (l->items[i] == b)
+            return;
+    ulist_push(&lists[a], b);
+    ulist_push(&lists[b], a);
+}
+
+static const int TET_EDGES[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+static const int PRI_EDGES[9][2] = {{0, 1}, {0, 2}, {1, 2}, {0, 3}, {1, 4},
+                                    {2, 5}, {3, 4}, {3, 5}, {4, 5}};
+static const int HEX_EDGES[12][2] = {{0, 1}, {0, 3}, {1, 2}, {2, 3}, {0, 4}, {1, 5},
+                                     {2, 6}, {3, 7}, {4, 5}, {4, 7}, {5, 6}, {6, 7}};
+
+static void build_topology(om_mesh* m)
+{
+    int64_t nv = m->nv;
+    /* neighbour elements: counts then fill, tets -> pris -> hexs */
+    m->ne_base = (int64_t*)calloc((size_t)nv + 1, sizeof(int64_t));
+    for (int64_t i = 0; i < m->nt * 4; ++i) m->ne_base[m->tets[i] + 1]++;
+    for (int64_t i = 0; i < m->np * 6; ++i) m->ne_base[m->pris[i] + 1]++;
+    for (int64_t i = 0; i < m->nh * 8; ++i) m->ne_base[m->hexs[i] + 1]++;
+    for (int64_t v = 0; v < nv; ++v) m->ne_base[v + 1] += m->ne_base[v];
+    m->ne = (neig_elem*)malloc(sizeof(neig_elem) * (size_t)(m->ne_base[nv] + 1));
+    int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nv + 1));
+    memcpy(fill, m->ne_base, sizeof(int64_t) * (size_t)nv);
+
+    ulist* lists = (ulist*)calloc((size_t)nv, sizeof(ulist));
+    for (int64_t i = 0; i < m->nt; ++i)
+    {
+        const uint32_t* e = m->tets + 4 * i;
+        for (int k = 0; k < 4; ++k)
+        {
+            neig_elem n = {(uint32_t)i, OM_TET, k};
+            m->ne[fill[e[k]]++] = n;
+        }
+        for (int k = 0; k < 6; ++k) add_edge(lists, e[TET_EDGES[k][0]], e[TET_EDGES[k][1]]);
+    }
+    for (int64_t i = 0; i < m->np; ++i)
+    {
+        const uint32_t* e = m->pris + 6 * i;
+        for (int k = 0; k < 6; ++k)
+        {
+            neig_elem n = {(uint32_t)i, OM_PRI, k};
+            m->ne[fill[e[k]]++] = n;
+        }
+        for (int k = 0; k < 9; ++k) add_edge(lists, e[PRI_EDGES[k][0]], e[PRI_EDGES[k][1]]);
+    }
+    for (int64_t i = 0; i < m->nh; ++i)
+    {
+        const uint32_t* e = m->hexs + 8 * i;
+        for (int k = 0; k < 8; ++k)
+        {
+            neig_elem n = {(uint32_t)i, OM_HEX, k};
+            m->ne[fill[e[k]]++] = n;
+        }
+        for (int k = 0; k < 12; ++k) add_edge(lists, e[HEX_EDGES[k][0]], e[HEX_EDGES[k][1]]);
+    }
+    free(fill);
+
+    m->nvx_base = (int64_t*)calloc((size_t)nv + 1, sizeof(int64_t));
+    for (int64_t v = 0; v < nv; ++v) m->nvx_base[v + 1] = m->nvx_base[v] + lists[v].n;
+    m->nvx = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)(m->nvx_base[nv] + 1));
+    for (int64_t v = 0; v < nv; ++v)
+    {
+        if (lists[v].n)
+            memcpy(m->nvx + m->nvx_base[v], lists[v].items, sizeof(uint32_t) * lists[v].n);
+        free(lists[v].items);
+    }
+    free(lists);
+}
+
+om_mesh* om_create(int64_t nv, const double* pos, int64_t nt, const uint32_t* tets,
+                   int64_t np, const uint32_t* pris, int64_t nh, const uint32_t* hexs,
+                   const int32_t* cid)
+{
+    om_mesh* m = (om_mesh*)calloc(1, sizeof(om_mesh));
+    m->nv = nv;
+    m->nt = nt;
+    m->np = np;
+    m->nh = nh;
+    m->pos = (double*)malloc(sizeof(double) * (size_t)(3 * nv + 1));
+    memcpy(m->pos, pos, sizeof(double) * (size_t)(3 * nv));
+    m->tets = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)(4 * nt + 1));
+    if (nt) memcpy(m->tets, tets, sizeof(uint32_t) * (size_t)(4 * nt));
+    m->pris = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)(6 * np + 1));
+    if (np) memcpy(m->pris, pris, sizeof(uint32_t) * (size_t)(6 * np));
+    m->hexs = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)(8 * nh + 1));
+    if (nh) memcpy(m->hexs, hexs, sizeof(uint32_t) * (size_t)(8 * nh));
+    m->cid = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nv + 1));
+    memcpy(m->cid, cid, sizeof(int32_t) * (size_t)nv);
+    build_topology(m);
+    om_set_crew(m, OM_SAMPLER_UNIFORM, OM_MEASURER_METRIC_FREE, OM_EVALUATOR_MEAN_RATIO, 1.0, 1.0);
+    return m;
+}
+
+void om_destroy(om_mesh* m)
+{
+    if (!m) return;
+    free(m->pos);
+    free(m->tets);
+    free(m->pris);
+    free(m->hexs);
+    free(m->cid);
+    free(m->ne_base);
+    free(m->ne);
+    free(m->nvx_base);
+    free(m->nvx);
+    free(m->con_kind);
+    free(m->con_param);
+    free(m->con_derived);
+    free(m);
+}
+
+void om_set_constraints(om_mesh* m, int32_t n, const int32_t* kind, const double* params)
+{
+    free(m->con_kind);
+    free(m->con_param);
+    free(m->con_derived);
+    m->ncon = n;
+    m->con_kind = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n + 1));
+    m->con_param = (double*)malloc(sizeof(double) * 6 * (size_t)(n + 1));
+    m->con_derived = (double*)calloc(4 * (size_t)(n + 1), sizeof(double));
+    memcpy(m->con_kind, kind, sizeof(int32_t) * (size_t)n);
+    memcpy(m->con_param, params, sizeof(double) * 6 * (size_t)n);
+    for (int32_t i = 0; i < n; ++i)
+    {
+        double* pp = m->con_param + 6 * i;
+        double* d = m->con_derived + 4 * i;
+        if (kind[i] == OM_CON_PLANE)
+        {
+            /* PlaneConstraint ctor normalizes n (FaceConstraint.cpp:172-176) */
+            v3 nn = normalize(V(pp[3], pp[4], pp[5]));
+            d[0] = nn.x;
+            d[1] = nn.y;
+            d[2] = nn.z;
+        }
+        else if (kind[i] == OM_CON_SEGMENT)
+        {
+            /* SegmentConstraint ctor (EdgeConstraint.cpp:176-181) */
+            v3 a = V(pp[0], pp[1], pp[2]), b = V(pp[3], pp[4], pp[5]);
+            v3 u = normalize(sub(b, a));
+            d[0] = u.x;
+            d[1] = u.y;
+            d[2] = u.z;
+            d[3] = length(sub(b, a));
+        }
+    }
+}
+
+void om_set_crew(om_mesh* m, int32_t sampler, int32_t measurer, int32_t evaluator,
+                 double scaling, double aspect_ratio)
+{
+    m->sampler = sampler;
+    m->measurer = measurer;
+    m->evaluator = evaluator;
+    /* AbstractSampler::setScaling (Samplers/AbstractSampler.cpp:46-51) */
+    m->scaling = scaling;
+    m->scaling2 = m->scaling * scaling;
+    m->scaling3 = m->scaling2 * scaling;
+    m->aspect_ratio = aspect_ratio;
+    /* AbstractSampler ctor rotation (Samplers/AbstractSampler.cpp:30-40) */
+    m3 id = mdiag(1, 1, 1);
+    m->rot = mrotate(id, 3.14159265358979323846 / 4.0, V(0, 0, 1));
+    m->rot = mrotate(m->rot, 3.14159265358979323846 / 4.0, V(0, -1, 0));
+    m->rotinv = mtranspose(m->rot);
+}
+
+void om_get_pos(const om_mesh* m, double* out) { memcpy(out, m->pos, sizeof(double) * 3 * (size_t)m->nv); }
+void om_set_pos(om_mesh* m, const double* in) { memcpy(m->pos, in, sizeof(double) * 3 * (size_t)m->nv); }
+int64_t om_patch_eval_count(const om_mesh* m) { return m->patch_evals; }
+void om_reset_patch_eval_count(om_mesh* m) { m->patch_evals = 0; }
+
+/* ------------------------------------------------------------------------ */
+/* boundary projection                                                       */
+/* ------------------------------------------------------------------------ */
+
+static inline int is_constrained(const om_mesh* m, uint32_t v) { return m->cid[v] != 0; }
+
+static v3 project_id(const om_mesh* m, int32_t id, v3 pos)
+{
+    if (id <= 0 || id >= m->ncon) return pos; /* VolumeConstraint: identity */
+    const double* pp = m->con_param + 6 * id;
+    const double* d = m->con_derived + 4 * id;
+    switch (m->con_kind[id])
+    {
+    case OM_CON_PLANE:
+    {
+        /* PlaneConstraint::operator() (FaceConstraint.cpp:180-185) */
+        v3 n = V(d[0], d[1], d[2]);
+        v3 dist = sub(pos, V(pp[0], pp[1], pp[2]));
+        double l = dot(dist, n);
+        return sub(pos, mul(n, l));
+    }
+    case OM_CON_SEGMENT:
+    {
+        /* SegmentConstraint::operator() (EdgeConstraint.cpp:185-199) */
+        v3 a = V(pp[0], pp[1], pp[2]);
+        v3 u = V(d[0], d[1], d[2]);
+        v3 dist = sub(pos, a);
+        double l = dot(dist, u);
+        if (l < 0) return a;
+        else if (l > d[3]) return V(pp[3], pp[4], pp[5]);
+        else
+        {
+            v3 t = sub(dist, mul(u, l));
+            return sub(pos, t);
+        }
+    }
+    case OM_CON_SPHERE:
+        /* SphereBoundary::Face::operator() (SphereBoundary.cpp:42-45) */
+        return normalize(pos);
+    case OM_CON_POINT:
+        return V(pp[0], pp[1], pp[2]);
+    default:
+        return pos;
+    }
+}
+
+/* (*topo.snapToBoundary)(pos).  A fixed vertex (id < 0) carries a
+ * VertexConstraint built from its own position (MeshTopo(fixedPosition),
+ * DataStructures/Mesh.cpp:149-152; VertexConstraint.cpp:60-63), and fixed
+ * vertices never move, so its projection is its current position. */
+static inline v3 snap(const om_mesh* m, uint32_t v, v3 pos)
+{
+    if (m->cid[v] < 0) return P(m, v);
+    return project_id(m, m->cid[v], pos);
+}
+
+void om_project(const om_mesh* m, int64_t v, const double* in, double* out)
+{
+    v3 r = snap(m, (uint32_t)v, V(in[0], in[1], in[2]));
+    out[0] = r.x;
+    out[1] = r.y;
+    out[2] = r.z;
+}
+
+/* ------------------------------------------------------------------------ */
+/* samplers                                                                  */
+/* ------------------------------------------------------------------------ */
+
+static m3 metric_at(const om_mesh* m, v3 p)
+{
+    switch (m->sampler)
+    {
+    case OM_SAMPLER_ANALYTIC:
+    {
+        /* AbstractSampler::vertMetric(position) (AbstractSampler.cpp:190-208),
+         * returned by AnalyticSampler::metricAt (AnalyticSampler.cpp:45-49) */
+        double x = mmulv(m->rot, p).x * (2.5 * 3.14159265358979323846);
+        double a = m->aspect_ratio;
+        double c = (1.0 - cos(x)) / 2.0;
+        double sizeX = m->scaling * pow(a, pow(c, a));
+        double Mx = sizeX * sizeX;
+        double My = m->scaling2;
+        double Mz = My;
+        m3 Mm = mdiag(Mx, My, Mz);
+        return mmul(mmul(m->rotinv, Mm), m->rot);
+    }
+    case OM_SAMPLER_SINE:
+    {
+        /* sine-graded anisotropic metric s^2 * diag(1 + 9 sin^2(4 pi x), 1, 1):
+         * a new sampler plugin with the shape of UniformSampler::metricAt */
+        double sx = sin(4.0 * 3.14159265358979323846 * p.x);
+        double s2 = m->scaling2;
+        return mdiag(s2 * (1.0 + 9.0 * sx * sx), s2, s2);
+    }
+    default:
+        /* UniformSampler::metricAt (UniformSampler.cpp:45-51) */
+        return mdiag(m->scaling * m->scaling, m->scaling * m->scaling, m->scaling * m->scaling);
+    }
+}
+
+void om_metric_at(const om_mesh* m, const double* p, double* out9)
+{
+    m3 r = metric_at(m, V(p[0], p[1], p[2]));
+    memcpy(out9, &r, sizeof(double) * 9);
+}
+
+/* ------------------------------------------------------------------------ */
+/* measurers                                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* MetricWiseMeasurer::riemannianDistance, localized segment division
+ * (Measurers/MetricWiseMeasurer.cpp:9,64-116) */
+static double metric_wise_distance(const om_mesh* m, v3 a, v3 b)
+{
+    const double DIFF_THRESHOLD = 0.01;
+    int curr = 0;
+    int base = 2;
+    double len = 0.0;
+    v3 d = sub(b, a);
+    v3 bv = dvs(d, (double)base);
+    while (curr < base)
+    {
+        double p0 = (curr + 0.5) / base;
+        double p1 = (curr + 1.5) / base;
+        m3 M0 = metric_at(m, add(a, mul(d, p0)));
+        m3 M1 = metric_at(m, add(a, mul(d, p1)));
+        double l0 = sqrt(dot(bv, mmulv(M0, bv)));
+        double l1 = sqrt(dot(bv, mmulv(M1, bv)));
+        double sum = (l0 + l1);
+        double diff = fabs(l0 - l1) / (sum / 2.0);
+        if (diff < DIFF_THRESHOLD)
+        {
+            len += sum;
+            curr += 2;
+            if ((curr & 2) == 0)
+            {
+                base >>= 1;
+                curr >>= 1;
+            }
+            bv = dvs(d, (double)base);
+        }
+        else
+        {
+            base <<= 1;
+            curr <<= 1;
+            bv = dvs(bv, 2.0);
+        }
+    }
+    return len;
+}
+
+double om_riemannian_distance(const om_mesh* m, const double* a, const double* b)
+{
+    v3 A = V(a[0], a[1], a[2]), B = V(b[0], b[1], b[2]);
+    if (m->measurer == OM_MEASURER_METRIC_WISE) return metric_wise_distance(m, A, B);
+    return length(sub(B, A)) * m->scaling;
+}
+
+/* riemannianSegment: MetricFreeMeasurer.cpp:36-43 / MetricWiseMeasurer.cpp:119-126 */
+static inline v3 segment(const om_mesh* m, v3 a, v3 b)
+{
+    if (m->measurer == OM_MEASURER_METRIC_WISE)
+        return mul(normalize(sub(b, a)), metric_wise_distance(m, a, b));
+    return mul(sub(b, a), m->scaling);
+}
+
+/* tet/pri/hex volumes: MetricFreeMeasurer.cpp:45-105, MetricWiseMeasurer.cpp:128-188 */
+static double tet_volume(const om_mesh* m, const v3* vp)
+{
+    if (m->measurer == OM_MEASURER_METRIC_WISE)
+    {
+        double detSum = mdet(M(segment(m, vp[0], vp[3]), segment(m, vp[1], vp[3]),
+                               segment(m, vp[2], vp[3])));
+        return detSum / 6.0;
+    }
+    double detSum = mdet(M(sub(vp[3], vp[0]), sub(vp[3], vp[1]), sub(vp[3], vp[2])));
+    return m->scaling3 * detSum / 6.0;
+}
+
+static double pri_volume(const om_mesh* m, const v3* vp)
+{
+    v3 e02, e12, e32, e42, e52;
+    if (m->measurer == OM_MEASURER_METRIC_WISE)
+    {
+        e02 = segment(m, vp[0], vp[2]);
+        e12 = segment(m, vp[1], vp[2]);
+        e32 = segment(m, vp[3], vp[2]);
+        e42 = segment(m, vp[4], vp[2]);
+        e52 = segment(m, vp[5], vp[2]);
+    }
+    else
+    {
+        e02 = sub(vp[2], vp[0]);
+        e12 = sub(vp[2], vp[1]);
+        e32 = sub(vp[2], vp[3]);
+        e42 = sub(vp[2], vp[4]);
+        e52 = sub(vp[2], vp[5]);
+    }
+    double detSum = 0.0;
+    detSum += mdet(M(e32, e52, e42));
+    detSum += mdet(M(e02, e32, e42));
+    detSum += mdet(M(e12, e02, e42));
+    if (m->measurer == OM_MEASURER_METRIC_WISE) return detSum / 6.0;
+    return m->scaling3 * detSum / 6.0;
+}
+
+static double hex_volume(const om_mesh* m, const v3* vp)
+{
+    double detSum = 0.0;
+    if (m->measurer == OM_MEASURER_METRIC_WISE)
+    {
+        detSum += mdet(M(segment(m, vp[1], vp[0]), segment(m, vp[4], vp[0]), segment(m, vp[3], vp[0])));
+        detSum += mdet(M(segment(m, vp[1], vp[2]), segment(m, vp[3], vp[2]), segment(m, vp[6], vp[2])));
+        detSum += mdet(M(segment(m, vp[4], vp[5]), segment(m, vp[1], vp[5]), segment(m, vp[6], vp[5])));
+        detSum += mdet(M(segment(m, vp[4], vp[7]), segment(m, vp[6], vp[7]), segment(m, vp[3], vp[7])));
+        detSum += mdet(M(segment(m, vp[1], vp[4]), segment(m, vp[6], vp[4]), segment(m, vp[3], vp[4])));
+        return detSum / 6.0;
+    }
+    detSum += mdet(M(sub(vp[0], vp[1]), sub(vp[0], vp[4]), sub(vp[0], vp[3])));
+    detSum += mdet(M(sub(vp[2], vp[1]), sub(vp[2], vp[3]), sub(vp[2], vp[6])));
+    detSum += mdet(M(sub(vp[5], vp[4]), sub(vp[5], vp[1]), sub(vp[5], vp[6])));
+    detSum += mdet(M(sub(vp[7], vp[4]), sub(vp[7], vp[6]), sub(vp[7], vp[3])));
+    detSum += mdet(M(sub(vp[4], vp[1]), sub(vp[4], vp[6]), sub(vp[4], vp[3])));
+    return m->scaling3 * detSum / 6.0;
+}
+
+/* AbstractMeasurer::computeLocalElementSize (Measurers/AbstractMeasurer.cpp:137-155) */
+static double local_size(const om_mesh* m, uint32_t v)
+{
+    v3 pos = P(m, v);
+    double total = 0.0;
+    int64_t b = m->nvx_base[v], e = m->nvx_base[v + 1];
+    for (int64_t n = b; n < e; ++n) total += length(sub(pos, P(m, m->nvx[n])));
+    return total / (double)(e - b);
+}
+
+double om_local_size(const om_mesh* m, int64_t v) { return local_size(m, (uint32_t)v); }
+
+/* ------------------------------------------------------------------------ */
+/* evaluators                                                                */
+/* ------------------------------------------------------------------------ */
+
+/* MeanRatioEvaluator::cornerQuality (Evaluators/MeanRatioEvaluator.cpp:22-32) */
+static inline double corner_quality(m3 Fk)
+{
+    double det = mdet(Fk);
+    double frob2 = dot(Fk.c[0], Fk.c[0]) + dot(Fk.c[1], Fk.c[1]) + dot(Fk.c[2], Fk.c[2]);
+    return gsign(det) * 3.0 * pow(fabs(det), 2.0 / 3.0) / frob2;
+}
+
+/* combine corner qualities: min if any <= 0, else harmonic mean
+ * (MeanRatioEvaluator.cpp:91-110, 140-166) */
+static inline double combine_corners(const double* q, int n)
+{
+    int bad = 0;
+    for (int i = 0; i < n; ++i)
+        if (q[i] <= 0.0) bad = 1;
+    if (bad)
+    {
+        double mn = q[0];
+        for (int i = 1; i < n; ++i)
+            if (q[i] < mn) mn = q[i];
+        return mn;
+    }
+    double s = 1 / q[0];
+    for (int i = 1; i < n; ++i) s = s + 1 / q[i];
+    return (double)n / s;
+}
+
+/* MeanRatioEvaluator::tetQuality (MeanRatioEvaluator.cpp:34-50) */
+static double mr_tet(const om_mesh* m, const v3* vp)
+{
+    v3 e03 = segment(m, vp[0], vp[3]);
+    v3 e13 = segment(m, vp[1], vp[3]);
+    v3 e23 = segment(m, vp[2], vp[3]);
+    m3 Fk0 = mmul(M(e03, e13, e23), *fr_tet_inv());
+    return corner_quality(Fk0);
+}
+
+/* MeanRatioEvaluator::priQuality (MeanRatioEvaluator.cpp:52-111) */
+static double mr_pri(const om_mesh* m, const v3* vp)
+{
+    v3 e03 = segment(m, vp[0], vp[3]);
+    v3 e14 = segment(m, vp[1], vp[4]);
+    v3 e25 = segment(m, vp[2], vp[5]);
+    v3 e01 = segment(m, vp[0], vp[1]);
+    v3 e12 = segment(m, vp[1], vp[2]);
+    v3 e20 = segment(m, vp[2], vp[0]);
+    v3 e34 = segment(m, vp[3], vp[4]);
+    v3 e45 = segment(m, vp[4], vp[5]);
+    v3 e53 = segment(m, vp[5], vp[3]);
+    const m3* F = fr_pri_inv();
+    double q[6];
+    q[0] = corner_quality(mmul(M(neg(e01), e20, e03), *F));
+    q[1] = corner_quality(mmul(M(neg(e12), e01, e14), *F));
+    q[2] = corner_quality(mmul(M(neg(e20), e12, e25), *F));
+    q[3] = corner_quality(mmul(M(neg(e34), e53, e03), *F));
+    q[4] = corner_quality(mmul(M(neg(e45), e34, e14), *F));
+    q[5] = corner_quality(mmul(M(neg(e53), e45, e25), *F));
+    return combine_corners(q, 6);
+}
+
+/* MeanRatioEvaluator::hexQuality (MeanRatioEvaluator.cpp:113-167); note the
+ * reference passes hex.c[3] for e23, which only matters for local samplers */
+static double mr_hex(const om_mesh* m, const v3* vp)
+{
+    v3 e01 = segment(m, vp[0], vp[1]);
+    v3 e03 = segment(m, vp[0], vp[3]);
+    v3 e04 = segment(m, vp[0], vp[4]);
+    v3 e12 = segment(m, vp[1], vp[2]);
+    v3 e15 = segment(m, vp[1], vp[5]);
+    v3 e23 = segment(m, vp[2], vp[3]);
+    v3 e26 = segment(m, vp[2], vp[6]);
+    v3 e37 = segment(m, vp[3], vp[7]);
+    v3 e45 = segment(m, vp[4], vp[5]);
+    v3 e47 = segment(m, vp[4], vp[7]);
+    v3 e56 = segment(m, vp[5], vp[6]);
+    v3 e67 = segment(m, vp[6], vp[7]);
+    double q[8];
+    q[0] = corner_quality(M(e01, e04, neg(e03)));
+    q[1] = corner_quality(M(e01, e12, e15));
+    q[2] = corner_quality(M(e12, e26, neg(e23)));
+    q[3] = corner_quality(M(e03, e23, e37));
+    q[4] = corner_quality(M(e04, e45, e47));
+    q[5] = corner_quality(M(e15, neg(e56), e45));
+    q[6] = corner_quality(M(e26, e56, e67));
+    q[7] = corner_quality(M(e37, e67, neg(e47)));
+    return combine_corners(q, 8);
+}
+
+/* MetricConformityEvaluator::specifiedMetric (MetricConformityEvaluator.cpp:25-44) */
+static m3 specified_metric(const om_mesh* m, v3 v0, v3 v1, v3 v2, v3 v3_)
+{
+    const double H = 0.5;
+    const double Q = (1.0 - H) / 3.0;
+    m3 r = mscale(metric_at(m, dvs(add(add(add(v0, v1), v2), v3_), 4.0)), -0.8);
+    r = madd(r, mscale(metric_at(m, add(add(add(mul(v0, H), mul(v1, Q)), mul(v2, Q)), mul(v3_, Q))), 0.45));
+    r = madd(r, mscale(metric_at(m, add(add(add(mul(v0, Q), mul(v1, H)), mul(v2, Q)), mul(v3_, Q))), 0.45));
+    r = madd(r, mscale(metric_at(m, add(add(add(mul(v0, Q), mul(v1, Q)), mul(v2, H)), mul(v3_, Q))), 0.45));
+    r = madd(r, mscale(metric_at(m, add(add(add(mul(v0, Q), mul(v1, Q)), mul(v2, Q)), mul(v3_, H))), 0.45));
+    return r;
+}
+
+/* MetricConformityEvaluator::metricConformity (MetricConformityEvaluator.cpp:46-71) */
+static double metric_conformity(m3 Fk, m3 Ms)
+{
+    m3 Fk_inv = minverse(mtranspose(Fk));
+    m3 Mk = mmul(Fk_inv, mtranspose(Fk_inv));
+    m3 Mk_inv = minverse(Mk);
+    m3 Ms_inv = minverse(Ms);
+    m3 tNc = msub(madd(mmul(Mk_inv, Ms), mmul(Ms_inv, Mk)), mdiag(2.0, 2.0, 2.0));
+    double frob2 = dot(tNc.c[0], tNc.c[0]) + dot(tNc.c[1], tNc.c[1]) + dot(tNc.c[2], tNc.c[2]);
+    if (!isnan(frob2))
+    {
+        double Fk_sign = gsign(mdet(Fk));
+        return Fk_sign / sqrt(1.0 + sqrt(frob2));
+    }
+    return 0.0;
+}
+
+/* MetricConformityEvaluator::tetQuality (MetricConformityEvaluator.cpp:73-89) */
+static double mc_tet(const om_mesh* m, const v3* vp)
+{
+    v3 e03 = sub(vp[3], vp[0]);
+    v3 e13 = sub(vp[3], vp[1]);
+    v3 e23 = sub(vp[3], vp[2]);
+    m3 Fk = mmul(M(e03, e13, e23), *fr_tet_inv());
+    m3 Ms0 = specified_metric(m, vp[0], vp[1], vp[2], vp[3]);
+    return metric_conformity(Fk, Ms0);
+}
+
+/* MetricConformityEvaluator::priQuality (MetricConformityEvaluator.cpp:91-148) */
+static double mc_pri(const om_mesh* m, const v3* vp)
+{
+    v3 e03 = sub(vp[3], vp[0]);
+    v3 e14 = sub(vp[4], vp[1]);
+    v3 e25 = sub(vp[5], vp[2]);
+    v3 e01 = sub(vp[1], vp[0]);
+    v3 e12 = sub(vp[2], vp[1]);
+    v3 e20 = sub(vp[0], vp[2]);
+    v3 e34 = sub(vp[4], vp[3]);
+    v3 e45 = sub(vp[5], vp[4]);
+    v3 e53 = sub(vp[3], vp[5]);
+    const m3* F = fr_pri_inv();
+    double q[6];
+    q[0] = metric_conformity(mmul(M(neg(e01), e20, e03), *F), specified_metric(m, vp[0], vp[1], vp[2], vp[3]));
+    q[1] = metric_conformity(mmul(M(neg(e12), e01, e14), *F), specified_metric(m, vp[0], vp[1], vp[2], vp[4]));
+    q[2] = metric_conformity(mmul(M(neg(e20), e12, e25), *F), specified_metric(m, vp[0], vp[1], vp[2], vp[5]));
+    q[3] = metric_conformity(mmul(M(neg(e34), e53, e03), *F), specified_metric(m, vp[0], vp[3], vp[4], vp[5]));
+    q[4] = metric_conformity(mmul(M(neg(e45), e34, e14), *F), specified_metric(m, vp[1], vp[3], vp[4], vp[5]));
+    q[5] = metric_conformity(mmul(M(neg(e53), e45, e25), *F), specified_metric(m, vp[2], vp[3], vp[4], vp[5]));
+    return combine_corners(q, 6);
+}
+
+/* MetricConformityEvaluator::hexQuality (MetricConformityEvaluator.cpp:150-224) */
+static double mc_hex(const om_mesh* m, const v3* vp)
+{
+    v3 e01 = sub(vp[1], vp[0]);
+    v3 e03 = sub(vp[3], vp[0]);
+    v3 e04 = sub(vp[4], vp[0]);
+    v3 e12 = sub(vp[2], vp[1]);
+    v3 e15 = sub(vp[5], vp[1]);
+    v3 e23 = sub(vp[3], vp[2]);
+    v3 e26 = sub(vp[6], vp[2]);
+    v3 e37 = sub(vp[7], vp[3]);
+    v3 e45 = sub(vp[5], vp[4]);
+    v3 e47 = sub(vp[7], vp[4]);
+    v3 e56 = sub(vp[6], vp[5]);
+    v3 e67 = sub(vp[7], vp[6]);
+    double q[8];
+    q[0] = metric_conformity(M(e01, e04, neg(e03)), specified_metric(m, vp[0], vp[1], vp[3], vp[4]));
+    q[1] = metric_conformity(M(e01, e12, e15), specified_metric(m, vp[0], vp[1], vp[2], vp[5]));
+    q[2] = metric_conformity(M(e12, e26, neg(e23)), specified_metric(m, vp[1], vp[2], vp[3], vp[6]));
+    q[3] = metric_conformity(M(e03, e23, e37), specified_metric(m, vp[0], vp[2], vp[3], vp[7]));
+    q[4] = metric_conformity(M(e04, e45, e47), specified_metric(m, vp[0], vp[4], vp[5], vp[7]));
+    q[5] = metric_conformity(M(e15, neg(e56), e45), specified_metric(m, vp[1], vp[4], vp[5], vp[6]));
+    q[6] = metric_conformity(M(e26, e56, e67), specified_metric(m, vp[2], vp[5], vp[6], vp[7]));
+    q[7] = metric_conformity(M(e37, e67, neg(e47)), specified_metric(m, vp[3], vp[4], vp[6], vp[7]));
+    return combine_corners(q, 8);
+}
+
+static double quality_vp(const om_mesh* m, int type, const v3* vp)
+{
+    if (m->evaluator == OM_EVALUATOR_METRIC_CONFORMITY)
+    {
+        if (type == OM_TET) return mc_tet(m, vp);
+        if (type == OM_PRI) return mc_pri(m, vp);
+        if (type == OM_HEX) return mc_hex(m, vp);
+    }
+    else
+    {
+        if (type == OM_TET) return mr_tet(m, vp);
+        if (type == OM_PRI) return mr_pri(m, vp);
+        if (type == OM_HEX) return mr_hex(m, vp);
+    }
+    return 0.0;
+}
+
+static inline const uint32_t* elem_verts(const om_mesh* m, int type, int64_t idx, int* n)
+{
+    if (type == OM_TET) { *n = 4; return m->tets + 4 * idx; }
+    if (type == OM_PRI) { *n = 6; return m->pris + 6 * idx; }
+    *n = 8;
+    return m->hexs + 8 * idx;
+}
+
+static double element_quality(const om_mesh* m, int type, int64_t idx)
+{
+    int n;
+    const uint32_t* e = elem_verts(m, type, idx, &n);
+    v3 vp[8];
+    for (int k = 0; k < n; ++k) vp[k] = P(m, e[k]);
+    return quality_vp(m, type, vp);
+}
+
+double om_element_quality(const om_mesh* m, int32_t type, int64_t idx) { return element_quality(m, type, idx); }
+
+/* AbstractEvaluator::patchQuality + accumulatePatchQuality +
+ * finalizePatchQuality (Evaluators/AbstractEvaluator.cpp:236-279, 778-803) */
+static double patch_quality(const om_mesh* m, uint32_t v)
+{
+    double weight = 0.0, quality = 0.0;
+    for (int64_t n = m->ne_base[v]; n < m->ne_base[v + 1]; ++n)
+    {
+        const neig_elem* ne = &m->ne[n];
+        double q = element_quality(m, ne->type, ne->id);
+        if (weight != -1.0 && q > 0.0)
+        {
+            weight += 1.0;
+            quality += 1 / q;
+        }
+        else
+        {
+            weight = -1.0;
+            quality = gmin(quality, q);
+        }
+    }
+    if (weight > 0.0) return weight / quality;
+    return quality;
+}
+
+double om_patch_quality(const om_mesh* m, int64_t v) { return patch_quality(m, (uint32_t)v); }
+
+/* QualityHistogram::add (DataStructures/QualityHistogram.cpp:63-76).  The
+ * reference's size_t(value*20) is undefined for negative values; it is
+ * read here as bucket 0. */
+typedef struct
+{
+    double mn, inv_sum, count;
+    double buckets[OM_HIST_BUCKETS];
+} hist;
+
+static inline void hist_add(hist* h, double value)
+{
+    h->count += 1;
+    h->mn = gmin(h->mn, value);
+    if (value > 0.0) h->inv_sum += 1.0 / value;
+    else h->inv_sum = INFINITY;
+    double b = value * OM_HIST_BUCKETS;
+    int64_t bi = (b > 0.0) ? (int64_t)b : 0;
+    if (bi > OM_HIST_BUCKETS - 1) bi = OM_HIST_BUCKETS - 1;
+    h->buckets[bi] += 1;
+}
+
+typedef struct
+{
+    const om_mesh* m;
+    int t, nthreads;
+    hist h;
+} eval_job;
+
+static void* eval_worker(void* arg)
+{
+    /* AbstractEvaluator::evaluateMeshQualityThread (AbstractEvaluator.cpp:404-453):
+     * contiguous element ranges per worker, per-worker histograms merged in
+     * worker order */
+    eval_job* j = (eval_job*)arg;
+    const om_mesh* m = j->m;
+    int64_t T = j->nthreads, t = j->t;
+    int64_t tb = (m->nt * t) / T, te = (m->nt * (t + 1)) / T;
+    int64_t pb = (m->np * t) / T, pe = (m->np * (t + 1)) / T;
+    int64_t hb = (m->nh * t) / T, he = (m->nh * (t + 1)) / T;
+    for (int64_t i = tb; i < te; ++i) hist_add(&j->h, element_quality(m, OM_TET, i));
+    for (int64_t i = pb; i < pe; ++i) hist_add(&j->h, element_quality(m, OM_PRI, i));
+    for (int64_t i = hb; i < he; ++i) hist_add(&j->h, element_quality(m, OM_HEX, i));
+    return NULL;
+}
+
+void om_evaluate(const om_mesh* m, double* out, int32_t nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    hist total;
+    memset(&total, 0, sizeof(total));
+    total.mn = 1.0;
+    eval_job* jobs = (eval_job*)calloc((size_t)nthreads, sizeof(eval_job));
+    pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+    for (int t = 0; t < nthreads; ++t)
+    {
+        jobs[t].m = m;
+        jobs[t].t = t;
+        jobs[t].nthreads = nthreads;
+        jobs[t].h.mn = 1.0;
+        if (nthreads == 1) eval_worker(&jobs[t]);
+        else pthread_create(&th[t], NULL, eval_worker, &jobs[t]);
+    }
+    for (int t = 0; t < nthreads; ++t)
+    {
+        if (nthreads > 1) pthread_join(th[t], NULL);
+        /* QualityHistogram::merge (QualityHistogram.cpp:78-92) */
+        if (jobs[t].h.count == 0) continue;
+        total.count += jobs[t].h.count;
+        total.mn = gmin(total.mn, jobs[t].h.mn);
+        total.inv_sum += jobs[t].h.inv_sum;
+        for (int b = 0; b < OM_HIST_BUCKETS; ++b) total.buckets[b] += jobs[t].h.buckets[b];
+    }
+    out[0] = total.mn;
+    out[1] = total.inv_sum;
+    out[2] = total.count;
+    for (int b = 0; b < OM_HIST_BUCKETS; ++b) out[3 + b] = total.buckets[b];
+    free(jobs);
+    free(th);
+}
+
+/* ------------------------------------------------------------------------ */
+/* vertex-wise smoothers                                                     */
+/* ------------------------------------------------------------------------ */
+
+typedef struct { double x, y, z, w; } v4;
+static inline v4 V4(v3 p, double w) { v4 r = {p.x, p.y, p.z, w}; return r; }
+static inline v3 xyz(v4 a) { return V(a.x, a.y, a.z); }
+static inline void swap4(v4* a, v4* b) { v4 t = *a; *a = *b; *b = t; }
+
+typedef struct
+{
+    double p[8];
+} smooth_params;
+
+/* evaluate the patch of v with the vertex at `at` (the reference writes the
+ * trial position into verts[vId] and calls patchQuality) */
+static inline double eval_at(om_mesh* m, uint32_t v, v3 at, int64_t* evals)
+{
+    setP(m, v, at);
+    ++*evals;
+    return patch_quality(m, v);
+}
+
+/* NelderMeadSmoother::smoothVertices (Smoothers/VertexWise/NelderMeadSmoother.cpp:100-260) */
+static void nm_vertex(om_mesh* m, uint32_t vId, const smooth_params* sp, int64_t* evals)
+{
+    const double shiftFactor = sp->p[0];
+    const int securityCycles = (int)sp->p[1];
+    const double valueConvergence = sp->p[2];
+    const double alpha = sp->p[3], beta = sp->p[4], gamma = sp->p[5];
+    const int constrained = is_constrained(m, vId);
+
+    double localSize = local_size(m, vId);
+    double nodeShift = localSize * shiftFactor;
+
+    v3 pos = P(m, vId);
+    ++*evals;
+    v4 vo = V4(pos, patch_quality(m, vId));
+    v4 simplex[4] = {V4(add(pos, V(nodeShift, 0, 0)), 0), V4(add(pos, V(0, nodeShift, 0)), 0),
+                     V4(add(pos, V(0, 0, nodeShift)), 0), vo};
+
+    int cycle = 0;
+    int reset = 0;
+    int terminated = 0;
+    while (!terminated)
+    {
+        for (int p = 0; p < 3; ++p)
+        {
+            pos = xyz(simplex[p]);
+            if (constrained) pos = snap(m, vId, pos);
+            simplex[p] = V4(pos, eval_at(m, vId, pos, evals));
+        }
+
+        if (simplex[0].w > simplex[1].w) swap4(&simplex[0], &simplex[1]);
+        if (simplex[1].w > simplex[2].w) swap4(&simplex[1], &simplex[2]);
+        if (simplex[2].w > simplex[3].w) swap4(&simplex[2], &simplex[3]);
+        if (simplex[0].w > simplex[1].w) swap4(&simplex[0], &simplex[1]);
+        if (simplex[1].w > simplex[2].w) swap4(&simplex[1], &simplex[2]);
+        if (simplex[0].w > simplex[1].w) swap4(&simplex[0], &simplex[1]);
+
+        for (; cycle < securityCycles; ++cycle)
+        {
+            v3 c = mul(add(add(xyz(simplex[1]), xyz(simplex[2])), xyz(simplex[3])), 1 / 3.0);
+            double f = 0.0;
+
+            pos = add(c, mul(sub(c, xyz(simplex[0])), alpha));
+            if (constrained) pos = snap(m, vId, pos);
+            double fr = f = eval_at(m, vId, pos, evals);
+            v3 xr = pos;
+
+            if (simplex[3].w < fr)
+            {
+                pos = add(c, mul(sub(pos, c), gamma));
+                if (constrained) pos = snap(m, vId, pos);
+                double fe = f = eval_at(m, vId, pos, evals);
+                if (fe <= fr)
+                {
+                    pos = xr;
+                    f = fr;
+                }
+            }
+            else if (simplex[1].w >= fr)
+            {
+                if (fr > simplex[0].w)
+                {
+                    pos = add(c, mul(sub(xr, c), beta));
+                    if (constrained) pos = snap(m, vId, pos);
+                    f = eval_at(m, vId, pos, evals);
+                }
+                else
+                {
+                    pos = add(c, mul(sub(xyz(simplex[0]), c), beta));
+                    if (constrained) pos = snap(m, vId, pos);
+                    f = eval_at(m, vId, pos, evals);
+                }
+            }
+
+            v4 vertex = V4(pos, f);
+            if (vertex.w > simplex[3].w) swap4(&simplex[3], &vertex);
+            if (vertex.w > simplex[2].w) swap4(&simplex[2], &vertex);
+            if (vertex.w > simplex[1].w) swap4(&simplex[1], &vertex);
+            if (vertex.w > simplex[0].w) swap4(&simplex[0], &vertex);
+
+            if ((simplex[3].w - simplex[1].w) < valueConvergence)
+            {
+                terminated = 1;
+                break;
+            }
+        }
+
+        if (terminated || (cycle >= securityCycles && reset)) break;
+        simplex[0] = V4(sub(xyz(vo), V(nodeShift, 0, 0)), vo.w);
+        simplex[1] = V4(sub(xyz(vo), V(0, nodeShift, 0)), vo.w);
+        simplex[2] = V4(sub(xyz(vo), V(0, 0, nodeShift)), vo.w);
+        simplex[3] = vo;
+        reset = 1;
+        cycle = 0;
+    }
+
+    pos = xyz(simplex[3]);
+    if (constrained) pos = snap(m, vId, pos);
+    setP(m, vId, pos);
+}
+
+/* GradientDescentSmoother::smoothVertices (Smoothers/VertexWise/GradientDescentSmoother.cpp:73-202) */
+static void gd_vertex(om_mesh* m, uint32_t vId, const smooth_params* sp, int64_t* evals)
+{
+    const double shiftFactor = sp->p[0];
+    const int securityCycles = (int)sp->p[1];
+    const int constrained = is_constrained(m, vId);
+    static const double OFFSETS[8] = {-0.25, 0.00, 0.10, 0.20, 0.40, 0.80, 1.20, 1.60};
+
+    double localSize = local_size(m, vId);
+    double nodeShift = localSize * shiftFactor;
+    double originalNodeShift = nodeShift;
+
+    for (int c = 0; c < securityCycles; ++c)
+    {
+        v3 pos = P(m, vId);
+        double q[6];
+        v3 g[6] = {add(pos, V(-nodeShift, 0.0, 0.0)), add(pos, V(nodeShift, 0.0, 0.0)),
+                   add(pos, V(0.0, -nodeShift, 0.0)), add(pos, V(0.0, nodeShift, 0.0)),
+                   add(pos, V(0.0, 0.0, -nodeShift)), add(pos, V(0.0, 0.0, nodeShift))};
+        if (constrained)
+            for (int p = 0; p < 6; ++p) g[p] = snap(m, vId, g[p]);
+        v3 originalPos = pos;
+        for (int p = 0; p < 6; ++p) q[p] = eval_at(m, vId, g[p], evals);
+        pos = originalPos;
+        setP(m, vId, pos);
+
+        v3 gradQ = V(q[1] - q[0], q[3] - q[2], q[5] - q[4]);
+        double gradQNorm = length(gradQ);
+        if (gradQNorm == 0) break;
+
+        v3 shift = mul(gradQ, nodeShift / gradQNorm);
+        v3 props[8];
+        for (int p = 0; p < 8; ++p) props[p] = add(pos, mul(shift, OFFSETS[p]));
+        if (constrained)
+            for (int p = 0; p < 8; ++p) props[p] = snap(m, vId, props[p]);
+
+        int best = 0;
+        double bestQ = -INFINITY;
+        for (int p = 0; p < 8; ++p)
+        {
+            double pq = eval_at(m, vId, props[p], evals);
+            if (pq > bestQ)
+            {
+                bestQ = pq;
+                best = p;
+            }
+        }
+        setP(m, vId, props[best]);
+
+        nodeShift *= fabs(OFFSETS[best]);
+        if (nodeShift < originalNodeShift / 10.0) break;
+    }
+}
+
+/* SpawnSearchSmoother offsets (SpawnSearchSmoother.cpp:33-55) and
+ * smoothVertices (SpawnSearchSmoother.cpp:161-226) */
+static v3 SPAWN_OFFSETS[64];
+static pthread_once_t spawn_once = PTHREAD_ONCE_INIT;
+static void spawn_init(void)
+{
+    int n = 0;
+    for (int k = 0; k < 4; ++k)
+        for (int j = 0; j < 4; ++j)
+            for (int i = 0; i < 4; ++i) SPAWN_OFFSETS[n++] = sub(V(i, j, k), V(1.5, 1.5, 1.5));
+    SPAWN_OFFSETS[0] = V(0, 0, 0);
+}
+
+static void spawn_vertex(om_mesh* m, uint32_t vId, const smooth_params* sp, int64_t* evals)
+{
+    pthread_once(&spawn_once, spawn_init);
+    const double moveCoeff = sp->p[0];
+    const int iterations = (int)sp->p[1];
+    const int constrained = is_constrained(m, vId);
+    double localSize = local_size(m, vId);
+    double scale = moveCoeff * localSize;
+    for (int iter = 0; iter < iterations; ++iter)
+    {
+        v3 pos = P(m, vId);
+        v3 props[64];
+        for (int p = 0; p < 64; ++p) props[p] = add(pos, mul(SPAWN_OFFSETS[p], scale));
+        if (constrained)
+            for (int p = 0; p < 64; ++p) props[p] = snap(m, vId, props[p]);
+        int best = 0;
+        double bestQ = -INFINITY;
+        for (int p = 0; p < 64; ++p)
+        {
+            double pq = eval_at(m, vId, props[p], evals);
+            if (pq > bestQ)
+            {
+                bestQ = pq;
+                best = p;
+            }
+        }
+        setP(m, vId, props[best]);
+        scale /= 3.0;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* GETMe (element-wise)                                                      */
+/* ------------------------------------------------------------------------ */
+
+/* per (element, corner) transformed position and the element's weight */
+typedef struct
+{
+    v3 p;
+    double w;
+} corner_out;
+
+/* GetmeSmoother::smoothTets (Smoothers/ElementWise/GetmeSmoother.cpp:55-125) */
+static void getme_tet(const om_mesh* m, int64_t eId, double lambda, corner_out* out)
+{
+    const uint32_t* vi = m->tets + 4 * eId;
+    v3 vp[4], vpp[4];
+    for (int k = 0; k < 4; ++k) vp[k] = P(m, vi[k]);
+    v3 n[4] = {cross(sub(vp[3], vp[1]), sub(vp[2], vp[1])), cross(sub(vp[3], vp[2]), sub(vp[0], vp[2])),
+               cross(sub(vp[1], vp[3]), sub(vp[0], vp[3])), cross(sub(vp[1], vp[0]), sub(vp[2], vp[0]))};
+    for (int k = 0; k < 4; ++k) vpp[k] = add(vp[k], mul(n[k], lambda / sqrt(length(n[k]))));
+    double volume = tet_volume(m, vp);
+    double volumePrime = tet_volume(m, vpp);
+    double absVolumeRation = fabs(volume / volumePrime);
+    double volumeVar = pow(absVolumeRation, 1.0 / 3.0);
+    v3 center = mul(add(add(add(vp[0], vp[1]), vp[2]), vp[3]), 1.0 / 4.0);
+    for (int k = 0; k < 4; ++k) vpp[k] = add(center, mul(sub(vpp[k], center), volumeVar));
+    for (int k = 0; k < 4; ++k)
+        if (is_constrained(m, vi[k])) vpp[k] = snap(m, vi[k], vpp[k]);
+    double quality = quality_vp(m, OM_TET, vp);
+    double qualityPrime = quality_vp(m, OM_TET, vpp);
+    double weight = qualityPrime / (1.0 + quality);
+    for (int k = 0; k < 4; ++k)
+    {
+        out[k].p = vpp[k];
+        out[k].w = weight;
+    }
+}
+
+/* GetmeSmoother::smoothPris (GetmeSmoother.cpp:127-233) */
+static void getme_pri(const om_mesh* m, int64_t eId, double lambda, corner_out* out)
+{
+    const uint32_t* vi = m->pris + 6 * eId;
+    v3 vp[6], vpp[6];
+    for (int k = 0; k < 6; ++k) vp[k] = P(m, vi[k]);
+    v3 aux[5] = {dvs(add(add(vp[0], vp[1]), vp[2]), 3.0),
+                 dvs(add(add(add(vp[0], vp[1]), vp[4]), vp[3]), 4.0),
+                 dvs(add(add(add(vp[1], vp[2]), vp[5]), vp[4]), 4.0),
+                 dvs(add(add(add(vp[2], vp[0]), vp[3]), vp[5]), 4.0),
+                 dvs(add(add(vp[3], vp[4]), vp[5]), 3.0)};
+    v3 n[6] = {cross(sub(aux[1], aux[0]), sub(aux[3], aux[0])), cross(sub(aux[2], aux[0]), sub(aux[1], aux[0])),
+               cross(sub(aux[3], aux[0]), sub(aux[2], aux[0])), cross(sub(aux[3], aux[4]), sub(aux[1], aux[4])),
+               cross(sub(aux[1], aux[4]), sub(aux[2], aux[4])), cross(sub(aux[2], aux[4]), sub(aux[3], aux[4]))};
+    double t = (4.0 / 5.0) * (1.0 - pow(4.0 / 39.0, 0.25) * lambda);
+    double it = 1.0 - t;
+    v3 bases[6] = {add(mul(aux[0], it), dvs(mul(add(aux[3], aux[1]), t), 2.0)),
+                   add(mul(aux[0], it), dvs(mul(add(aux[1], aux[2]), t), 2.0)),
+                   add(mul(aux[0], it), dvs(mul(add(aux[2], aux[3]), t), 2.0)),
+                   add(mul(aux[4], it), dvs(mul(add(aux[3], aux[1]), t), 2.0)),
+                   add(mul(aux[4], it), dvs(mul(add(aux[1], aux[2]), t), 2.0)),
+                   add(mul(aux[4], it), dvs(mul(add(aux[2], aux[3]), t), 2.0))};
+    for (int k = 0; k < 6; ++k) vpp[k] = add(bases[k], mul(n[k], lambda / sqrt(length(n[k]))));
+    double volume = pri_volume(m, vp);
+    double volumePrime = pri_volume(m, vpp);
+    double volumeVar = pow(fabs(volume / volumePrime), 1.0 / 3.0);
+    v3 center = mul(add(add(add(add(add(vp[0], vp[1]), vp[2]), vp[3]), vp[4]), vp[5]), 1.0 / 6.0);
+    for (int k = 0; k < 6; ++k) vpp[k] = add(center, mul(sub(vpp[k], center), volumeVar));
+    for (int k = 0; k < 6; ++k)
+        if (is_constrained(m, vi[k])) vpp[k] = snap(m, vi[k], vpp[k]);
+    double quality = quality_vp(m, OM_PRI, vp);
+    double qualityPrime = quality_vp(m, OM_PRI, vpp);
+    double weight = qualityPrime / (1.0 + quality);
+    for (int k = 0; k < 6; ++k)
+    {
+        out[k].p = vpp[k];
+        out[k].w = weight;
+    }
+}
+
+/* GetmeSmoother::smoothHexs (GetmeSmoother.cpp:235-374) */
+static void getme_hex(const om_mesh* m, int64_t eId, double lambda, corner_out* out)
+{
+    const uint32_t* vi = m->hexs + 8 * eId;
+    v3 vp[8], vpp[8];
+    for (int k = 0; k < 8; ++k) vp[k] = P(m, vi[k]);
+    v3 aux[6] = {dvs(add(add(add(vp[0], vp[1]), vp[2]), vp[3]), 4.0),
+                 dvs(add(add(add(vp[0], vp[4]), vp[5]), vp[1]), 4.0),
+                 dvs(add(add(add(vp[1], vp[5]), vp[6]), vp[2]), 4.0),
+                 dvs(add(add(add(vp[2], vp[6]), vp[7]), vp[3]), 4.0),
+                 dvs(add(add(add(vp[0], vp[3]), vp[7]), vp[4]), 4.0),
+                 dvs(add(add(add(vp[4], vp[7]), vp[6]), vp[5]), 4.0)};
+    v3 n[8] = {cross(sub(aux[1], aux[0]), sub(aux[4], aux[0])), cross(sub(aux[2], aux[0]), sub(aux[1], aux[0])),
+               cross(sub(aux[3], aux[0]), sub(aux[2], aux[0])), cross(sub(aux[4], aux[0]), sub(aux[3], aux[0])),
+               cross(sub(aux[4], aux[5]), sub(aux[1], aux[5])), cross(sub(aux[1], aux[5]), sub(aux[2], aux[5])),
+               cross(sub(aux[2], aux[5]), sub(aux[3], aux[5])), cross(sub(aux[3], aux[5]), sub(aux[4], aux[5]))};
+    v3 bases[8] = {dvs(add(add(aux[0], aux[1]), aux[4]), 3.0), dvs(add(add(aux[0], aux[2]), aux[1]), 3.0),
+                   dvs(add(add(aux[0], aux[3]), aux[2]), 3.0), dvs(add(add(aux[0], aux[4]), aux[3]), 3.0),
+                   dvs(add(add(aux[5], aux[4]), aux[1]), 3.0), dvs(add(add(aux[5], aux[1]), aux[2]), 3.0),
+                   dvs(add(add(aux[5], aux[2]), aux[3]), 3.0), dvs(add(add(aux[5], aux[3]), aux[4]), 3.0)};
+    for (int k = 0; k < 8; ++k) vpp[k] = add(bases[k], mul(n[k], lambda / sqrt(length(n[k]))));
+    double volume = hex_volume(m, vp);
+    double volumePrime = hex_volume(m, vpp);
+    double volumeVar = pow(fabs(volume / volumePrime), 1.0 / 3.0);
+    v3 center = mul(add(add(add(add(add(add(add(vp[0], vp[1]), vp[2]), vp[3]), vp[4]), vp[5]), vp[6]), vp[7]),
+                    1.0 / 8.0);
+    for (int k = 0; k < 8; ++k) vpp[k] = add(center, mul(sub(vpp[k], center), volumeVar));
+    for (int k = 0; k < 8; ++k)
+        if (is_constrained(m, vi[k])) vpp[k] = snap(m, vi[k], vpp[k]);
+    double quality = quality_vp(m, OM_HEX, vp);
+    double qualityPrime = quality_vp(m, OM_HEX, vpp);
+    double weight = qualityPrime / (1.0 + quality);
+    for (int k = 0; k < 8; ++k)
+    {
+        out[k].p = vpp[k];
+        out[k].w = weight;
+    }
+}
+
+/* AbstractElementWiseSmoother::updateVertexPositions
+ * (Smoothers/ElementWise/AbstractElementWiseSmoother.cpp:406-444), with the
+ * vertex accumulator (VertexAccum.cpp: NotThreadSafeVertexAccum) summed in
+ * element order, which is the vertex's neighbour-element order */
+static void getme_update_vertex(om_mesh* m, uint32_t vId, const int64_t* corner_base,
+                                const corner_out* corners, int64_t* evals)
+{
+    v3 posAccum = V(0, 0, 0);
+    double weightAccum = 0.0;
+    for (int64_t n = m->ne_base[vId]; n < m->ne_base[vId + 1]; ++n)
+    {
+        const neig_elem* ne = &m->ne[n];
+        const corner_out* c = &corners[corner_base[ne->type] + (int64_t)ne->id *
+                                       (ne->type == OM_TET ? 4 : ne->type == OM_PRI ? 6 : 8) + ne->vid];
+        posAccum = add(posAccum, mul(c->p, c->w));
+        weightAccum += c->w;
+    }
+    v3 pos = P(m, vId);
+    if (weightAccum != 0.0)
+    {
+        v3 posPrim = dvs(posAccum, weightAccum);
+        if (is_constrained(m, vId)) posPrim = snap(m, vId, posPrim);
+        ++*evals;
+        double patchQuality = patch_quality(m, vId);
+        setP(m, vId, posPrim);
+        ++*evals;
+        double patchQualityPrime = patch_quality(m, vId);
+        if (patchQualityPrime < patchQuality) setP(m, vId, pos);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* pass driver: colour-major groups, strided worker slices and a barrier per */
+/* colour, as AbstractVertexWiseSmoother::smoothMeshThread                    */
+/* (Smoothers/VertexWise/AbstractVertexWiseSmoother.cpp:84-152) and          */
+/* NodeGroups::dispatchCpuWorkgroups (DataStructures/NodeGroups.cpp:621-659)  */
+/* ------------------------------------------------------------------------ */
+
+typedef struct
+{
+    om_mesh* m;
+    int32_t smoother;
+    smooth_params sp;
+    int64_t ngroups;
+    const int64_t* group_base;
+    const uint32_t* members;
+    int nthreads;
+    pthread_barrier_t* barrier;
+    /* GETMe */
+    const int64_t* corner_base;
+    corner_out* corners;
+    int64_t evals[64];
+} pass_ctx;
+
+typedef struct
+{
+    pass_ctx* ctx;
+    int t;
+} pass_arg;
+
+static void* pass_worker(void* arg)
+{
+    pass_arg* a = (pass_arg*)arg;
+    pass_ctx* c = a->ctx;
+    int t = a->t, T = c->nthreads;
+    int64_t evals = 0;
+
+    if (c->smoother == OM_SMOOTH_GETME)
+    {
+        /* element pass: every element reads the positions at pass start
+         * (GetmeSmoother::smoothTets/Pris/Hexs run before any update) */
+        om_mesh* m = c->m;
+        double lambda = c->sp.p[0];
+        for (int64_t i = t; i < m->nt; i += T) getme_tet(m, i, lambda, c->corners + c->corner_base[OM_TET] + 4 * i);
+        for (int64_t i = t; i < m->np; i += T) getme_pri(m, i, lambda, c->corners + c->corner_base[OM_PRI] + 6 * i);
+        for (int64_t i = t; i < m->nh; i += T) getme_hex(m, i, lambda, c->corners + c->corner_base[OM_HEX] + 8 * i);
+        if (T > 1) pthread_barrier_wait(c->barrier);
+    }
+
+    for (int64_t g = 0; g < c->ngroups; ++g)
+    {
+        int64_t b = c->group_base[g], e = c->group_base[g + 1];
+        for (int64_t i = b + t; i < e; i += T)
+        {
+            uint32_t v = c->members[i];
+            switch (c->smoother)
+            {
+            case OM_SMOOTH_NELDER_MEAD: nm_vertex(c->m, v, &c->sp, &evals); break;
+            case OM_SMOOTH_GRADIENT_DESCENT: gd_vertex(c->m, v, &c->sp, &evals); break;
+            case OM_SMOOTH_SPAWN_SEARCH: spawn_vertex(c->m, v, &c->sp, &evals); break;
+            case OM_SMOOTH_GETME: getme_update_vertex(c->m, v, c->corner_base, c->corners, &evals); break;
+            default: break;
+            }
+        }
+        if (T > 1) pthread_barrier_wait(c->barrier);
+    }
+    c->evals[t] = evals;
+    return NULL;
+}
+
+void om_smooth_pass(om_mesh* m, int32_t smoother, const double* params, int64_t ngroups,
+                    const int64_t* group_base, const uint32_t* members, int32_t nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 64) nthreads = 64;
+    pass_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.m = m;
+    c.smoother = smoother;
+    memcpy(c.sp.p, params, sizeof(c.sp.p));
+    c.ngroups = ngroups;
+    c.group_base = group_base;
+    c.members = members;
+    c.nthreads = nthreads;
+    int64_t corner_base[4] = {0, 0, 4 * m->nt, 4 * m->nt + 6 * m->np};
+    if (smoother == OM_SMOOTH_GETME)
+    {
+        c.corner_base = corner_base;
+        c.corners = (corner_out*)malloc(sizeof(corner_out) * (size_t)(4 * m->nt + 6 * m->np + 8 * m->nh + 1));
+    }
+    pthread_barrier_t barrier;
+    if (nthreads > 1) pthread_barrier_init(&barrier, NULL, (unsigned)nthreads);
+    c.barrier = &barrier;
+    pass_arg args[64];
+    pthread_t th[64];
+    for (int t = 0; t < nthreads; ++t)
+    {
+        args[t].ctx = &c;
+        args[t].t = t;
+        if (nthreads == 1) pass_worker(&args[t]);
+        else pthread_create(&th[t], NULL, pass_worker, &args[t]);
+    }
+    if (nthreads > 1)
+    {
+        for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+        pthread_barrier_destroy(&barrier);
+    }
+    for (int t = 0; t < nthreads; ++t) m->patch_evals += c.evals[t];
+    free(c.corners);
+}

