@@ -27,13 +27,19 @@ def device_for(raw, groups, crew):
     return dev
 
 
+TET_EDGES = ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3))
+PRI_EDGES = ((0, 1), (0, 2), (1, 2), (0, 3), (1, 4), (2, 5), (3, 4), (3, 5), (4, 5))
+HEX_EDGES = ((0, 1), (0, 3), (1, 2), (2, 3), (0, 4), (1, 5), (2, 6), (3, 7), (4, 5), (4, 7), (5, 6), (6, 7))
+
+
 def edge_lengths(raw):
     """Mean edge length around each vertex (the local element size)."""
-    edges = set()
-    for t in raw.tets:
-        for a, b in ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)):
-            edges.add((min(t[a], t[b]), max(t[a], t[b])))
-    e = np.array(sorted(edges), dtype=np.int64)
+    pairs = []
+    for E, edges in ((raw.tets, TET_EDGES), (raw.pris, PRI_EDGES), (raw.hexs, HEX_EDGES)):
+        if E.shape[0]:
+            for a, b in edges:
+                pairs.append(np.stack([E[:, a], E[:, b]], axis=1))
+    e = np.unique(np.sort(np.concatenate(pairs).astype(np.int64), axis=1), axis=0)
     L = np.linalg.norm(raw.pos[e[:, 0]] - raw.pos[e[:, 1]], axis=1)
     s = np.zeros(raw.nv)
     c = np.zeros(raw.nv)
