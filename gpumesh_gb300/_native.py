@@ -83,6 +83,8 @@ def lib():
         "gm_mesh_save_positions": [vp],
         "gm_mesh_restore_positions": [vp],
         "gm_probe_fp32_tflops": [ctypes.POINTER(ctypes.c_double)],
+        "gm_evaluate_noalloc": [u32, vp, u32, vp, u32, vp, u32, vp, i32, i32, i32, ctypes.c_double,
+                                ctypes.c_double, vp, vp],
     }
     for name, args in sigs.items():
         f = getattr(L, name)

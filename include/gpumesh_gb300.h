@@ -212,6 +212,24 @@ gm_status gm_getme_update_group(gm_mesh* mesh, const double* params, uint32_t me
  * element evaluations, vertices relocated in FP64].  Synchronous. */
 gm_status gm_mesh_counters(gm_mesh* mesh, uint64_t* out5, int32_t reset);
 
+/* No counterpart in the reference.  Quality evaluation that allocates
+ * nothing, for callers that cannot call cudaMalloc (a host framework that
+ * owns every device allocation, a fully committed memory budget, a loop
+ * that must not allocate once running).  Every pointer is a device pointer:
+ * pos = nv float4 (x, y, z, unused; 16-byte aligned), tets / hexs = 4 / 8
+ * uint32 per element (16-byte aligned), pris = 6 uint32 per element (8-byte
+ * aligned); *out receives the gm_quality on the device, asynchronously on
+ * `stream`.  The only scratch is a 112 KiB array inside this library that
+ * every GPU which loads the library holds until exit; meshes above
+ * 16,777,216 elements are rejected with GM_ERR_UNSUPPORTED.  The first call
+ * on a device looks up that array's device address, so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+gm_status gm_evaluate_noalloc(uint32_t nv, const void* pos, uint32_t nt, const uint32_t* tets, uint32_t np,
+                              const uint32_t* pris, uint32_t nh, const uint32_t* hexs, int32_t sampler,
+                              int32_t measurer, int32_t evaluator, double scaling, double aspect_ratio,
+                              gm_quality* out, void* stream);
+
 /* Device peak probe: a dependent-FFMA loop over every SM; *tflops receives
  * the achieved FP32 rate (2 flops per FFMA).  The roofline denominator of
  * the relocation kernels. */
