@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-eval-roofline", action="store_true")
+    ap.add_argument("--only", choices=["eval", "relocate"], default=None,
+                    help="profiling driver: a few launches of one kernel family, no JSON line")
     return ap.parse_args()
 
 
@@ -243,9 +245,13 @@ def cpu_sample_run(w, raw, groups, seconds, threads):
                 orc.smooth_pass(smoother, b, m, params=params, nthreads=threads)
         return time.perf_counter() - t0, int(m.size) * w.passes()
 
-    t, n = timed(0.002)
-    frac = min(1.0, 0.002 * seconds / max(t, 1e-3))
+    frac = 0.002
     t, n = timed(frac)
+    for _ in range(2):  # per-pass overheads make the time sublinear in the sample: refine twice
+        frac = min(1.0, frac * (0.5 * seconds) / max(t, 1e-3))
+        t, n = timed(frac)
+        if t > 0.3 * seconds:
+            break
     return n / t, frac, n, t
 
 
@@ -405,8 +411,37 @@ def bench_gpu(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def profile_driver(args):
+    """A few launches of one kernel family, for ncu: `eval` = the evaluation
+    kernel on the 128^3 hex mesh (4 launches); `relocate` = one pass of each
+    smoother of the workload's schedule."""
+    import torch
+
+    from gpumesh_gb300 import mesh as M
+    from gpumesh_gb300 import meshgen
+
+    if args.only == "eval":
+        raw = meshgen.box_mesh(128, "hex", 0.15, 2, gaussian=True)
+        dev = M.DeviceMesh(raw, None)
+        dev.set_crew("uniform", "metric_free", "mean_ratio")
+        for _ in range(4):
+            h = dev.evaluate()
+        print("eval", h.minimumQuality(), h.harmonicMean())
+    else:
+        w, raw, groups = prepare(args.workload)
+        dev = M.DeviceMesh(raw, groups)
+        dev.set_crew(**w.crew(raw))
+        for smoother, passes, params in w.schedule:
+            dev.smooth_pass(smoother, params)
+        print("relocate", dev.evaluate().as_dict()["mean"])
+    torch.cuda.synchronize()
+
+
 def main():
     args = parse()
+    if args.only:
+        profile_driver(args)
+        return
     rank, world, local = dist_init(args.gpus)
     if args.impl == "reference":
         bench_reference(args, rank, world)

@@ -273,34 +273,31 @@ __device__ __forceinline__ void pri_frame(V3<R> a, V3<R> b, V3<R> e, V3<R>& c0, 
     c2 = e;
 }
 
+// Running combination of corner qualities (MeanRatioEvaluator.cpp:91-110,
+// 140-166): the harmonic mean when every corner is valid, else the minimum
+// corner quality -- which is then the minimum over the non-positive corners,
+// so the valid corners never need their q, only their 1/q.
 template <class R>
-__device__ __forceinline__ EQ<R> combine(const R* rq, const R* q, const bool* pos, int n)
+struct CornerAcc
 {
+    R rsum = R(0);
+    R minbad = R(3.0e38);
     bool all = true;
-    for (int i = 0; i < n; ++i) all = all && pos[i];
-    EQ<R> r;
-    if (all)
+    __device__ __forceinline__ void add(R rq, R q, bool pos)
     {
-        R s = 0;
-        for (int i = 0; i < n; ++i) s += rq[i];
-        r.v = s / R(n);
-        r.pos = true;
-    }
-    else
-    {
-        // min over corners; valid corners need their q = 1/rq
-        R mn = pos[0] ? R(1) / rq[0] : q[0];
-        for (int i = 1; i < n; ++i)
+        if (pos) rsum += rq;
+        else
         {
-            R qi = pos[i] ? R(1) / rq[i] : q[i];
-            mn = qi < mn ? qi : mn;
+            all = false;
+            minbad = q < minbad ? q : minbad;
         }
-        r.v = mn;
-        r.pos = mn > R(0);
-        if (r.pos) r.v = R(1) / mn;
     }
-    return r;
-}
+    __device__ __forceinline__ EQ<R> result(int n) const
+    {
+        if (all) return EQ<R>{rsum / R(n), true};
+        return EQ<R>{minbad, false};
+    }
+};
 
 template <int VAR, class R>
 __device__ __forceinline__ EQ<R> mr_tet(const Crew& c, const V3<R>* p)
@@ -319,16 +316,17 @@ __device__ __forceinline__ EQ<R> mr_pri(const Crew& c, const V3<R>* p)
     V3<R> e03 = segment<VAR, R>(c, p[0], p[3]), e14 = segment<VAR, R>(c, p[1], p[4]), e25 = segment<VAR, R>(c, p[2], p[5]);
     V3<R> e01 = segment<VAR, R>(c, p[0], p[1]), e12 = segment<VAR, R>(c, p[1], p[2]), e20 = segment<VAR, R>(c, p[2], p[0]);
     V3<R> e34 = segment<VAR, R>(c, p[3], p[4]), e45 = segment<VAR, R>(c, p[4], p[5]), e53 = segment<VAR, R>(c, p[5], p[3]);
-    R rq[6], q[6];
-    bool pos[6];
+    CornerAcc<R> acc;
     V3<R> a, b, d;
-    pri_frame(-e01, e20, e03, a, b, d); mr_corner(a, b, d, rq[0], q[0], pos[0]);
-    pri_frame(-e12, e01, e14, a, b, d); mr_corner(a, b, d, rq[1], q[1], pos[1]);
-    pri_frame(-e20, e12, e25, a, b, d); mr_corner(a, b, d, rq[2], q[2], pos[2]);
-    pri_frame(-e34, e53, e03, a, b, d); mr_corner(a, b, d, rq[3], q[3], pos[3]);
-    pri_frame(-e45, e34, e14, a, b, d); mr_corner(a, b, d, rq[4], q[4], pos[4]);
-    pri_frame(-e53, e45, e25, a, b, d); mr_corner(a, b, d, rq[5], q[5], pos[5]);
-    return combine(rq, q, pos, 6);
+    R rq = 0, q = 0;
+    bool pos;
+    pri_frame(-e01, e20, e03, a, b, d); mr_corner(a, b, d, rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e12, e01, e14, a, b, d); mr_corner(a, b, d, rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e20, e12, e25, a, b, d); mr_corner(a, b, d, rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e34, e53, e03, a, b, d); mr_corner(a, b, d, rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e45, e34, e14, a, b, d); mr_corner(a, b, d, rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e53, e45, e25, a, b, d); mr_corner(a, b, d, rq, q, pos); acc.add(rq, q, pos);
+    return acc.result(6);
 }
 
 template <int VAR, class R>
@@ -338,17 +336,18 @@ __device__ __forceinline__ EQ<R> mr_hex(const Crew& c, const V3<R>* p)
     V3<R> e12 = segment<VAR, R>(c, p[1], p[2]), e15 = segment<VAR, R>(c, p[1], p[5]), e23 = segment<VAR, R>(c, p[2], p[3]);
     V3<R> e26 = segment<VAR, R>(c, p[2], p[6]), e37 = segment<VAR, R>(c, p[3], p[7]), e45 = segment<VAR, R>(c, p[4], p[5]);
     V3<R> e47 = segment<VAR, R>(c, p[4], p[7]), e56 = segment<VAR, R>(c, p[5], p[6]), e67 = segment<VAR, R>(c, p[6], p[7]);
-    R rq[8], q[8];
-    bool pos[8];
-    mr_corner(e01, e04, -e03, rq[0], q[0], pos[0]);
-    mr_corner(e01, e12, e15, rq[1], q[1], pos[1]);
-    mr_corner(e12, e26, -e23, rq[2], q[2], pos[2]);
-    mr_corner(e03, e23, e37, rq[3], q[3], pos[3]);
-    mr_corner(e04, e45, e47, rq[4], q[4], pos[4]);
-    mr_corner(e15, -e56, e45, rq[5], q[5], pos[5]);
-    mr_corner(e26, e56, e67, rq[6], q[6], pos[6]);
-    mr_corner(e37, e67, -e47, rq[7], q[7], pos[7]);
-    return combine(rq, q, pos, 8);
+    CornerAcc<R> acc;
+    R rq = 0, q = 0;
+    bool pos;
+    mr_corner(e01, e04, -e03, rq, q, pos); acc.add(rq, q, pos);
+    mr_corner(e01, e12, e15, rq, q, pos); acc.add(rq, q, pos);
+    mr_corner(e12, e26, -e23, rq, q, pos); acc.add(rq, q, pos);
+    mr_corner(e03, e23, e37, rq, q, pos); acc.add(rq, q, pos);
+    mr_corner(e04, e45, e47, rq, q, pos); acc.add(rq, q, pos);
+    mr_corner(e15, -e56, e45, rq, q, pos); acc.add(rq, q, pos);
+    mr_corner(e26, e56, e67, rq, q, pos); acc.add(rq, q, pos);
+    mr_corner(e37, e67, -e47, rq, q, pos); acc.add(rq, q, pos);
+    return acc.result(8);
 }
 
 // MetricConformityEvaluator::specifiedMetric: 5-point Keast rule
@@ -391,23 +390,42 @@ __device__ __forceinline__ Sym3<R> sym_inverse(const Sym3<R>& m)
 }
 
 // MetricConformityEvaluator::metricConformity: with F the corner matrix,
-// Mk^-1 = F F^T and Mk = (F F^T)^-1; tNc = Mk^-1 Ms + Ms^-1 Mk - 2I and
-// q = sign(det F) / sqrt(1 + |tNc|_F).  Returns 1/q for valid corners.
+// Mk^-1 = F F^T (no inversion) and Mk = F^-T F^-1 = G^T G with G = F^-1, so
+// only F (not F F^T, whose condition number is squared) is inverted;
+// tNc = Mk^-1 Ms + Ms^-1 Mk - 2I and q = sign(det F) / sqrt(1 + |tNc|_F).
+// Returns 1/q for valid corners.
 template <class R>
 __device__ __forceinline__ void mc_corner(V3<R> c0, V3<R> c1, V3<R> c2, const Sym3<R>& Ms, R& rq, R& q, bool& pos)
 {
-    // A = F F^T, F has columns c0, c1, c2
-    Sym3<R> A;
+    // F has columns c0, c1, c2: F[r][c] = c_c.r
+    const R F[3][3] = {{c0.x, c1.x, c2.x}, {c0.y, c1.y, c2.y}, {c0.z, c1.z, c2.z}};
+    const R det = det3(c0, c1, c2);
+    // G = F^-1 = adj(F) / det
+    const R id = R(1) / det;
+    R G[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+        {
+            const int r0 = (j + 1) % 3, r1 = (j + 2) % 3, k0 = (i + 1) % 3, k1 = (i + 2) % 3;
+            G[i][j] = (F[r0][k0] * F[r1][k1] - F[r0][k1] * F[r1][k0]) * id;
+        }
+    // A = F F^T (= Mk^-1), Mk = G^T G
+    Sym3<R> A, Mk;
     A.xx = c0.x * c0.x + c1.x * c1.x + c2.x * c2.x;
     A.yy = c0.y * c0.y + c1.y * c1.y + c2.y * c2.y;
     A.zz = c0.z * c0.z + c1.z * c1.z + c2.z * c2.z;
     A.xy = c0.x * c0.y + c1.x * c1.y + c2.x * c2.y;
     A.xz = c0.x * c0.z + c1.x * c1.z + c2.x * c2.z;
     A.yz = c0.y * c0.z + c1.y * c1.z + c2.y * c2.z;
-    R det = det3(c0, c1, c2);
-    Sym3<R> Mk = sym_inverse(A);
+    Mk.xx = G[0][0] * G[0][0] + G[1][0] * G[1][0] + G[2][0] * G[2][0];
+    Mk.yy = G[0][1] * G[0][1] + G[1][1] * G[1][1] + G[2][1] * G[2][1];
+    Mk.zz = G[0][2] * G[0][2] + G[1][2] * G[1][2] + G[2][2] * G[2][2];
+    Mk.xy = G[0][0] * G[0][1] + G[1][0] * G[1][1] + G[2][0] * G[2][1];
+    Mk.xz = G[0][0] * G[0][2] + G[1][0] * G[1][2] + G[2][0] * G[2][2];
+    Mk.yz = G[0][1] * G[0][2] + G[1][1] * G[1][2] + G[2][1] * G[2][2];
     Sym3<R> Msi = sym_inverse(Ms);
-    // P = A Ms ; Qm = Msi Mk ; tNc = P + Qm - 2I
     R t[9];
 #define GM_SYM(m, i, j) ((i) == (j) ? ((i) == 0 ? m.xx : (i) == 1 ? m.yy : m.zz) \
     : (((i) + (j)) == 1 ? m.xy : ((i) + (j)) == 2 ? m.xz : m.yz))
@@ -455,16 +473,17 @@ __device__ __noinline__ EQ<R> mc_pri(const Crew& c, const V3<R>* p)
     V3<R> e03 = p[3] - p[0], e14 = p[4] - p[1], e25 = p[5] - p[2];
     V3<R> e01 = p[1] - p[0], e12 = p[2] - p[1], e20 = p[0] - p[2];
     V3<R> e34 = p[4] - p[3], e45 = p[5] - p[4], e53 = p[3] - p[5];
-    R rq[6], q[6];
-    bool pos[6];
+    CornerAcc<R> acc;
     V3<R> a, b, d;
-    pri_frame(-e01, e20, e03, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[3]), rq[0], q[0], pos[0]);
-    pri_frame(-e12, e01, e14, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[4]), rq[1], q[1], pos[1]);
-    pri_frame(-e20, e12, e25, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[5]), rq[2], q[2], pos[2]);
-    pri_frame(-e34, e53, e03, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[3], p[4], p[5]), rq[3], q[3], pos[3]);
-    pri_frame(-e45, e34, e14, a, b, d); mc_corner(a, b, d, specified_metric(c, p[1], p[3], p[4], p[5]), rq[4], q[4], pos[4]);
-    pri_frame(-e53, e45, e25, a, b, d); mc_corner(a, b, d, specified_metric(c, p[2], p[3], p[4], p[5]), rq[5], q[5], pos[5]);
-    return combine(rq, q, pos, 6);
+    R rq = 0, q = 0;
+    bool pos;
+    pri_frame(-e01, e20, e03, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[3]), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e12, e01, e14, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[4]), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e20, e12, e25, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[5]), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e34, e53, e03, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[3], p[4], p[5]), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e45, e34, e14, a, b, d); mc_corner(a, b, d, specified_metric(c, p[1], p[3], p[4], p[5]), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e53, e45, e25, a, b, d); mc_corner(a, b, d, specified_metric(c, p[2], p[3], p[4], p[5]), rq, q, pos); acc.add(rq, q, pos);
+    return acc.result(6);
 }
 
 template <class R>
@@ -473,17 +492,18 @@ __device__ __noinline__ EQ<R> mc_hex(const Crew& c, const V3<R>* p)
     V3<R> e01 = p[1] - p[0], e03 = p[3] - p[0], e04 = p[4] - p[0], e12 = p[2] - p[1];
     V3<R> e15 = p[5] - p[1], e23 = p[3] - p[2], e26 = p[6] - p[2], e37 = p[7] - p[3];
     V3<R> e45 = p[5] - p[4], e47 = p[7] - p[4], e56 = p[6] - p[5], e67 = p[7] - p[6];
-    R rq[8], q[8];
-    bool pos[8];
-    mc_corner(e01, e04, -e03, specified_metric(c, p[0], p[1], p[3], p[4]), rq[0], q[0], pos[0]);
-    mc_corner(e01, e12, e15, specified_metric(c, p[0], p[1], p[2], p[5]), rq[1], q[1], pos[1]);
-    mc_corner(e12, e26, -e23, specified_metric(c, p[1], p[2], p[3], p[6]), rq[2], q[2], pos[2]);
-    mc_corner(e03, e23, e37, specified_metric(c, p[0], p[2], p[3], p[7]), rq[3], q[3], pos[3]);
-    mc_corner(e04, e45, e47, specified_metric(c, p[0], p[4], p[5], p[7]), rq[4], q[4], pos[4]);
-    mc_corner(e15, -e56, e45, specified_metric(c, p[1], p[4], p[5], p[6]), rq[5], q[5], pos[5]);
-    mc_corner(e26, e56, e67, specified_metric(c, p[2], p[5], p[6], p[7]), rq[6], q[6], pos[6]);
-    mc_corner(e37, e67, -e47, specified_metric(c, p[3], p[4], p[6], p[7]), rq[7], q[7], pos[7]);
-    return combine(rq, q, pos, 8);
+    CornerAcc<R> acc;
+    R rq = 0, q = 0;
+    bool pos;
+    mc_corner(e01, e04, -e03, specified_metric(c, p[0], p[1], p[3], p[4]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e01, e12, e15, specified_metric(c, p[0], p[1], p[2], p[5]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e12, e26, -e23, specified_metric(c, p[1], p[2], p[3], p[6]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e03, e23, e37, specified_metric(c, p[0], p[2], p[3], p[7]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e04, e45, e47, specified_metric(c, p[0], p[4], p[5], p[7]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e15, -e56, e45, specified_metric(c, p[1], p[4], p[5], p[6]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e26, e56, e67, specified_metric(c, p[2], p[5], p[6], p[7]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e37, e67, -e47, specified_metric(c, p[3], p[4], p[6], p[7]), rq, q, pos); acc.add(rq, q, pos);
+    return acc.result(8);
 }
 
 // quality of an element of the given type; MAXK = 4 means tets only
