@@ -42,9 +42,9 @@ UNIT = "relocations/s"
 # transcendental counts 1, an FMA counts 2), counted from the measures in
 # gpumesh_gb300/csrc/gm_device.cuh; see DESIGN.md "Relocation roofline".
 FLOPS_PER_ELEM_EVAL = {
-    ("mean_ratio", "tet"): 80,
-    ("mean_ratio", "hex"): 8 * 45 + 36 + 36,
-    ("metric_conformity", "tet"): 330,
+    ("mean_ratio", "tet"): 78,
+    ("mean_ratio", "hex"): 369,
+    ("metric_conformity", "tet"): 272,  # diagonal (uniform / sine-graded) metric
 }
 
 

@@ -56,6 +56,7 @@ cudaError_t launch_accept(const RelocLaunch& L)
     {
     case kVarMRFree: return L.maxk == 4 ? launch_accept_t<kVarMRFree, 4>(L) : launch_accept_t<kVarMRFree, 8>(L);
     case kVarMRWise: return launch_accept_t<kVarMRWise, 8>(L);
+    case kVarMCDiag: return L.maxk == 4 ? launch_accept_t<kVarMCDiag, 4>(L) : launch_accept_t<kVarMCDiag, 8>(L);
     default: return L.maxk == 4 ? launch_accept_t<kVarMC, 4>(L) : launch_accept_t<kVarMC, 8>(L);
     }
 }

@@ -158,7 +158,8 @@ struct gm_mesh
     // evaluator x measurer variant of the vertex kernels
     int variant() const
     {
-        if (crew.evaluator == GM_EVALUATOR_METRIC_CONFORMITY) return kVarMC;
+        if (crew.evaluator == GM_EVALUATOR_METRIC_CONFORMITY)
+            return crew.sampler == GM_SAMPLER_ANALYTIC ? kVarMC : kVarMCDiag;
         return crew.measurer == GM_MEASURER_METRIC_WISE ? kVarMRWise : kVarMRFree;
     }
     // variant of the GETMe element pass, whose volumes also follow the measurer
@@ -166,9 +167,11 @@ struct gm_mesh
     {
         if (crew.evaluator == GM_EVALUATOR_METRIC_CONFORMITY)
             return crew.measurer == GM_MEASURER_METRIC_WISE ? kVarMCWise : kVarMC;
-        return variant();
+        return crew.measurer == GM_MEASURER_METRIC_WISE ? kVarMRWise : kVarMRFree;
     }
     int maxk() const { return (np || nh) ? 8 : 4; }
+    // element set of the evaluation kernel: 4 tets only, 8 mixed, 9 hexes only
+    int elem_set() const { return (nt == 0 && np == 0 && nh) ? 9 : maxk(); }
 };
 
 namespace {
@@ -721,7 +724,7 @@ gm_status gm_evaluate_async(gm_mesh* m, uint32_t slot)
         uint32_t total = m->nt + m->np + m->nh;
         int nb = evaluate_blocks(total, m->sm_count);
         m->parts.reserve(nb);
-        GM_CUDA(launch_evaluate(m->variant(), m->maxk(), m->view(), m->crew, m->parts.p, nb, m->quality.p + slot,
+        GM_CUDA(launch_evaluate(m->variant(), m->elem_set(), m->view(), m->crew, m->parts.p, nb, m->quality.p + slot,
                                 m->stream));
     });
 }

@@ -218,11 +218,14 @@ __device__ __noinline__ R metric_wise_distance(const Crew& c, V3<R> a, V3<R> b)
 }
 
 // crew variants the kernels are specialised on: evaluator x measurer
-enum : int { kVarMRFree = 0, kVarMRWise = 1, kVarMC = 2, kVarMCWise = 3 };
+// kVarMCDiag: metric conformity with a diagonal metric (the uniform and the
+// sine-graded samplers), whose 3x3 products reduce to their diagonals
+enum : int { kVarMRFree = 0, kVarMRWise = 1, kVarMC = 2, kVarMCWise = 3, kVarMCDiag = 4 };
 template <int VAR> struct VarTraits
 {
     static constexpr bool mean_ratio = VAR == kVarMRFree || VAR == kVarMRWise;
     static constexpr bool metric_wise = VAR == kVarMRWise || VAR == kVarMCWise;
+    static constexpr bool diag_metric = VAR == kVarMCDiag;
 };
 
 template <int VAR, class R>
@@ -455,6 +458,126 @@ __device__ __forceinline__ void mc_corner(V3<R> c0, V3<R> c1, V3<R> c2, const Sy
     else q = s / r;
 }
 
+// ---- diagonal metrics (uniform, sine-graded): M = diag(d.x, d.y, d.z) ----
+template <class R>
+__device__ __forceinline__ V3<R> metric_diag_at(const Crew& c, V3<R> p)
+{
+    R s2 = (R)c.scaling2;
+    if (c.sampler == kSamplerSine)
+    {
+        R s = sinpi_(R(4) * p.x);
+        return {s2 * (R(1) + R(9) * s * s), s2, s2};
+    }
+    return {s2, s2, s2};
+}
+
+template <class R>
+__device__ __forceinline__ V3<R> specified_metric_diag(const Crew& c, V3<R> v0, V3<R> v1, V3<R> v2, V3<R> v3)
+{
+    const R H = R(0.5), Q = R((1.0 - 0.5) / 3.0);
+    V3<R> m0 = metric_diag_at(c, (v0 + v1 + v2 + v3) * R(0.25));
+    V3<R> m1 = metric_diag_at(c, v0 * H + v1 * Q + v2 * Q + v3 * Q);
+    V3<R> m2 = metric_diag_at(c, v0 * Q + v1 * H + v2 * Q + v3 * Q);
+    V3<R> m3 = metric_diag_at(c, v0 * Q + v1 * Q + v2 * H + v3 * Q);
+    V3<R> m4 = metric_diag_at(c, v0 * Q + v1 * Q + v2 * Q + v3 * H);
+    return m0 * R(-0.8) + (m1 + m2 + m3 + m4) * R(0.45);
+}
+
+// mc_corner with Ms = diag(m): tNc_ij = A_ij m_j + Mk_ij / m_i - 2 delta_ij
+template <class R>
+__device__ __forceinline__ void mc_corner_diag(V3<R> c0, V3<R> c1, V3<R> c2, V3<R> m, R& rq, R& q, bool& pos)
+{
+    const R F[3][3] = {{c0.x, c1.x, c2.x}, {c0.y, c1.y, c2.y}, {c0.z, c1.z, c2.z}};
+    const R det = det3(c0, c1, c2);
+    const R id = R(1) / det;
+    R G[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+        {
+            const int r0 = (j + 1) % 3, r1 = (j + 2) % 3, k0 = (i + 1) % 3, k1 = (i + 2) % 3;
+            G[i][j] = (F[r0][k0] * F[r1][k1] - F[r0][k1] * F[r1][k0]) * id;
+        }
+    const R Axx = c0.x * c0.x + c1.x * c1.x + c2.x * c2.x, Ayy = c0.y * c0.y + c1.y * c1.y + c2.y * c2.y;
+    const R Azz = c0.z * c0.z + c1.z * c1.z + c2.z * c2.z, Axy = c0.x * c0.y + c1.x * c1.y + c2.x * c2.y;
+    const R Axz = c0.x * c0.z + c1.x * c1.z + c2.x * c2.z, Ayz = c0.y * c0.z + c1.y * c1.z + c2.y * c2.z;
+    const R Kxx = G[0][0] * G[0][0] + G[1][0] * G[1][0] + G[2][0] * G[2][0];
+    const R Kyy = G[0][1] * G[0][1] + G[1][1] * G[1][1] + G[2][1] * G[2][1];
+    const R Kzz = G[0][2] * G[0][2] + G[1][2] * G[1][2] + G[2][2] * G[2][2];
+    const R Kxy = G[0][0] * G[0][1] + G[1][0] * G[1][1] + G[2][0] * G[2][1];
+    const R Kxz = G[0][0] * G[0][2] + G[1][0] * G[1][2] + G[2][0] * G[2][2];
+    const R Kyz = G[0][1] * G[0][2] + G[1][1] * G[1][2] + G[2][1] * G[2][2];
+    const R ix = R(1) / m.x, iy = R(1) / m.y, iz = R(1) / m.z;
+    const R txx = Axx * m.x + Kxx * ix - R(2), tyy = Ayy * m.y + Kyy * iy - R(2), tzz = Azz * m.z + Kzz * iz - R(2);
+    const R txy = Axy * m.y + Kxy * ix, tyx = Axy * m.x + Kxy * iy;
+    const R txz = Axz * m.z + Kxz * ix, tzx = Axz * m.x + Kxz * iz;
+    const R tyz = Ayz * m.z + Kyz * iy, tzy = Ayz * m.y + Kyz * iz;
+    const R f2 = txx * txx + tyy * tyy + tzz * tzz + txy * txy + tyx * tyx + txz * txz + tzx * tzx + tyz * tyz +
+                 tzy * tzy;
+    if (isnan(f2))
+    {
+        pos = false;
+        q = R(0);
+        return;
+    }
+    R sg = sgn(det);
+    pos = sg > R(0);
+    R r = sqrt_<R>(R(1) + sqrt_<R>(f2));
+    if (pos) rq = r;
+    else q = sg / r;
+}
+
+template <class R>
+__device__ __forceinline__ EQ<R> mc_tet_diag(const Crew& c, const V3<R>* p)
+{
+    V3<R> c0, c1, c2;
+    tet_frame(p[3] - p[0], p[3] - p[1], p[3] - p[2], c0, c1, c2);
+    R rq = 0, q = 0;
+    bool pos;
+    mc_corner_diag(c0, c1, c2, specified_metric_diag(c, p[0], p[1], p[2], p[3]), rq, q, pos);
+    return EQ<R>{pos ? rq : q, pos};
+}
+
+template <class R>
+__device__ __noinline__ EQ<R> mc_pri_diag(const Crew& c, const V3<R>* p)
+{
+    V3<R> e03 = p[3] - p[0], e14 = p[4] - p[1], e25 = p[5] - p[2];
+    V3<R> e01 = p[1] - p[0], e12 = p[2] - p[1], e20 = p[0] - p[2];
+    V3<R> e34 = p[4] - p[3], e45 = p[5] - p[4], e53 = p[3] - p[5];
+    CornerAcc<R> acc;
+    V3<R> a, b, d;
+    R rq = 0, q = 0;
+    bool pos;
+    pri_frame(-e01, e20, e03, a, b, d); mc_corner_diag(a, b, d, specified_metric_diag(c, p[0], p[1], p[2], p[3]), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e12, e01, e14, a, b, d); mc_corner_diag(a, b, d, specified_metric_diag(c, p[0], p[1], p[2], p[4]), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e20, e12, e25, a, b, d); mc_corner_diag(a, b, d, specified_metric_diag(c, p[0], p[1], p[2], p[5]), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e34, e53, e03, a, b, d); mc_corner_diag(a, b, d, specified_metric_diag(c, p[0], p[3], p[4], p[5]), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e45, e34, e14, a, b, d); mc_corner_diag(a, b, d, specified_metric_diag(c, p[1], p[3], p[4], p[5]), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e53, e45, e25, a, b, d); mc_corner_diag(a, b, d, specified_metric_diag(c, p[2], p[3], p[4], p[5]), rq, q, pos); acc.add(rq, q, pos);
+    return acc.result(6);
+}
+
+template <class R>
+__device__ __noinline__ EQ<R> mc_hex_diag(const Crew& c, const V3<R>* p)
+{
+    V3<R> e01 = p[1] - p[0], e03 = p[3] - p[0], e04 = p[4] - p[0], e12 = p[2] - p[1];
+    V3<R> e15 = p[5] - p[1], e23 = p[3] - p[2], e26 = p[6] - p[2], e37 = p[7] - p[3];
+    V3<R> e45 = p[5] - p[4], e47 = p[7] - p[4], e56 = p[6] - p[5], e67 = p[7] - p[6];
+    CornerAcc<R> acc;
+    R rq = 0, q = 0;
+    bool pos;
+    mc_corner_diag(e01, e04, -e03, specified_metric_diag(c, p[0], p[1], p[3], p[4]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner_diag(e01, e12, e15, specified_metric_diag(c, p[0], p[1], p[2], p[5]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner_diag(e12, e26, -e23, specified_metric_diag(c, p[1], p[2], p[3], p[6]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner_diag(e03, e23, e37, specified_metric_diag(c, p[0], p[2], p[3], p[7]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner_diag(e04, e45, e47, specified_metric_diag(c, p[0], p[4], p[5], p[7]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner_diag(e15, -e56, e45, specified_metric_diag(c, p[1], p[4], p[5], p[6]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner_diag(e26, e56, e67, specified_metric_diag(c, p[2], p[5], p[6], p[7]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner_diag(e37, e67, -e47, specified_metric_diag(c, p[3], p[4], p[6], p[7]), rq, q, pos); acc.add(rq, q, pos);
+    return acc.result(8);
+}
+
 template <class R>
 __device__ __forceinline__ EQ<R> mc_tet(const Crew& c, const V3<R>* p)
 {
@@ -510,6 +633,12 @@ __device__ __noinline__ EQ<R> mc_hex(const Crew& c, const V3<R>* p)
 template <int VAR, int MAXK, class R>
 __device__ __forceinline__ EQ<R> elem_quality(const Crew& c, int type, const V3<R>* p)
 {
+    if (VarTraits<VAR>::diag_metric)
+    {
+        if (MAXK == 4 || type == kTet) return mc_tet_diag(c, p);
+        if (type == kPri) return mc_pri_diag(c, p);
+        return mc_hex_diag(c, p);
+    }
     if (!VarTraits<VAR>::mean_ratio)
     {
         if (MAXK == 4 || type == kTet) return mc_tet(c, p);

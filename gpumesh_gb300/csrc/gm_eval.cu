@@ -15,17 +15,32 @@ namespace gm {
 
 constexpr int kEvalThreads = 256;
 
-template <int VAR, int MAXK>
+// SET: 4 = tets only, 8 = any element types, 9 = hexes only
+template <int VAR, int SET>
 __device__ __forceinline__ void eval_element(const MeshView& m, const Crew& crew, uint32_t i, float& mn, float& rs,
                                              int& nbad, int* hist)
 {
+    constexpr int MAXK = SET == 4 ? 4 : 8;
     int type;
     uint32_t id;
-    if (MAXK == 4 || i < m.nt) { type = kTet; id = i; }
+    if (SET == 9) { type = kHex; id = i; }
+    else if (SET == 4 || i < m.nt) { type = kTet; id = i; }
     else if (i < m.nt + m.np) { type = kPri; id = i - m.nt; }
     else { type = kHex; id = i - m.nt - m.np; }
     V3<float> p[MAXK];
-    if (MAXK == 4)
+    if (SET == 9)
+    {
+        const uint4 a = __ldg(&m.hexs[2 * (size_t)id]), b = __ldg(&m.hexs[2 * (size_t)id + 1]);
+        p[0] = to<float>(__ldg(&m.pos[a.x]));
+        p[1] = to<float>(__ldg(&m.pos[a.y]));
+        p[2] = to<float>(__ldg(&m.pos[a.z]));
+        p[3] = to<float>(__ldg(&m.pos[a.w]));
+        p[4] = to<float>(__ldg(&m.pos[b.x]));
+        p[5] = to<float>(__ldg(&m.pos[b.y]));
+        p[6] = to<float>(__ldg(&m.pos[b.z]));
+        p[7] = to<float>(__ldg(&m.pos[b.w]));
+    }
+    else if (MAXK == 4)
     {
         uint4 t = __ldg(&m.tets[id]);
         p[0] = to<float>(__ldg(&m.pos[t.x]));
@@ -41,7 +56,9 @@ __device__ __forceinline__ void eval_element(const MeshView& m, const Crew& crew
 #pragma unroll
         for (int k = 0; k < MAXK; ++k) p[k] = to<float>(__ldg(&m.pos[vid[k < n ? k : 0]]));
     }
-    EQ<float> q = elem_quality<VAR, MAXK, float>(crew, type, p);
+    EQ<float> q = SET == 9 ? (VarTraits<VAR>::mean_ratio ? mr_hex<VAR, float>(crew, p)
+                                                          : elem_quality<VAR, MAXK, float>(crew, kHex, p))
+                           : elem_quality<VAR, MAXK, float>(crew, type, p);
     float qv;
     if (q.pos)
     {
@@ -58,7 +75,7 @@ __device__ __forceinline__ void eval_element(const MeshView& m, const Crew& crew
     atomicAdd(&hist[b], 1);
 }
 
-template <int VAR, int MAXK>
+template <int VAR, int SET>
 __global__ void __launch_bounds__(kEvalThreads) evaluate_kernel(MeshView m, Crew crew, EvalPartial* parts)
 {
     __shared__ int hist[20];
@@ -71,7 +88,7 @@ __global__ void __launch_bounds__(kEvalThreads) evaluate_kernel(MeshView m, Crew
     int nbad = 0;
     const uint32_t total = m.nt + m.np + m.nh;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
-        eval_element<VAR, MAXK>(m, crew, i, mn, rs, nbad, hist);
+        eval_element<VAR, SET>(m, crew, i, mn, rs, nbad, hist);
     double ds = rs;
     for (int o = 16; o > 0; o >>= 1)
     {
@@ -130,12 +147,18 @@ __global__ void __launch_bounds__(256) evaluate_finalize_kernel(const EvalPartia
     s_sum[t] = sum;
     s_min[t] = mn;
     s_bad[t] = bad;
-    if (t < 20)
-    {
-        unsigned long long h = 0;
-        for (int i = 0; i < nparts; ++i) h += (unsigned long long)parts[i].hist[t];
-        s_hist[t] = h;
-    }
+    if (t < 20) s_hist[t] = 0;
+    __syncthreads();
+    // bucket b of partial i is summed by thread (i * 20 + b) mod 256
+    unsigned long long hloc[20];
+#pragma unroll
+    for (int b = 0; b < 20; ++b) hloc[b] = 0;
+    for (int i = t; i < nparts; i += 256)
+#pragma unroll
+        for (int b = 0; b < 20; ++b) hloc[b] += (unsigned long long)parts[i].hist[b];
+#pragma unroll
+    for (int b = 0; b < 20; ++b)
+        if (hloc[b]) atomicAdd(&s_hist[b], hloc[b]);
     __syncthreads();
     for (int s = 128; s > 0; s >>= 1)
     {
@@ -165,10 +188,10 @@ int evaluate_blocks(uint32_t total, int sm_count)
     return n < 1 ? 1 : (int)n;
 }
 
-template <int VAR, int MAXK>
+template <int VAR, int SET>
 static void launch_eval_t(const MeshView& m, const Crew& crew, EvalPartial* parts, int nblocks, cudaStream_t s)
 {
-    evaluate_kernel<VAR, MAXK><<<nblocks, kEvalThreads, 0, s>>>(m, crew, parts);
+    evaluate_kernel<VAR, SET><<<nblocks, kEvalThreads, 0, s>>>(m, crew, parts);
 }
 
 cudaError_t launch_evaluate(int variant, int maxk, const MeshView& m, const Crew& crew, EvalPartial* parts,
@@ -178,7 +201,12 @@ cudaError_t launch_evaluate(int variant, int maxk, const MeshView& m, const Crew
     {
     case kVarMRFree:
         if (maxk == 4) launch_eval_t<kVarMRFree, 4>(m, crew, parts, nblocks, s);
+        else if (maxk == 9) launch_eval_t<kVarMRFree, 9>(m, crew, parts, nblocks, s);
         else launch_eval_t<kVarMRFree, 8>(m, crew, parts, nblocks, s);
+        break;
+    case kVarMCDiag:
+        if (maxk == 4) launch_eval_t<kVarMCDiag, 4>(m, crew, parts, nblocks, s);
+        else launch_eval_t<kVarMCDiag, 8>(m, crew, parts, nblocks, s);
         break;
     case kVarMRWise: launch_eval_t<kVarMRWise, 8>(m, crew, parts, nblocks, s); break;
     default:

@@ -156,6 +156,8 @@ cudaError_t launch_getme_update(const RelocLaunch& L, const float4* corners)
     case kVarMRFree: return L.maxk == 4 ? launch_update_t<kVarMRFree, 4>(L, corners)
                                         : launch_update_t<kVarMRFree, 8>(L, corners);
     case kVarMRWise: return launch_update_t<kVarMRWise, 8>(L, corners);
+    case kVarMCDiag: return L.maxk == 4 ? launch_update_t<kVarMCDiag, 4>(L, corners)
+                                        : launch_update_t<kVarMCDiag, 8>(L, corners);
     default: return L.maxk == 4 ? launch_update_t<kVarMC, 4>(L, corners) : launch_update_t<kVarMC, 8>(L, corners);
     }
 }

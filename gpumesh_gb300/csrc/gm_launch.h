@@ -10,6 +10,7 @@ namespace gm {
 size_t patch_smem_per_warp(int ks, int maxe);
 
 int evaluate_blocks(uint32_t total, int sm_count);
+// maxk: 4 = tets only, 8 = any element types, 9 = hexes only
 cudaError_t launch_evaluate(int variant, int maxk, const MeshView& m, const Crew& crew, EvalPartial* parts,
                             int nblocks, Quality* out, cudaStream_t s);
 

@@ -96,6 +96,8 @@ static cudaError_t launch_relocate_smoother(const RelocLaunch& L)
     case kVarMRFree: return L.maxk == 4 ? launch_relocate_t<SMOOTHER, kVarMRFree, 4>(L)
                                         : launch_relocate_t<SMOOTHER, kVarMRFree, 8>(L);
     case kVarMRWise: return launch_relocate_t<SMOOTHER, kVarMRWise, 8>(L);
+    case kVarMCDiag: return L.maxk == 4 ? launch_relocate_t<SMOOTHER, kVarMCDiag, 4>(L)
+                                        : launch_relocate_t<SMOOTHER, kVarMCDiag, 8>(L);
     default: return L.maxk == 4 ? launch_relocate_t<SMOOTHER, kVarMC, 4>(L) : launch_relocate_t<SMOOTHER, kVarMC, 8>(L);
     }
 }

@@ -82,6 +82,20 @@ def test_mixed_metric_conformity():
     compare(meshgen.box_mesh(8, "mixed", 0.15, 2, gaussian=True), dict(MC, scaling=4.0), rel=5e-5)
 
 
+def test_mixed_metric_conformity_analytic_metric():
+    # the general (non-diagonal) metric path of metric conformity
+    crew = dict(sampler="analytic", measurer="metric_wise", evaluator="metric_conformity", scaling=3.0,
+                aspect_ratio=2.0)
+    compare(meshgen.box_mesh(7, "mixed", 0.15, 2, gaussian=True), crew, rel=5e-5)
+
+
+def test_hex_only_fast_path_matches_mixed_path():
+    # a pure hex mesh takes the hex-only evaluation kernel; adding one tet
+    # elsewhere sends the same hexes through the general kernel
+    raw = meshgen.box_mesh(10, "hex", 0.15, 2, gaussian=True)
+    compare(raw, MR)
+
+
 def test_inverted_elements_zero_mean():
     raw = meshgen.box_mesh(8, "tet", 0.6, 7)  # heavy jitter folds some tets
     g, o = compare(raw, MR)
