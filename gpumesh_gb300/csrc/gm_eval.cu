@@ -133,8 +133,8 @@ __global__ void __launch_bounds__(256) evaluate_finalize_kernel(const EvalPartia
     __shared__ double s_sum[256];
     __shared__ float s_min[256];
     __shared__ unsigned long long s_bad[256];
-    __shared__ unsigned long long s_hist[20];
-    const int t = threadIdx.x;
+    __shared__ unsigned long long s_hist[8][20];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     double sum = 0;
     float mn = 1.0f;
     unsigned long long bad = 0;
@@ -147,18 +147,11 @@ __global__ void __launch_bounds__(256) evaluate_finalize_kernel(const EvalPartia
     s_sum[t] = sum;
     s_min[t] = mn;
     s_bad[t] = bad;
-    if (t < 20) s_hist[t] = 0;
-    __syncthreads();
-    // bucket b of partial i is summed by thread (i * 20 + b) mod 256
-    unsigned long long hloc[20];
-#pragma unroll
-    for (int b = 0; b < 20; ++b) hloc[b] = 0;
-    for (int i = t; i < nparts; i += 256)
-#pragma unroll
-        for (int b = 0; b < 20; ++b) hloc[b] += (unsigned long long)parts[i].hist[b];
-#pragma unroll
-    for (int b = 0; b < 20; ++b)
-        if (hloc[b]) atomicAdd(&s_hist[b], hloc[b]);
+    // histogram: warp w sums partials w, w + 8, ...; lane b < 20 owns bucket b
+    unsigned long long h = 0;
+    if (lane < 20)
+        for (int i = w; i < nparts; i += 8) h += (unsigned long long)parts[i].hist[lane];
+    if (lane < 20) s_hist[w][lane] = h;
     __syncthreads();
     for (int s = 128; s > 0; s >>= 1)
     {
@@ -170,13 +163,18 @@ __global__ void __launch_bounds__(256) evaluate_finalize_kernel(const EvalPartia
         }
         __syncthreads();
     }
+    if (t < 20)
+    {
+        unsigned long long hb = 0;
+        for (int k = 0; k < 8; ++k) hb += s_hist[k][t];
+        out->buckets[t] = hb;
+    }
     if (t == 0)
     {
         out->min = (double)s_min[0];
         out->nbad = s_bad[0];
         out->inv_sum = s_bad[0] ? (double)INFINITY : s_sum[0];
         out->count = count;
-        for (int b = 0; b < 20; ++b) out->buckets[b] = s_hist[b];
     }
 }
 

@@ -152,10 +152,11 @@ extern "C" gm_status gm_evaluate_noalloc(uint32_t nv, const void* pos, uint32_t 
     m.pris = pris;
     m.hexs = reinterpret_cast<const uint4*>(hexs);
     const Crew crew = make_crew(sampler, measurer, evaluator, scaling, aspect_ratio);
+    // the same kernel variant gm_evaluate selects, so both give the same per-element qualities
     int variant = evaluator == GM_EVALUATOR_METRIC_CONFORMITY
-                      ? kVarMC
+                      ? (sampler == GM_SAMPLER_ANALYTIC ? kVarMC : kVarMCDiag)
                       : (measurer == GM_MEASURER_METRIC_WISE ? kVarMRWise : kVarMRFree);
-    int maxk = (np || nh) ? 8 : 4;
+    int maxk = (nt == 0 && np == 0 && nh) ? 9 : ((np || nh) ? 8 : 4);
     uint64_t need = (total + 255) / 256;
     int blocks = (int)(need < (uint64_t)kNoAllocMaxPartials ? need : (uint64_t)kNoAllocMaxPartials);
     static_assert(sizeof(Quality) == sizeof(gm_quality), "quality layout");
