@@ -1,0 +1,59 @@
+"""Generate tests/golden/*.npz from the reference's own CPU code.
+
+Each fixture holds a small seeded mesh (inputs), the reference's NodeGroups
+permutation and colour groups, its mesh evaluation, and the vertex positions
+after one pass of each smoother (reference constants), all produced by the
+reference compiled from its sources (oracle/refbuild.py).  Run from the repo
+root where the reference tree exists:
+
+    python tests/golden/make_golden.py
+"""
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import pyref  # noqa: E402
+from gpumesh_gb300 import meshgen  # noqa: E402
+
+CASES = {
+    "tet_box_6": (lambda: meshgen.box_mesh(6, "tet", 0.3, 0), "box", dict(sampler="uniform", evaluator="mean_ratio")),
+    "mixed_box_5": (lambda: meshgen.box_mesh(5, "mixed", 0.15, 2, gaussian=True), "box",
+                    dict(sampler="uniform", evaluator="mean_ratio")),
+    "sphere_mc_8": (lambda: meshgen.sphere_mesh(8, 0.25, 1), "sphere",
+                    dict(sampler="sine", evaluator="metric_conformity", scaling=4.0)),
+}
+SMOOTHERS = ["nelder_mead", "gradient_descent", "spawn_search", "getme"]
+
+
+def make(name):
+    build, boundary, crew = CASES[name]
+    raw = build()
+    out = dict(pos=raw.pos, tets=raw.tets, pris=raw.pris, hexs=raw.hexs, cid=raw.cid, con_kind=raw.con_kind,
+               con_param=raw.con_param, boundary=boundary, sampler=crew["sampler"], evaluator=crew["evaluator"],
+               scaling=crew.get("scaling", 1.0))
+    ref = pyref.RefMesh(raw, boundary)
+    ref.set_crew(**crew)
+    out["perm"] = ref.perm()
+    base, members, ranges = ref.groups()
+    out.update(group_base=base, members=members, ranges=ranges)
+    e = ref.evaluate()
+    out.update(eval_min=e["min"], eval_inv_sum=e["inv_sum"], eval_count=e["count"], eval_buckets=e["buckets"])
+    start = ref.pos
+    for s in SMOOTHERS:
+        ref.pos = start
+        ref.smooth(s, 1)
+        out["after_" + s] = ref.pos
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
+if __name__ == "__main__":
+    for n in CASES:
+        make(n)
+        print("wrote", n)
