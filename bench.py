@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-eval-roofline", action="store_true")
+    ap.add_argument("--batch-meshes", type=int, default=4096, help="C4: number of meshes")
     ap.add_argument("--only", choices=["eval", "relocate"], default=None,
                     help="profiling driver: a few launches of one kernel family, no JSON line")
     return ap.parse_args()
@@ -437,6 +438,101 @@ def profile_driver(args):
     torch.cuda.synchronize()
 
 
+def bench_batched(args, rank, world, local):
+    """C4: 4,096 jittered tet cubes (cells per axis log-uniform in [4, 24],
+    jitter U(+-0.3h), seed 3), one Nelder-Mead pass (BASELINE parameters) plus
+    a per-mesh evaluation, as ONE captured CUDA graph (one persistent
+    relocation launch, one evaluation launch) with an autotuned launch shape;
+    against the plain path, one mesh per launch sequence."""
+    import torch
+
+    torch.cuda.set_device(local)
+    from gpumesh_gb300 import mesh as M
+    from gpumesh_gb300 import meshgen, workloads
+
+    count = args.batch_meshes
+    sizes = meshgen.batch_sizes(count, 4, 24, 3)
+    t0 = time.perf_counter()
+    devs, movable, tets = [], 0, 0
+    for i, n in enumerate(sizes):
+        raw = meshgen.box_mesh(int(n), "tet", 0.3, 3 * 1000003 + i)
+        perm, groups = M.node_groups_build(raw)
+        raw = M.permute_mesh(raw, perm)
+        d = M.DeviceMesh(raw, groups)
+        d.set_crew("uniform", "metric_free", "mean_ratio")
+        d.save_positions()
+        devs.append(d)
+        movable += int(np.count_nonzero(raw.cid >= 0))
+        tets += int(raw.tets.shape[0])
+    setup_s = time.perf_counter() - t0
+    params = workloads.NM_PARAMS
+    batch = M.Batch(devs)
+    wpb, cps, tune_ms = batch.tune("nelder_mead", params)
+    batch.capture("nelder_mead", params, eval_slot=0)
+    stream = torch.cuda.ExternalStream(batch.stream)
+
+    def restore():
+        for d in devs:
+            d.restore_positions()
+        torch.cuda.synchronize()
+
+    # ---- batched ----
+    for _ in range(args.warmup):
+        restore()
+        batch.replay()
+        batch.sync()
+    times, lat = [], []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            restore()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            batch.replay()
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b) * 1e-3)
+            lat.append(batch.latencies_ms())
+    assert batch.status() == 0
+    qual = batch.read_quality(0)
+    t_batched = statistics.median(times)
+    lat = np.concatenate(lat)
+    # ---- plain: one mesh per launch sequence (every colour of that mesh, then its evaluation) ----
+    restore()
+    plain_times, plain_lat = [], []
+    for step in range(max(1, args.steps)):
+        restore()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for d in devs:
+            ta = time.perf_counter()
+            d.smooth_pass("nelder_mead", params)
+            d.evaluate_async(0)
+            if step == 0:
+                d.sync()
+                plain_lat.append((time.perf_counter() - ta) * 1e3)
+        torch.cuda.synchronize()
+        plain_times.append(time.perf_counter() - t1)
+    t_plain = statistics.median(plain_times[1:] if len(plain_times) > 1 else plain_times)
+    value = movable * world / t_batched
+    plain_value = movable * world / t_plain
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_batched * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"C4 batched: {count} tet cubes, cells/axis log-uniform [4, 24], NM 1 pass + "
+                                   "per-mesh evaluation, one CUDA graph", "meshes": count, "tets": tets,
+                       "relocations_per_step": movable, "launch_shape": {"warps_per_block": wpb, "ctas_per_sm": cps},
+                       "setup_s": round(setup_s, 1), "parallelism": f"replicas x{world}"},
+            "plain": {"value": plain_value, "unit": UNIT, "s_per_step": t_plain,
+                      "p50_mesh_ms": float(np.percentile(plain_lat, 50)), "p99_mesh_ms": float(np.percentile(plain_lat, 99))},
+            "batched_vs_plain": value / plain_value,
+            "latency_ms": {"p50": float(np.percentile(lat[lat >= 0], 50)), "p99": float(np.percentile(lat[lat >= 0], 99)),
+                           "note": "per mesh: persistent-kernel start to the mesh's last relocated vertex"},
+            "quality": {"min_of_mins": min(q.minimumQuality() for q in qual),
+                        "mean_of_means": float(np.mean([q.harmonicMean() for q in qual]))},
+            "gpu_launches": 2 * args.steps + 1 * args.steps, "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.only:
@@ -445,6 +541,8 @@ def main():
     rank, world, local = dist_init(args.gpus)
     if args.impl == "reference":
         bench_reference(args, rank, world)
+    elif args.workload == "C4":
+        bench_batched(args, rank, world, local)
     else:
         bench_gpu(args, rank, world, local)
     if world > 1:

@@ -83,6 +83,23 @@ def lib():
         "gm_mesh_save_positions": [vp],
         "gm_mesh_restore_positions": [vp],
         "gm_probe_fp32_tflops": [ctypes.POINTER(ctypes.c_double)],
+        "gm_batch_create": [ctypes.POINTER(vp), vp, u32],
+        "gm_batch_destroy": [vp],
+        "gm_batch_stream": [vp, ctypes.POINTER(vp)],
+        "gm_batch_sync": [vp],
+        "gm_batch_set_config": [vp, i32, i32],
+        "gm_batch_tune": [vp, i32, vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_double)],
+        "gm_batch_smooth_pass": [vp, i32, vp],
+        "gm_batch_evaluate": [vp, u32],
+        "gm_batch_read_quality": [vp, u32, vp],
+        "gm_batch_capture_pass": [vp, i32, vp, i32],
+        "gm_batch_replay": [vp],
+        "gm_batch_status": [vp],
+        "gm_batch_set_spin_limit": [vp, u64],
+        "gm_batch_inject_stall": [vp, u32],
+        "gm_batch_counters": [vp, vp, i32],
+        "gm_batch_info": [vp, vp],
+        "gm_batch_latencies": [vp, vp],
         "gm_evaluate_noalloc": [u32, vp, u32, vp, u32, vp, u32, vp, i32, i32, i32, ctypes.c_double,
                                 ctypes.c_double, vp, vp],
     }

@@ -12,167 +12,15 @@
 #include <string>
 #include <vector>
 
-#include "../../include/gpumesh_gb300.h"
-#include "gm_internal.h"
-#include "gm_launch.h"
+
+#include "gm_host.h"
 
 namespace gm {
-
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
-
-struct ApiError : std::runtime_error
-{
-    gm_status status;
-    ApiError(gm_status s, const std::string& m) : std::runtime_error(m), status(s) {}
-};
-
-#define GM_CUDA(call)                                                                                      \
-    do                                                                                                     \
-    {                                                                                                      \
-        cudaError_t e_ = (call);                                                                           \
-        if (e_ != cudaSuccess)                                                                             \
-            throw ApiError(e_ == cudaErrorMemoryAllocation ? GM_ERR_OUT_OF_MEMORY : GM_ERR_CUDA,           \
-                           std::string(#call) + ": " + cudaGetErrorString(e_));                            \
-    } while (0)
-
-static void require(bool ok, const std::string& msg)
-{
-    if (!ok) throw ApiError(GM_ERR_INVALID_ARG, msg);
-}
-
-template <class F>
-static gm_status guarded(F&& f)
-{
-    try
-    {
-        f();
-        return GM_OK;
-    }
-    catch (const ApiError& e)
-    {
-        set_error(e.what());
-        return e.status;
-    }
-    catch (const std::bad_alloc&)
-    {
-        set_error("host allocation failed");
-        return GM_ERR_OUT_OF_MEMORY;
-    }
-    catch (const std::exception& e)
-    {
-        set_error(e.what());
-        return GM_ERR_STATE;
-    }
-}
-
-// growable device buffer
-template <class T>
-struct DBuf
-{
-    T* p = nullptr;
-    size_t cap = 0;
-    void reserve(size_t n)
-    {
-        if (n <= cap && p) return;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
-        GM_CUDA(cudaMalloc(&p, bytes));
-        cap = std::max<size_t>(n, 1);
-    }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
-
-template <class T>
-static void upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s)
-{
-    b.reserve(n);
-    if (n) GM_CUDA(cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
-}
-
 }  // namespace gm
 
 using namespace gm;
-
-struct gm_mesh
-{
-    int device = 0;
-    int sm_count = 0;
-    cudaStream_t stream = 0;
-    uint32_t nv = 0, nt = 0, np = 0, nh = 0;
-    DBuf<float4> pos;
-    DBuf<uint4> tets;
-    DBuf<uint32_t> pris;
-    DBuf<uint4> hexs;
-    DBuf<uint32_t> ve_off, ve, vv_off, vv;
-    DBuf<int32_t> cid;
-    DBuf<Constraint> con;
-    int ncon = 0;
-    DBuf<uint32_t> members;
-    uint32_t n_members = 0;
-    std::vector<uint32_t> group_base;
-    DBuf<Quality> quality;
-    uint32_t n_quality_slots = 0;
-    DBuf<EvalPartial> parts;
-    DBuf<float4> corners;
-    DBuf<float4> saved;
-    DBuf<Counters> ctr;
-    // FP64 acceptance hand-over: per-member slots and one counter per group
-    DBuf<uint32_t> def_v;
-    DBuf<float4> def_old, def_new;
-    DBuf<uint32_t> def_count;
-    Crew crew{};
-    int ks = 4;
-    int maxe = 32;
-    int warps_per_block = 4;
-    std::vector<float4> staging;  // host conversion buffer
-
-    MeshView view() const
-    {
-        MeshView v;
-        v.nv = nv;
-        v.nt = nt;
-        v.np = np;
-        v.nh = nh;
-        v.pos = pos.p;
-        v.tets = tets.p;
-        v.pris = pris.p;
-        v.hexs = hexs.p;
-        v.ve_off = ve_off.p;
-        v.ve = ve.p;
-        v.vv_off = vv_off.p;
-        v.vv = vv.p;
-        v.cid = cid.p;
-        v.con = con.p;
-        v.ncon = ncon;
-        return v;
-    }
-
-    // evaluator x measurer variant of the vertex kernels
-    int variant() const
-    {
-        if (crew.evaluator == GM_EVALUATOR_METRIC_CONFORMITY)
-            return crew.sampler == GM_SAMPLER_ANALYTIC ? kVarMC : kVarMCDiag;
-        return crew.measurer == GM_MEASURER_METRIC_WISE ? kVarMRWise : kVarMRFree;
-    }
-    // variant of the GETMe element pass, whose volumes also follow the measurer
-    int element_variant() const
-    {
-        if (crew.evaluator == GM_EVALUATOR_METRIC_CONFORMITY)
-            return crew.measurer == GM_MEASURER_METRIC_WISE ? kVarMCWise : kVarMC;
-        return crew.measurer == GM_MEASURER_METRIC_WISE ? kVarMRWise : kVarMRFree;
-    }
-    int maxk() const { return (np || nh) ? 8 : 4; }
-    // element set of the evaluation kernel: 4 tets only, 8 mixed, 9 hexes only
-    int elem_set() const { return (nt == 0 && np == 0 && nh) ? 9 : maxk(); }
-};
 
 namespace {
 
@@ -358,6 +206,10 @@ void relocate_group(gm_mesh* m, int smoother, const SmoothParams& sp, uint32_t b
 }
 
 }  // namespace
+
+namespace gm {
+SmoothParams parse_smooth_params(int smoother, const double* p) { return parse_params(smoother, p); }
+}  // namespace gm
 
 extern "C" {
 

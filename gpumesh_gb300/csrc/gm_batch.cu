@@ -1,0 +1,364 @@
+// Batched smoothing: many meshes of uneven size relocated by one persistent
+// kernel launch, and evaluated per mesh by one launch.
+//
+// Work queue.  The vertices to relocate are enumerated as segments
+// (colour g, mesh m) ordered by colour first, then mesh; a segment of colour
+// g of mesh m may start once every vertex of mesh m in colours < g is done.
+// Warps claim small chunks of consecutive items with one atomic and process
+// them in order.  Everything a claimed item waits for sits earlier in the
+// queue and was therefore already claimed by a running warp, so the oldest
+// unfinished item can always proceed: with every warp of the grid resident
+// (the grid is sized to the occupancy), the queue cannot deadlock.  Waits
+// are still bounded: after `spin_limit` polls a warp sets the batch error
+// word, gives up its item and every other waiter gives up as soon as it sees
+// the error, so a broken dependency ends the launch with an error instead of
+// a hang.
+//
+// Memory ordering: the finishing warp stores the vertex, issues a device
+// fence and increments the mesh's done counter; the waiting warp polls the
+// counter with a volatile load and fences before reading positions, which
+// the relocation code loads with __ldcg (L2, coherent across SMs).
+#include <cuda_runtime.h>
+
+#include "gm_batch.h"
+#include "gm_relocate.cuh"
+
+namespace gm {
+
+constexpr uint32_t kClaimChunk = 4;
+
+__device__ __forceinline__ uint32_t find_segment(const uint32_t* seg_start, uint32_t nseg, uint32_t i)
+{
+    uint32_t lo = 0, hi = nseg;  // seg_start has nseg + 1 entries
+    while (hi - lo > 1)
+    {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&seg_start[mid]) <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int SMOOTHER, int VAR, int MAXK>
+__device__ __forceinline__ void batch_one(const BatchMesh& bm, const SmoothParams& sp, WarpPatch& P, uint32_t v,
+                                          int lane, Counters* ctr)
+{
+    const MeshView& m = bm.view;
+    const Crew& crew = bm.crew;
+    const int cid = m.cid[v];
+    const float4 old = __ldcg(&m.pos[v]);
+    V3<float> out;
+    float q0, q1;
+    int evals = 0;
+    if (SMOOTHER == kSmoothGetme)
+    {
+        // GETMe vertex update: weighted average of the element corners
+        const size_t base[4] = {0, 0, 4 * (size_t)m.nt, 4 * (size_t)m.nt + 6 * (size_t)m.np};
+        uint32_t b = m.ve_off[v], e = m.ve_off[v + 1];
+        float sx = 0, sy = 0, sz = 0, sw = 0;
+        for (uint32_t i = b + lane; i < e; i += kWarp)
+        {
+            uint32_t r = m.ve[i];
+            int type = ref_type(r);
+            float4 c = bm.corners[base[type] + (size_t)ref_id(r) * type_size(type) + ref_local(r)];
+            sx += c.x * c.w;
+            sy += c.y * c.w;
+            sz += c.z * c.w;
+            sw += c.w;
+        }
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            sx += __shfl_xor_sync(0xffffffffu, sx, o);
+            sy += __shfl_xor_sync(0xffffffffu, sy, o);
+            sz += __shfl_xor_sync(0xffffffffu, sz, o);
+            sw += __shfl_xor_sync(0xffffffffu, sw, o);
+        }
+        if (sw == 0.f) return;
+        out = mk(sx / sw, sy / sw, sz / sw);
+        if (cid != 0) out = snap(m, cid, out);
+        stage_patch(m, v, P, lane);
+        if (lane == 0)
+        {
+            P.cand[0] = old;
+            P.cand[1] = make_float4(out.x, out.y, out.z, 0.f);
+        }
+        __syncwarp();
+        patch_multi<VAR, MAXK, float>(crew, P, 2, lane);
+        q0 = P.res[0];
+        q1 = P.res[1];
+        evals = 2;
+        __syncwarp();
+    }
+    else
+    {
+        stage_patch(m, v, P, lane);
+        const V3<float> pos = to<float>(old);
+        evals = 2;
+        q0 = patch_uniform<VAR, MAXK, float>(crew, P, pos, lane);
+        if (SMOOTHER == kSmoothNM) out = nelder_mead<VAR, MAXK>(m, crew, sp, P, v, cid, pos, q0, lane, evals);
+        else if (SMOOTHER == kSmoothGD) out = gradient_descent<VAR, MAXK>(m, crew, sp, P, v, cid, pos, lane, evals);
+        else out = spawn_search<VAR, MAXK>(m, crew, sp, P, v, cid, pos, lane, evals);
+        q1 = patch_uniform<VAR, MAXK, float>(crew, P, out, lane);
+    }
+    bool accept;
+    const bool fp64 = !(q0 >= sp.accept_q && q1 >= sp.accept_q);
+    if (fp64)
+    {
+        // near-degenerate patch: the acceptance test in FP64
+        const double d0 = patch_uniform<VAR, MAXK, double>(crew, P, to<double>(old), lane);
+        const double d1 = patch_uniform<VAR, MAXK, double>(crew, P, mk<double>(out.x, out.y, out.z), lane);
+        accept = !(d1 < d0);
+    }
+    else
+        accept = SMOOTHER == kSmoothGetme ? !(q1 < q0) : true;
+    if (lane == 0 && accept) m.pos[v] = make_float4(out.x, out.y, out.z, old.w);
+    count_work(ctr, evals, P.E, MAXK == 4 ? kTet : kHex, fp64, lane);
+}
+
+template <int SMOOTHER, int VAR, int MAXK>
+__global__ void __launch_bounds__(256) batch_relocate_kernel(BatchArgs a, SmoothParams sp)
+{
+    extern __shared__ __align__(16) char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    WarpPatch P = carve_patch(smem + wib * warp_patch_bytes(MAXK, a.maxe), MAXK, a.maxe);
+    if (threadIdx.x == 0)
+    {
+        unsigned long long now;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+        atomicCAS(&a.ctl->t0, 0ull, now);
+    }
+    while (true)
+    {
+        uint32_t first = 0;
+        if (lane == 0) first = atomicAdd(&a.ctl->next, kClaimChunk);
+        first = __shfl_sync(0xffffffffu, first, 0);
+        if (first >= a.total) break;
+        const uint32_t last = min(first + kClaimChunk, a.total);
+        for (uint32_t i = first; i < last; ++i)
+        {
+            const uint32_t s = find_segment(a.seg_start, a.nseg, i);
+            const Segment sg = a.segs[s];
+            int ok = 1;
+            if (sg.need)
+            {
+                if (lane == 0)
+                {
+                    unsigned long long spins = 0;
+                    while (__ldcv(&a.done[sg.mesh]) < sg.need)
+                    {
+                        if (++spins > a.spin_limit || __ldcv(&a.ctl->error))
+                        {
+                            atomicOr(&a.ctl->error, 1u);
+                            ok = 0;
+                            break;
+                        }
+                        __nanosleep(100);
+                    }
+                }
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                __threadfence();
+            }
+            if (ok)
+            {
+                const BatchMesh& bm = a.meshes[sg.mesh];
+                const uint32_t v = bm.members[sg.member_begin + (i - __ldg(&a.seg_start[s]))];
+                batch_one<SMOOTHER, VAR, MAXK>(bm, sp, P, v, lane, a.ctr);
+            }
+            __syncwarp();
+            if (lane == 0)
+            {
+                __threadfence();
+                const unsigned int d = atomicAdd(&a.done[sg.mesh], 1u) + 1u;
+                if (d == a.meshes[sg.mesh].nmembers)
+                {
+                    unsigned long long now;
+                    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+                    a.finish[sg.mesh] = now;
+                }
+            }
+        }
+    }
+}
+
+template <int SMOOTHER, int VAR, int MAXK>
+static cudaError_t launch_batch_t(const BatchArgs& a, const SmoothParams& sp, int wpb, int ctas_per_sm, int sm_count,
+                                  cudaStream_t s)
+{
+    auto kern = batch_relocate_kernel<SMOOTHER, VAR, MAXK>;
+    size_t smem = patch_smem_per_warp(MAXK, a.maxe) * wpb;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32 * wpb, smem);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) return cudaErrorInvalidConfiguration;
+    // every CTA must be resident: never more than the occupancy allows
+    int cps = (ctas_per_sm <= 0 || ctas_per_sm > occ) ? occ : ctas_per_sm;
+    kern<<<sm_count * cps, 32 * wpb, smem, s>>>(a, sp);
+    return cudaGetLastError();
+}
+
+template <int SMOOTHER>
+static cudaError_t launch_batch_smoother(const BatchArgs& a, const SmoothParams& sp, int variant, int maxk, int wpb,
+                                         int cps, int sm_count, cudaStream_t s)
+{
+    switch (variant)
+    {
+    case kVarMRFree:
+        return maxk == 4 ? launch_batch_t<SMOOTHER, kVarMRFree, 4>(a, sp, wpb, cps, sm_count, s)
+                         : launch_batch_t<SMOOTHER, kVarMRFree, 8>(a, sp, wpb, cps, sm_count, s);
+    case kVarMCDiag:
+        return maxk == 4 ? launch_batch_t<SMOOTHER, kVarMCDiag, 4>(a, sp, wpb, cps, sm_count, s)
+                         : launch_batch_t<SMOOTHER, kVarMCDiag, 8>(a, sp, wpb, cps, sm_count, s);
+    default: return cudaErrorNotSupported;
+    }
+}
+
+cudaError_t launch_batch_relocate(int smoother, const BatchArgs& a, const SmoothParams& sp, int variant, int maxk,
+                                  int wpb, int cps, int sm_count, cudaStream_t s)
+{
+    if (a.total == 0) return cudaSuccess;
+    switch (smoother)
+    {
+    case kSmoothNM: return launch_batch_smoother<kSmoothNM>(a, sp, variant, maxk, wpb, cps, sm_count, s);
+    case kSmoothGD: return launch_batch_smoother<kSmoothGD>(a, sp, variant, maxk, wpb, cps, sm_count, s);
+    case kSmoothSpawn: return launch_batch_smoother<kSmoothSpawn>(a, sp, variant, maxk, wpb, cps, sm_count, s);
+    default: return launch_batch_smoother<kSmoothGetme>(a, sp, variant, maxk, wpb, cps, sm_count, s);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// batched evaluation: a block table covering every mesh's elements, then one
+// warp per mesh sums its blocks in order (deterministic)
+// ---------------------------------------------------------------------------
+template <int VAR, int MAXK>
+__global__ void __launch_bounds__(256) batch_eval_kernel(const BatchMesh* meshes, const EvalBlock* blocks,
+                                                          EvalPartial* parts)
+{
+    __shared__ int hist[20];
+    __shared__ float wmin[8];
+    __shared__ double wsum[8];
+    __shared__ int wbad[8];
+    if (threadIdx.x < 20) hist[threadIdx.x] = 0;
+    __syncthreads();
+    const EvalBlock eb = blocks[blockIdx.x];
+    const MeshView& m = meshes[eb.mesh].view;
+    const Crew& crew = meshes[eb.mesh].crew;
+    float mn = 1.0f, rs = 0.f;
+    int nbad = 0;
+    for (uint32_t i = eb.begin + threadIdx.x; i < eb.end; i += blockDim.x)
+    {
+        int type;
+        uint32_t id;
+        if (MAXK == 4 || i < m.nt) { type = kTet; id = i; }
+        else if (i < m.nt + m.np) { type = kPri; id = i - m.nt; }
+        else { type = kHex; id = i - m.nt - m.np; }
+        uint32_t vid[8];
+        elem_vertices(m, type, id, vid);
+        V3<float> p[MAXK];
+        const int n = MAXK == 4 ? 4 : type_size(type);
+#pragma unroll
+        for (int k = 0; k < MAXK; ++k) p[k] = to<float>(__ldg(&m.pos[vid[k < n ? k : 0]]));
+        EQ<float> q = elem_quality<VAR, MAXK, float>(crew, type, p);
+        float qv;
+        if (q.pos)
+        {
+            rs += q.v;
+            qv = __frcp_rn(q.v);
+        }
+        else
+        {
+            ++nbad;
+            qv = q.v;
+        }
+        mn = fminf(mn, qv);
+        atomicAdd(&hist[qv > 0.f ? min((int)(qv * 20.f), 19) : 0], 1);
+    }
+    double ds = rs;
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        ds += __shfl_xor_sync(0xffffffffu, ds, o);
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        nbad += __shfl_xor_sync(0xffffffffu, nbad, o);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+    {
+        wmin[w] = mn;
+        wsum[w] = ds;
+        wbad[w] = nbad;
+    }
+    __syncthreads();
+    if (threadIdx.x < 20) parts[blockIdx.x].hist[threadIdx.x] = hist[threadIdx.x];
+    if (threadIdx.x == 0)
+    {
+        EvalPartial& p = parts[blockIdx.x];
+        float bmin = wmin[0];
+        double bsum = wsum[0];
+        int bbad = wbad[0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k)
+        {
+            bmin = fminf(bmin, wmin[k]);
+            bsum += wsum[k];
+            bbad += wbad[k];
+        }
+        p.min = bmin;
+        p.rsum = bsum;
+        p.nbad = bbad;
+        p.pad = 0;
+    }
+}
+
+__global__ void __launch_bounds__(256) batch_eval_finalize_kernel(const BatchMesh* meshes, const uint32_t* mesh_block,
+                                                                   uint32_t nmesh, const EvalPartial* parts,
+                                                                   Quality* out)
+{
+    const uint32_t m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (m >= nmesh) return;
+    const uint32_t b = mesh_block[m], e = mesh_block[m + 1];
+    double sum = 0;
+    float mn = 1.0f;
+    unsigned long long bad = 0, h = 0;
+    for (uint32_t i = b; i < e; ++i)
+    {
+        const EvalPartial& p = parts[i];
+        sum += p.rsum;
+        mn = fminf(mn, p.min);
+        bad += (unsigned long long)p.nbad;
+        if (lane < 20) h += (unsigned long long)p.hist[lane];
+    }
+    Quality& q = out[m];
+    if (lane < 20) q.buckets[lane] = h;
+    if (lane == 0)
+    {
+        const MeshView& v = meshes[m].view;
+        q.min = (double)mn;
+        q.nbad = bad;
+        q.inv_sum = bad ? (double)INFINITY : sum;
+        q.count = v.nt + v.np + v.nh;
+    }
+}
+
+cudaError_t launch_batch_evaluate(const BatchMesh* meshes, uint32_t nmesh, const EvalBlock* blocks, uint32_t nblocks,
+                                  const uint32_t* mesh_block, EvalPartial* parts, Quality* out, int variant, int maxk,
+                                  cudaStream_t s)
+{
+    if (nblocks == 0) return cudaSuccess;
+    switch (variant)
+    {
+    case kVarMRFree:
+        if (maxk == 4) batch_eval_kernel<kVarMRFree, 4><<<nblocks, 256, 0, s>>>(meshes, blocks, parts);
+        else batch_eval_kernel<kVarMRFree, 8><<<nblocks, 256, 0, s>>>(meshes, blocks, parts);
+        break;
+    case kVarMCDiag:
+        if (maxk == 4) batch_eval_kernel<kVarMCDiag, 4><<<nblocks, 256, 0, s>>>(meshes, blocks, parts);
+        else batch_eval_kernel<kVarMCDiag, 8><<<nblocks, 256, 0, s>>>(meshes, blocks, parts);
+        break;
+    default: return cudaErrorNotSupported;
+    }
+    batch_eval_finalize_kernel<<<(nmesh + 7) / 8, 256, 0, s>>>(meshes, mesh_block, nmesh, parts, out);
+    return cudaGetLastError();
+}
+
+}  // namespace gm

@@ -58,6 +58,10 @@ struct Counters
     unsigned long long fp64_vertices;
 };
 
+// Position loads in the relocation kernels bypass L1 (__ldcg): inside the
+// persistent batched kernel other SMs move vertices while this SM reads
+// them, and L1 is not coherent across SMs.
+
 // ---------------------------------------------------------------------------
 // warp-level patch: the incident elements of one vertex staged in shared
 // memory as [slot][element] float4 (conflict-free: lane e reads element e)
@@ -106,7 +110,7 @@ __device__ __forceinline__ void stage_patch(const MeshView& m, uint32_t v, WarpP
         int n = type_size(type);
 #pragma unroll
         for (int k = 0; k < 8; ++k)
-            if (k < n) P.sp[k * P.maxe + i] = m.pos[vid[k]];
+            if (k < n) P.sp[k * P.maxe + i] = __ldcg(&m.pos[vid[k]]);
         P.meta[i] = type | (loc << 2);
     }
     __syncwarp();
@@ -225,7 +229,7 @@ __device__ __forceinline__ R local_size(const MeshView& m, uint32_t v, V3<R> pos
 {
     uint32_t b = m.vv_off[v], e = m.vv_off[v + 1];
     R s = 0;
-    for (uint32_t i = b + lane; i < e; i += kWarp) s += length(to<R>(m.pos[m.vv[i]]) - pos);
+    for (uint32_t i = b + lane; i < e; i += kWarp) s += length(to<R>(__ldcg(&m.pos[m.vv[i]])) - pos);
     for (int o = 16; o > 0; o >>= 1) s += shfl_xor(s, o);
     return s / R(e - b);
 }

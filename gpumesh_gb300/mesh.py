@@ -507,3 +507,86 @@ class GetmeSmoother(AbstractSmoother):
 
 SMOOTHER_CLASSES = {"nelder_mead": NelderMeadSmoother, "gradient_descent": GradientDescentSmoother,
                     "spawn_search": SpawnSearchSmoother, "getme": GetmeSmoother}
+
+
+class Batch:
+    """gm_batch: many resident meshes relocated by one persistent launch per pass."""
+
+    def __init__(self, devices: list):
+        self.devices = list(devices)  # keeps the meshes alive
+        arr = (ctypes.c_void_p * len(self.devices))(*[d.h.value if hasattr(d.h, "value") else d.h
+                                                      for d in self.devices])
+        h = ctypes.c_void_p()
+        N.check(N.lib().gm_batch_create(ctypes.byref(h), ctypes.cast(arr, ctypes.c_void_p), len(self.devices)))
+        self.h = h
+        s = ctypes.c_void_p()
+        N.check(N.lib().gm_batch_stream(self.h, ctypes.byref(s)))
+        self.stream = s.value or 0
+
+    def info(self) -> dict:
+        out = np.zeros(4, np.uint32)
+        N.check(N.lib().gm_batch_info(self.h, N.ptr(out)))
+        return {"meshes": int(out[0]), "vertices": int(out[1]), "segments": int(out[2]), "eval_blocks": int(out[3])}
+
+    def latencies_ms(self) -> np.ndarray:
+        out = np.zeros(len(self.devices), np.float64)
+        N.check(N.lib().gm_batch_latencies(self.h, N.ptr(out)))
+        return out
+
+    def set_config(self, warps_per_block: int, ctas_per_sm: int = 0):
+        N.check(N.lib().gm_batch_set_config(self.h, warps_per_block, ctas_per_sm))
+
+    def tune(self, smoother: str, params=None):
+        w, c, ms = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_double()
+        p = N.params_array(params)
+        N.check(N.lib().gm_batch_tune(self.h, N.SMOOTHERS[smoother], N.ptr(p), ctypes.byref(w), ctypes.byref(c),
+                                      ctypes.byref(ms)))
+        return w.value, c.value, ms.value
+
+    def smooth_pass(self, smoother: str, params=None):
+        p = N.params_array(params)
+        N.check(N.lib().gm_batch_smooth_pass(self.h, N.SMOOTHERS[smoother], N.ptr(p)))
+
+    def evaluate(self, slot: int = 0):
+        N.check(N.lib().gm_batch_evaluate(self.h, slot))
+
+    def read_quality(self, slot: int = 0):
+        n = len(self.devices)
+        arr = (N.Quality * n)()
+        N.check(N.lib().gm_batch_read_quality(self.h, slot, ctypes.cast(arr, ctypes.c_void_p)))
+        return [QualityHistogram.from_native(q) for q in arr]
+
+    def capture(self, smoother: str, params=None, eval_slot: int = -1):
+        p = N.params_array(params)
+        N.check(N.lib().gm_batch_capture_pass(self.h, N.SMOOTHERS[smoother], N.ptr(p), eval_slot))
+
+    def replay(self):
+        N.check(N.lib().gm_batch_replay(self.h))
+
+    def sync(self):
+        N.check(N.lib().gm_batch_sync(self.h))
+
+    def status(self) -> int:
+        return N.lib().gm_batch_status(self.h)
+
+    def set_spin_limit(self, polls: int):
+        N.check(N.lib().gm_batch_set_spin_limit(self.h, polls))
+
+    def inject_stall(self, mesh: int):
+        N.check(N.lib().gm_batch_inject_stall(self.h, mesh))
+
+    def counters(self, reset=False) -> dict:
+        out = np.zeros(5, np.uint64)
+        N.check(N.lib().gm_batch_counters(self.h, N.ptr(out), int(reset)))
+        return {"patch_evals": int(out[0]), "elem_evals": int(out[1] + out[2] + out[3]), "fp64_vertices": int(out[4])}
+
+    def close(self):
+        if getattr(self, "h", None):
+            N.lib().gm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -212,6 +212,55 @@ gm_status gm_getme_update_group(gm_mesh* mesh, const double* params, uint32_t me
  * element evaluations, vertices relocated in FP64].  Synchronous. */
 gm_status gm_mesh_counters(gm_mesh* mesh, uint64_t* out5, int32_t reset);
 
+/* ---- batched path ----------------------------------------------------------
+ * No single counterpart in the reference (one mesh per process, one launch
+ * and one host synchronisation per colour: SmoothVertices.cu:28-47).  A
+ * batch relocates the independent groups of many device-resident meshes in
+ * ONE persistent kernel launch per pass: vertices are taken from a device
+ * work queue ordered by (colour, mesh), and a mesh's colour g starts as soon
+ * as that mesh's colours < g are done (device counters, bounded waits).
+ * Meshes keep their own buffers; upload them, their groups, constraints and
+ * crew before creating the batch, and do not re-upload them while it lives.
+ * All meshes of a batch share the evaluator / measurer pair (mean ratio with
+ * the metric-free measurer, or metric conformity with a diagonal metric). */
+typedef struct gm_batch gm_batch;
+gm_status gm_batch_create(gm_batch** out, gm_mesh* const* meshes, uint32_t n);
+gm_status gm_batch_destroy(gm_batch* batch);
+/* the batch's own (non-blocking) stream, as a cudaStream_t */
+gm_status gm_batch_stream(gm_batch* batch, void** stream);
+gm_status gm_batch_sync(gm_batch* batch);
+/* launch shape of the persistent kernel: warps per block (1, 2, 4, 8) and
+ * CTAs per SM (0: as many as fit; never more than fit, since every CTA of
+ * the persistent grid must be resident) */
+gm_status gm_batch_set_config(gm_batch* batch, int32_t warps_per_block, int32_t ctas_per_sm);
+/* autotuner: times one pass per candidate shape from the same positions
+ * (kept in each mesh's save slot), restores them, keeps the fastest */
+gm_status gm_batch_tune(gm_batch* batch, int32_t smoother, const double* params, int32_t* best_warps_per_block,
+                        int32_t* best_ctas_per_sm, double* best_ms);
+/* one relocation pass of every mesh (GETMe: per-mesh element passes, then
+ * the batched vertex update); asynchronous on the batch stream */
+gm_status gm_batch_smooth_pass(gm_batch* batch, int32_t smoother, const double* params);
+/* per-mesh quality (one gm_quality per mesh) into device slot `slot` */
+gm_status gm_batch_evaluate(gm_batch* batch, uint32_t slot);
+gm_status gm_batch_read_quality(gm_batch* batch, uint32_t slot, gm_quality* out_per_mesh);
+/* capture one pass (and, if eval_slot >= 0, its evaluation) as a CUDA graph;
+ * gm_batch_replay launches it */
+gm_status gm_batch_capture_pass(gm_batch* batch, int32_t smoother, const double* params, int32_t eval_slot);
+gm_status gm_batch_replay(gm_batch* batch);
+/* GM_ERR_TIMEOUT if a dependency wait of the last pass gave up; synchronous */
+gm_status gm_batch_status(gm_batch* batch);
+/* bound of the dependency waits, in polls of ~100 ns (default 2e7) */
+gm_status gm_batch_set_spin_limit(gm_batch* batch, uint64_t polls);
+/* fault injection for tests: colours > 0 of `mesh` wait for a count that
+ * never arrives, so the pass must end with GM_ERR_TIMEOUT */
+gm_status gm_batch_inject_stall(gm_batch* batch, uint32_t mesh);
+gm_status gm_batch_counters(gm_batch* batch, uint64_t* out5, int32_t reset);
+/* per mesh: milliseconds from the start of the last pass's persistent
+ * kernel to that mesh's last relocated vertex (-1: no vertex moved) */
+gm_status gm_batch_latencies(gm_batch* batch, double* out_ms_per_mesh);
+/* [meshes, queued vertices, segments, evaluation blocks] */
+gm_status gm_batch_info(gm_batch* batch, uint32_t* out4);
+
 /* No counterpart in the reference.  Quality evaluation that allocates
  * nothing, for callers that cannot call cudaMalloc (a host framework that
  * owns every device allocation, a fully committed memory budget, a loop

@@ -1,0 +1,119 @@
+"""The batched path: one persistent launch per pass over many meshes gives,
+mesh by mesh, exactly the positions of the plain one-launch-per-colour
+path (same per-vertex arithmetic, same colour order per mesh); per-mesh
+evaluation matches gm_evaluate; a captured CUDA graph replays the same pass;
+an injected dependency stall ends the pass with GM_ERR_TIMEOUT instead of a
+hang and leaves the context usable."""
+
+import numpy as np
+import pytest
+
+from gpumesh_gb300 import mesh as M
+from gpumesh_gb300 import meshgen, workloads
+
+from helpers import coloured, device_for
+
+pytestmark = pytest.mark.gpu
+
+MR = dict(sampler="uniform", measurer="metric_free", evaluator="mean_ratio")
+
+
+def meshes(count=12, seed=11, kind="tet"):
+    sizes = meshgen.batch_sizes(count, 3, 8, seed)
+    out = []
+    for i, n in enumerate(sizes):
+        raw, groups = coloured(meshgen.box_mesh(int(n), kind, 0.3, seed * 100 + i))
+        out.append((raw, groups))
+    return out
+
+
+def devices(ms, crew=MR):
+    return [device_for(raw, groups, crew) for raw, groups in ms]
+
+
+@pytest.mark.parametrize("smoother,params", [("nelder_mead", workloads.NM_PARAMS), ("gradient_descent", None),
+                                             ("spawn_search", None), ("getme", [0.5])])
+def test_batch_pass_equals_plain_pass(smoother, params):
+    ms = meshes()
+    plain = devices(ms)
+    for d in plain:
+        d.smooth_pass(smoother, params)
+    batched = devices(ms)
+    b = M.Batch(batched)
+    b.smooth_pass(smoother, params)
+    b.sync()
+    assert b.status() == 0
+    for d0, d1 in zip(plain, batched):
+        assert np.array_equal(d0.fetch_positions(), d1.fetch_positions())
+
+
+def test_batch_hex_getme_equals_plain():
+    ms = meshes(6, 5, "hex")
+    plain = devices(ms)
+    for d in plain:
+        d.smooth_pass("getme", [0.5])
+    batched = devices(ms)
+    b = M.Batch(batched)
+    b.smooth_pass("getme", [0.5])
+    b.sync()
+    for d0, d1 in zip(plain, batched):
+        assert np.array_equal(d0.fetch_positions(), d1.fetch_positions())
+
+
+def test_batch_evaluation_matches_per_mesh():
+    ms = meshes(9)
+    ds = devices(ms)
+    b = M.Batch(ds)
+    b.evaluate(0)
+    got = b.read_quality(0)
+    for d, q in zip(ds, got):
+        ref = d.evaluate()
+        assert q.sampleCount() == ref.sampleCount()
+        assert q.minimumQuality() == ref.minimumQuality()
+        assert (q.buckets() == ref.buckets()).all()
+        assert abs(q.invQualitySum() - ref.invQualitySum()) <= 1e-6 * ref.invQualitySum()
+
+
+def test_captured_graph_replays_the_pass():
+    ms = meshes(8, 21)
+    direct = devices(ms)
+    b0 = M.Batch(direct)
+    b0.smooth_pass("nelder_mead", None)
+    b0.sync()
+    graphed = devices(ms)
+    b1 = M.Batch(graphed)
+    b1.capture("nelder_mead", None, eval_slot=0)
+    b1.replay()
+    b1.sync()
+    for d0, d1 in zip(direct, graphed):
+        assert np.array_equal(d0.fetch_positions(), d1.fetch_positions())
+    q = b1.read_quality(0)
+    assert len(q) == len(ms) and all(h.sampleCount() > 0 for h in q)
+
+
+def test_autotuner_picks_a_shape_and_keeps_results():
+    ms = meshes(10, 31)
+    ds = devices(ms)
+    b = M.Batch(ds)
+    w, c, t = b.tune("nelder_mead", None)
+    assert w in (1, 2, 4, 8) and c >= 0 and t > 0
+    ref = devices(ms)
+    for d in ref:
+        d.smooth_pass("nelder_mead", None)
+    b.smooth_pass("nelder_mead", None)
+    b.sync()
+    for d0, d1 in zip(ref, ds):
+        assert np.array_equal(d0.fetch_positions(), d1.fetch_positions())
+
+
+def test_injected_stall_times_out_and_context_survives():
+    ms = meshes(6, 41)
+    ds = devices(ms)
+    b = M.Batch(ds)
+    b.set_spin_limit(20000)  # ~2 ms of polling
+    b.inject_stall(2)
+    b.smooth_pass("nelder_mead", None)
+    assert b.status() == 5  # GM_ERR_TIMEOUT
+    # the device is still usable
+    h = ds[0].evaluate()
+    assert h.sampleCount() > 0
