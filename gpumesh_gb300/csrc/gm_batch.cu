@@ -25,7 +25,7 @@
 
 namespace gm {
 
-constexpr uint32_t kClaimChunk = 4;
+constexpr uint32_t kClaimChunk = 8;
 
 __device__ __forceinline__ uint32_t find_segment(const uint32_t* seg_start, uint32_t nseg, uint32_t i)
 {
@@ -116,7 +116,7 @@ __device__ __forceinline__ void batch_one(const BatchMesh& bm, const SmoothParam
 }
 
 template <int SMOOTHER, int VAR, int MAXK>
-__global__ void __launch_bounds__(256) batch_relocate_kernel(BatchArgs a, SmoothParams sp)
+__global__ void __launch_bounds__(256, MAXK == 4 ? 3 : 1) batch_relocate_kernel(BatchArgs a, SmoothParams sp)
 {
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -134,9 +134,16 @@ __global__ void __launch_bounds__(256) batch_relocate_kernel(BatchArgs a, Smooth
         first = __shfl_sync(0xffffffffu, first, 0);
         if (first >= a.total) break;
         const uint32_t last = min(first + kClaimChunk, a.total);
+        // one search per chunk; later items of the chunk walk forward
+        uint32_t s = find_segment(a.seg_start, a.nseg, first);
+        uint32_t s_end = __ldg(&a.seg_start[s + 1]);
         for (uint32_t i = first; i < last; ++i)
         {
-            const uint32_t s = find_segment(a.seg_start, a.nseg, i);
+            while (i >= s_end)
+            {
+                ++s;
+                s_end = __ldg(&a.seg_start[s + 1]);
+            }
             const Segment sg = a.segs[s];
             int ok = 1;
             if (sg.need)

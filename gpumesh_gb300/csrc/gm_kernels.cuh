@@ -162,10 +162,16 @@ __device__ __forceinline__ R shfl_xor(R v, int o)
     return __shfl_xor_sync(0xffffffffu, v, o);
 }
 
-// reduce within aligned segments of S lanes (S a power of two)
+// reduce within aligned segments of S lanes (S a power of two); when no
+// lane saw a non-positive element (the common case) only the 1/q sums move
 template <class R>
 __device__ __forceinline__ void acc_reduce(PatchAcc<R>& a, int S)
 {
+    if (!__any_sync(0xffffffffu, a.nbad))
+    {
+        for (int o = S >> 1; o > 0; o >>= 1) a.rsum += shfl_xor(a.rsum, o);
+        return;
+    }
     for (int o = S >> 1; o > 0; o >>= 1)
     {
         a.rsum += shfl_xor(a.rsum, o);
