@@ -81,6 +81,8 @@ def lib():
         "gm_getme_update_group": [vp, vp, u32, u32],
         "gm_mesh_counters": [vp, vp, i32],
         "gm_mesh_save_positions": [vp],
+        "gm_mesh_clone": [vp, vp],
+        "gm_mesh_device_bytes": [vp, ctypes.POINTER(u64)],
         "gm_mesh_restore_positions": [vp],
         "gm_probe_fp32_tflops": [ctypes.POINTER(ctypes.c_double)],
         "gm_batch_create": [ctypes.POINTER(vp), vp, u32],

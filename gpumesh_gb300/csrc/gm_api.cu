@@ -508,6 +508,60 @@ gm_status gm_mesh_set_crew(gm_mesh* m, int32_t sampler, int32_t measurer, int32_
     });
 }
 
+gm_status gm_mesh_clone(gm_mesh* dst, const gm_mesh* src)
+{
+    return guarded([&] {
+        require(dst && src && dst != src, "invalid argument");
+        require(src->nv > 0 && src->cid.p, "source mesh has no topology");
+        cudaStream_t s = dst->stream;
+        GM_CUDA(cudaStreamSynchronize(src->stream));
+        auto copy = [&](auto& d, const auto& from, size_t n) {
+            d.reserve(n);
+            if (n) GM_CUDA(cudaMemcpyAsync(d.p, from.p, n * sizeof(*from.p), cudaMemcpyDeviceToDevice, s));
+        };
+        copy(dst->pos, src->pos, src->nv);
+        copy(dst->tets, src->tets, src->nt);
+        copy(dst->pris, src->pris, (size_t)src->np * 6);
+        copy(dst->hexs, src->hexs, (size_t)src->nh * 2);
+        copy(dst->ve_off, src->ve_off, (size_t)src->nv + 1);
+        copy(dst->vv_off, src->vv_off, (size_t)src->nv + 1);
+        std::vector<uint32_t> last(2);
+        GM_CUDA(cudaMemcpy(&last[0], src->ve_off.p + src->nv, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        GM_CUDA(cudaMemcpy(&last[1], src->vv_off.p + src->nv, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        copy(dst->ve, src->ve, last[0]);
+        copy(dst->vv, src->vv, last[1]);
+        copy(dst->cid, src->cid, src->nv);
+        copy(dst->con, src->con, (size_t)src->ncon);
+        copy(dst->members, src->members, src->n_members);
+        dst->nv = src->nv;
+        dst->nt = src->nt;
+        dst->np = src->np;
+        dst->nh = src->nh;
+        dst->ncon = src->ncon;
+        dst->n_members = src->n_members;
+        dst->group_base = src->group_base;
+        dst->crew = src->crew;
+        dst->ks = src->ks;
+        dst->maxe = src->maxe;
+        dst->warps_per_block = src->warps_per_block;
+        GM_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+gm_status gm_mesh_device_bytes(const gm_mesh* m, uint64_t* bytes)
+{
+    return guarded([&] {
+        require(m && bytes, "null argument");
+        uint64_t b = 0;
+        b += m->pos.cap * sizeof(float4) + m->tets.cap * sizeof(uint4) + m->pris.cap * 4 + m->hexs.cap * sizeof(uint4);
+        b += (m->ve_off.cap + m->ve.cap + m->vv_off.cap + m->vv.cap + m->members.cap) * 4 + m->cid.cap * 4;
+        b += m->con.cap * sizeof(Constraint) + m->parts.cap * sizeof(EvalPartial) + m->corners.cap * sizeof(float4);
+        b += m->saved.cap * sizeof(float4) + m->def_v.cap * 4 + (m->def_old.cap + m->def_new.cap) * sizeof(float4);
+        b += m->quality.cap * sizeof(Quality);
+        *bytes = b;
+    });
+}
+
 gm_status gm_mesh_save_positions(gm_mesh* m)
 {
     return guarded([&] {

@@ -232,11 +232,18 @@ def permute_mesh(raw: RawMesh, perm: np.ndarray) -> RawMesh:
 class DeviceMesh:
     """A gm_mesh handle: the mesh resident in HBM."""
 
-    def __init__(self, raw: RawMesh, groups: NodeGroups | None = None, stream: int | None = None):
+    def __init__(self, raw: RawMesh | None, groups: NodeGroups | None = None, stream: int | None = None,
+                 clone_of: "DeviceMesh | None" = None):
         L = N.lib()
         h = ctypes.c_void_p()
         N.check(L.gm_mesh_create(ctypes.byref(h)))
         self.h = h
+        if clone_of is not None:
+            if stream is not None:
+                N.check(L.gm_mesh_set_stream(self.h, ctypes.c_void_p(stream)))
+            N.check(L.gm_mesh_clone(self.h, clone_of.h))
+            self.nv = clone_of.nv
+            return
         self.nv = raw.nv
         if stream is not None:
             N.check(L.gm_mesh_set_stream(self.h, ctypes.c_void_p(stream)))
@@ -292,6 +299,11 @@ class DeviceMesh:
 
     def sync(self):
         N.check(N.lib().gm_mesh_sync(self.h))
+
+    def device_bytes(self) -> int:
+        b = ctypes.c_uint64()
+        N.check(N.lib().gm_mesh_device_bytes(self.h, ctypes.byref(b)))
+        return int(b.value)
 
     def save_positions(self):
         N.check(N.lib().gm_mesh_save_positions(self.h))

@@ -181,15 +181,8 @@ def _mk(pos, tets, pris, hexs, cid, kind, par, name, h):
                    name=name, h=h)
 
 
-def box_mesh(n: int, kind: str = "tet", jitter: float = 0.3, seed: int = 0,
-             gaussian: bool = False) -> RawMesh:
-    """Structured n^3-cell mesh of [-1,1]^3 under BoxBoundary.
-
-    kind: "tet" (6 Kuhn tets per cell), "hex", "pri" (2 prisms per cell) or
-    "mixed" (z-slabs: first third tets, second third prisms, rest hexes).
-    Interior vertices move by U(+-jitter*h) per axis, or by N(0, jitter*h)
-    when gaussian is true; boundary vertices stay on the box.
-    """
+def box_positions(n: int, jitter: float = 0.3, seed: int = 0, gaussian: bool = False) -> np.ndarray:
+    """Vertex positions of box_mesh(n, ..., jitter, seed, gaussian) (input order)."""
     h = 2.0 / n
     pos = _grid_positions(n)
     cid = _box_ids(n)
@@ -201,6 +194,21 @@ def box_mesh(n: int, kind: str = "tet", jitter: float = 0.3, seed: int = 0,
         else:
             d = (np.stack([uniform(seed, a, nv) for a in range(3)], axis=1) * 2.0 - 1.0) * (jitter * h)
         pos[interior] += d[interior]
+    return pos
+
+
+def box_mesh(n: int, kind: str = "tet", jitter: float = 0.3, seed: int = 0,
+             gaussian: bool = False) -> RawMesh:
+    """Structured n^3-cell mesh of [-1,1]^3 under BoxBoundary.
+
+    kind: "tet" (6 Kuhn tets per cell), "hex", "pri" (2 prisms per cell) or
+    "mixed" (z-slabs: first third tets, second third prisms, rest hexes).
+    Interior vertices move by U(+-jitter*h) per axis, or by N(0, jitter*h)
+    when gaussian is true; boundary vertices stay on the box.
+    """
+    h = 2.0 / n
+    pos = box_positions(n, jitter, seed, gaussian)
+    cid = _box_ids(n)
     cells = _cell_corners(n)
     tets = pris = hexs = None
     if kind == "tet":
@@ -221,11 +229,9 @@ def box_mesh(n: int, kind: str = "tet", jitter: float = 0.3, seed: int = 0,
     return _mk(pos, tets, pris, hexs, cid, ck, cp, f"box-{kind}-{n}", h)
 
 
-def sphere_mesh(n: int = 80, jitter: float = 0.25, seed: int = 1) -> RawMesh:
-    """The n^3-cell grid of [-1,1]^3 clipped to the unit ball (cells whose
-    centroid lies inside), split into Kuhn tets.  Vertices on the boundary of
-    the kept cell set carry the sphere face constraint and are projected onto
-    the sphere; interior vertices move by U(+-jitter*h) per axis."""
+def _sphere_layout(n: int):
+    """Kept cells, kept vertex ids (grid numbering) and boundary mask of the
+    n^3 grid clipped to the unit ball."""
     h = 2.0 / n
     r = np.arange(n)
     z, y, x = np.meshgrid(r, r, r, indexing="ij")
@@ -244,17 +250,37 @@ def sphere_mesh(n: int = 80, jitter: float = 0.25, seed: int = 1) -> RawMesh:
                 allk &= kept[vz + dz, vy + dy, vx + dx]
     used = np.zeros(W ** 3, dtype=bool)
     used[cells.ravel()] = True
-    remap = -np.ones(W ** 3, dtype=np.int64)
     ids = np.nonzero(used)[0]
-    remap[ids] = np.arange(ids.size)
-    pos = _grid_positions(n)[ids]
     boundary = ~allk.ravel()[ids]
-    cid = np.where(boundary, 1, 0).astype(np.int32)
+    return cells, ids, boundary
+
+
+def sphere_positions(n: int, jitter: float = 0.25, seed: int = 1, layout=None) -> np.ndarray:
+    """Vertex positions of sphere_mesh(n, jitter, seed) (input order)."""
+    h = 2.0 / n
+    cells, ids, boundary = layout if layout is not None else _sphere_layout(n)
+    pos = _grid_positions(n)[ids]
     nv = ids.size
     d = (np.stack([uniform(seed, a, nv) for a in range(3)], axis=1) * 2.0 - 1.0) * (jitter * h)
     pos[~boundary] += d[~boundary]
     b = pos[boundary]
     pos[boundary] = b * (1.0 / np.sqrt(np.einsum("ij,ij->i", b, b)))[:, None]
+    return pos
+
+
+def sphere_mesh(n: int = 80, jitter: float = 0.25, seed: int = 1) -> RawMesh:
+    """The n^3-cell grid of [-1,1]^3 clipped to the unit ball (cells whose
+    centroid lies inside), split into Kuhn tets.  Vertices on the boundary of
+    the kept cell set carry the sphere face constraint and are projected onto
+    the sphere; interior vertices move by U(+-jitter*h) per axis."""
+    h = 2.0 / n
+    layout = _sphere_layout(n)
+    cells, ids, boundary = layout
+    W = n + 1
+    remap = -np.ones(W ** 3, dtype=np.int64)
+    remap[ids] = np.arange(ids.size)
+    pos = sphere_positions(n, jitter, seed, layout)
+    cid = np.where(boundary, 1, 0).astype(np.int32)
     tets = remap[cells][:, KUHN].reshape(-1, 4)
     ck, cp = sphere_constraints()
     return _mk(pos, tets, None, None, cid, ck, cp, f"sphere-{n}", h)

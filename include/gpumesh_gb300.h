@@ -169,6 +169,13 @@ gm_status gm_mesh_set_constraints(gm_mesh* mesh, uint32_t n, const int32_t* kind
 gm_status gm_mesh_set_crew(gm_mesh* mesh, int32_t sampler, int32_t measurer, int32_t evaluator, double scaling,
                            double aspect_ratio);
 
+/* Copy a resident mesh (topology, groups, constraints, crew, positions)
+ * device to device into `dst`: a new job on an existing topology needs only
+ * its own positions uploaded afterwards.  Synchronous. */
+gm_status gm_mesh_clone(gm_mesh* dst, const gm_mesh* src);
+/* device bytes currently held by the mesh (for admission budgets) */
+gm_status gm_mesh_device_bytes(const gm_mesh* mesh, uint64_t* bytes);
+
 /* Keep a device copy of the current positions / restore it (no host
  * traffic); used to replay a smoothing schedule from the same input. */
 gm_status gm_mesh_save_positions(gm_mesh* mesh);

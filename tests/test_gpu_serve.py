@@ -1,0 +1,45 @@
+"""The served loop on the GPU: every job's result is the same alone and in
+the mix (exactly: per-vertex arithmetic and per-mesh evaluation do not
+depend on what else shares the launch), and admission respects the HBM
+budget."""
+
+import numpy as np
+import pytest
+
+from gpumesh_gb300 import serve
+
+pytestmark = pytest.mark.gpu
+
+
+def small_stream():
+    return serve.poisson_stream(rate=400.0, seconds=0.06, seed=4, lo=300, hi=20000)
+
+
+def test_same_result_alone_and_in_the_mix():
+    stream = small_stream()
+    assert len(stream) >= 12
+    mix = serve.Server(keep_results=True).run(stream, realtime=False)
+    assert mix.peak_active > 3  # jobs really shared launches
+    picks = [j for j in stream if j.job_id % 4 == 0][:6]
+    assert {j.smoother for j in picks} >= {"nelder_mead", "gradient_descent"}
+    for spec in picks:
+        alone = serve.Server(keep_results=True).run([spec], realtime=False)
+        a, m = alone.results[spec.job_id], mix.results[spec.job_id]
+        assert a["passes"] == m["passes"]
+        assert np.array_equal(a["pos"], m["pos"])
+        assert a["min"] == m["min"] and a["mean"] == m["mean"]
+
+
+def test_admission_respects_the_budget():
+    stream = small_stream()[:8]
+    s = serve.Server(hbm_budget_bytes=1)  # room for one job at a time
+    stats = s.run(stream, realtime=False)
+    assert stats.peak_active == 1
+    assert stats.jobs == 8 and len(stats.latencies_s) == 8
+
+
+def test_stop_rule_and_pass_cap():
+    stream = small_stream()[:6]
+    stats = serve.Server(max_passes=3, keep_results=True).run(stream, realtime=False)
+    for r in stats.results.values():
+        assert 1 <= r["passes"] <= 3
