@@ -127,6 +127,7 @@ class Job:
     final_min: float = 0.0
     final_mean: float = 0.0
     relocations: int = 0
+    charged: int = 0  # bytes counted against the budget while the job is active
 
 
 @dataclasses.dataclass
@@ -197,12 +198,16 @@ class Server:
                     time.sleep(max(0.0, min(0.01, stream[i].arrival - now)))
                 continue
             # admission against the HBM budget
+            # (a job is charged its template's footprint on admission and the
+            # same amount is released when it retires, so the books balance
+            # even though its per-pass buffers grow once it runs)
             while pending:
                 need = self.template(pending[0]).bytes
                 if active and used + need > self.budget:
                     break
                 job = self._admit(pending.popleft(), time.perf_counter() - t0)
-                used += job.device.device_bytes()
+                job.charged = max(need, job.device.device_bytes())
+                used += job.charged
                 active.append(job)
             peak_active = max(peak_active, len(active))
             peak_bytes = max(peak_bytes, used)
@@ -239,7 +244,7 @@ class Server:
                 if self.keep_results:
                     results[j.spec.job_id] = {"pos": j.device.fetch_positions(), "passes": j.passes,
                                               "min": j.final_min, "mean": j.final_mean}
-                used -= j.device.device_bytes()
+                used -= j.charged
                 j.device.close()
             active = still
         wall = time.perf_counter() - t0
