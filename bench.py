@@ -40,7 +40,7 @@ UNIT = "relocations/s"
 
 # FP32 operations per element-quality evaluation (an add, multiply or
 # transcendental counts 1, an FMA counts 2), counted from the measures in
-# gpumesh_gb300/csrc/gm_device.cuh; see DESIGN.md "Relocation roofline".
+# gpumesh_gb300/csrc/gm_device.cuh by hand.
 FLOPS_PER_ELEM_EVAL = {
     ("mean_ratio", "tet"): 78,
     ("mean_ratio", "hex"): 369,
@@ -443,7 +443,7 @@ def profile_driver(args):
 
 def bench_batched(args, rank, world, local):
     """C4: 4,096 jittered tet cubes (cells per axis log-uniform in [4, 24],
-    jitter U(+-0.3h), seed 3), one Nelder-Mead pass (BASELINE parameters) plus
+    jitter U(+-0.3h), seed 3), one Nelder-Mead pass (workloads.NM_PARAMS) plus
     a per-mesh evaluation, as ONE captured CUDA graph (one persistent
     relocation launch, one evaluation launch) with an autotuned launch shape;
     against the plain path, one mesh per launch sequence."""

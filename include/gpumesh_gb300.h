@@ -158,7 +158,8 @@ gm_status gm_mesh_upload_groups(gm_mesh* mesh, uint32_t n_members, const uint32_
 /* Constraint table indexed by constraint id (id 0 = volume).  params: 6
  * doubles per id -- plane: point, normal; segment: a, b; point: position.
  * The reference's constraint objects (Boundaries/Constraints/) carry these
- * as private members; the drop-in shim recovers them. */
+ * as private members; the drop-in shim recovers them from the boundary's
+ * geometry (box faces / edges / corners, unit sphere). */
 gm_status gm_mesh_set_constraints(gm_mesh* mesh, uint32_t n, const int32_t* kind, const double* params);
 /* Sampler / measurer / evaluator plugins and their uniforms.  Replaces the
  * install* drivers (Evaluating/MeanRatio.cu:156, MetricConformity.cu:196,

@@ -81,7 +81,7 @@ def test_one_colour_metric_conformity_sphere():
 
 
 def test_c1_nelder_mead_pass_quality():
-    """C1 (BASELINE parameters): harmonic mean within 1e-4 of the FP64
+    """C1 (10^3-cell tet cube, NM 1 pass, workloads.NM_PARAMS): harmonic mean within 1e-4 of the FP64
     oracle.  The minimum is set by one element; with these parameters an FP32
     rounding two colours earlier sends one vertex of that element to another
     optimum (min 0.6146 vs 0.6223 -- the same 0.6146 that an FP32 build of the
