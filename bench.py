@@ -68,15 +68,25 @@ def parse():
 
 
 # ---------------------------------------------------------------------------
+# Replicas: the path has no exchange step, so N GPUs run N independent
+# replicas.  The only collectives are the timing barrier and the reductions
+# of the step time (max) and of the units processed (sum).
 def dist_init(n):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
+        import torch
         import torch.distributed as dist
 
-        dist.init_process_group("nccl" if n > 0 else "gloo")
+        backend = os.environ.get("GM_DIST_BACKEND") or ("nccl" if torch.cuda.is_available() else "gloo")
+        dist.init_process_group(backend)
     return rank, world, local
+
+
+def shard(items, rank, world):
+    """Round-robin share of independent units (meshes, jobs) for one rank."""
+    return list(items)[rank::world]
 
 
 def barrier(world):
@@ -86,15 +96,28 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(x, world):
+def _reduce(x, world, op):
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(x, world):
+    import torch.distributed as dist
+
+    return _reduce(x, world, dist.ReduceOp.MAX if world > 1 else None)
+
+
+def sum_over_ranks(x, world):
+    import torch.distributed as dist
+
+    return _reduce(x, world, dist.ReduceOp.SUM if world > 1 else None)
 
 
 class ClockSampler:
@@ -384,7 +407,7 @@ def bench_gpu(args, rank, world, local):
             e2e_times.append(t1 - t0)
     e2e_total = max_over_ranks(sum(e2e_times), world)
     e2e = {"value": reloc * args.steps * world / e2e_total, "unit": UNIT, "h2d_bytes_per_step": raw.nv * 16,
-           "d2h_bytes_per_step": raw.nv * 16 + n * 208}
+           "d2h_bytes_per_step": raw.nv * 16 + n * __import__("ctypes").sizeof(N.Quality)}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
@@ -454,10 +477,14 @@ def bench_batched(args, rank, world, local):
     from gpumesh_gb300 import meshgen, workloads
 
     count = args.batch_meshes
-    sizes = meshgen.batch_sizes(count, 4, 24, 3)
+    # weak scaling: `count` meshes per rank, dealt round-robin from one
+    # stream of count * world meshes (N = 1 is the 4096-mesh workload itself)
+    sizes = meshgen.batch_sizes(count * world, 4, 24, 3)
+    mine = shard(range(count * world), rank, world)
     t0 = time.perf_counter()
     devs, movable, tets = [], 0, 0
-    for i, n in enumerate(sizes):
+    for i in mine:
+        n = sizes[i]
         raw = meshgen.box_mesh(int(n), "tet", 0.3, 3 * 1000003 + i)
         perm, groups = M.node_groups_build(raw)
         raw = M.permute_mesh(raw, perm)
@@ -485,6 +512,8 @@ def bench_batched(args, rank, world, local):
         batch.replay()
         batch.sync()
     times, lat = [], []
+    barrier(world)
+    torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
             restore()
@@ -495,10 +524,43 @@ def bench_batched(args, rank, world, local):
             b.synchronize()
             times.append(a.elapsed_time(b) * 1e-3)
             lat.append(batch.latencies_ms())
+    torch.cuda.synchronize()
+    barrier(world)
     assert batch.status() == 0
     qual = batch.read_quality(0)
-    t_batched = statistics.median(times)
+    t_batched = max_over_ranks(statistics.median(times), world)
+    units = sum_over_ranks(movable, world)
     lat = np.concatenate(lat)
+    # ---- e2e through the public API: every mesh's positions uploaded from
+    # pinned host memory, the captured pass, per-mesh histograms and
+    # positions read back ----
+    host_in = [torch.empty((d.nv, 4), dtype=torch.float32, pin_memory=True).numpy() for d in devs]
+    host_out = [torch.empty((d.nv, 4), dtype=torch.float32, pin_memory=True).numpy() for d in devs]
+    restore()
+    for d, h in zip(devs, host_in):
+        d.fetch_gpu_verts(h)
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for d, h in zip(devs, host_in):
+            d.upload_gpu_verts(h)
+        torch.cuda.synchronize()
+        batch.replay()
+        e2e_qual = batch.read_quality(0)
+        for d, h in zip(devs, host_out):
+            d.fetch_gpu_verts(h)
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_t = max_over_ranks(statistics.median(e2e_times), world)
+    nv_total = sum(d.nv for d in devs)
+    import ctypes
+
+    from gpumesh_gb300 import _native as N
+
+    e2e = {"value": units / e2e_t, "unit": UNIT, "h2d_bytes_per_step": nv_total * 16,
+           "d2h_bytes_per_step": nv_total * 16 + len(devs) * ctypes.sizeof(N.Quality)}
+    assert len(e2e_qual) == len(devs)
     # ---- plain: one mesh per launch sequence (every colour of that mesh, then its evaluation) ----
     restore()
     plain_times, plain_lat = [], []
@@ -515,9 +577,9 @@ def bench_batched(args, rank, world, local):
                 plain_lat.append((time.perf_counter() - ta) * 1e3)
         torch.cuda.synchronize()
         plain_times.append(time.perf_counter() - t1)
-    t_plain = statistics.median(plain_times[1:] if len(plain_times) > 1 else plain_times)
-    value = movable * world / t_batched
-    plain_value = movable * world / t_plain
+    t_plain = max_over_ranks(statistics.median(plain_times[1:] if len(plain_times) > 1 else plain_times), world)
+    value = units / t_batched
+    plain_value = units / t_plain
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_batched * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -532,8 +594,9 @@ def bench_batched(args, rank, world, local):
                            "note": "per mesh: persistent-kernel start to the mesh's last relocated vertex"},
             "quality": {"min_of_mins": min(q.minimumQuality() for q in qual),
                         "mean_of_means": float(np.mean([q.harmonicMean() for q in qual]))},
-            "gpu_launches": 2 * args.steps + 1 * args.steps, "clocks": clocks.summary()}
-    print(json.dumps(line), flush=True)
+            "e2e": e2e, "gpu_launches": 2 * args.steps + 1 * args.steps, "clocks": clocks.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def bench_served(args, rank, world, local):
@@ -549,14 +612,22 @@ def bench_served(args, rank, world, local):
     from gpumesh_gb300 import mesh as M
     from gpumesh_gb300 import serve
 
-    stream = serve.poisson_stream(args.serve_rate, args.serve_seconds, 4)
+    # weak scaling: one stream at world x the rate, jobs dealt round-robin,
+    # so every rank serves ~serve_rate jobs/s
+    stream = shard(serve.poisson_stream(args.serve_rate * world, args.serve_seconds, 4), rank, world)
     server = serve.Server(hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)))
     t0 = time.perf_counter()
     server.prepare(stream)
     setup_s = time.perf_counter() - t0
+    barrier(world)
+    torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         stats = server.run(stream, realtime=True)
+    torch.cuda.synchronize()
+    barrier(world)
     summ = stats.summary()
+    wall = max_over_ranks(summ["wall_s"], world)
+    served_units = sum_over_ranks(summ["relocations"], world)
     # plain path on a sample: each job alone, one launch per colour, evaluation after every pass
     sample = stream[:: max(1, len(stream) // 40)]
     reloc, t_plain, plain_lat = 0, 0.0, []
@@ -579,8 +650,8 @@ def bench_served(args, rank, world, local):
         t_plain += dt
         plain_lat.append(dt)
         d.close()
-    line = {"metric": METRIC, "value": summ["relocations_per_s"] * world, "unit": UNIT, "n_gpus": world,
-            "steps": 1, "warmup": 0, "ms_per_step": summ["wall_s"] * 1e3, "higher_is_better": True,
+    line = {"metric": METRIC, "value": served_units / wall, "unit": UNIT, "n_gpus": world,
+            "steps": 1, "warmup": 0, "ms_per_step": wall * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"C5 served: Poisson {args.serve_rate:g} jobs/s for {args.serve_seconds:g} s, "
                                    "1k-2M tets, NM/GD/GETMe, stop at min gain < 1e-3 or 20 passes",
@@ -592,8 +663,10 @@ def bench_served(args, rank, world, local):
                              "p99_job_s": float(np.percentile(plain_lat, 99)),
                              "note": "each job alone, no queueing: service time only"},
             "gpu_launches": None, "clocks": clocks.summary()}
-    line["served_vs_plain"] = line["value"] / max(line["plain_sample"]["relocations_per_s"], 1e-9)
-    print(json.dumps(line), flush=True)
+    # per GPU: this rank's served rate against the same GPU running its jobs one at a time
+    line["served_vs_plain"] = summ["relocations_per_s"] / max(line["plain_sample"]["relocations_per_s"], 1e-9)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def main():

@@ -629,7 +629,8 @@ gm_status gm_evaluate_async(gm_mesh* m, uint32_t slot)
         }
         uint32_t total = m->nt + m->np + m->nh;
         int nb = evaluate_blocks(total, m->sm_count);
-        m->parts.reserve(nb);
+        if (m->parts.reserve(nb))  // a fresh scratch starts with its ticket at 0
+            GM_CUDA(cudaMemsetAsync(m->parts.p, 0, sizeof(EvalPartial), m->stream));
         GM_CUDA(launch_evaluate(m->variant(), m->elem_set(), m->view(), m->crew, m->parts.p, nb, m->quality.p + slot,
                                 m->stream));
     });

@@ -76,7 +76,7 @@ __device__ __forceinline__ void batch_one(const BatchMesh& bm, const SmoothParam
         if (sw == 0.f) return;
         out = mk(sx / sw, sy / sw, sz / sw);
         if (cid != 0) out = snap(m, cid, out);
-        stage_patch(m, v, P, lane);
+        stage_patch_fp32<VAR, MAXK>(m, crew, v, to<float>(old), P, lane);
         if (lane == 0)
         {
             P.cand[0] = old;
@@ -91,8 +91,8 @@ __device__ __forceinline__ void batch_one(const BatchMesh& bm, const SmoothParam
     }
     else
     {
-        stage_patch(m, v, P, lane);
         const V3<float> pos = to<float>(old);
+        stage_patch_fp32<VAR, MAXK>(m, crew, v, pos, P, lane);
         evals = 2;
         q0 = patch_uniform<VAR, MAXK, float>(crew, P, pos, lane);
         if (SMOOTHER == kSmoothNM) out = nelder_mead<VAR, MAXK>(m, crew, sp, P, v, cid, pos, q0, lane, evals);
@@ -104,7 +104,13 @@ __device__ __forceinline__ void batch_one(const BatchMesh& bm, const SmoothParam
     const bool fp64 = !(q0 >= sp.accept_q && q1 >= sp.accept_q);
     if (fp64)
     {
-        // near-degenerate patch: the acceptance test in FP64
+        // near-degenerate patch: the acceptance test in FP64, on the corner
+        // positions (the FP32 search may have staged the canonical form)
+        if constexpr (TetCanon<VAR, MAXK>::on)
+        {
+            __syncwarp();
+            stage_patch(m, v, P, lane);
+        }
         const double d0 = patch_uniform<VAR, MAXK, double>(crew, P, to<double>(old), lane);
         const double d1 = patch_uniform<VAR, MAXK, double>(crew, P, mk<double>(out.x, out.y, out.z), lane);
         accept = !(d1 < d0);
@@ -251,8 +257,7 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchMesh* meshes
     const EvalBlock eb = blocks[blockIdx.x];
     const MeshView& m = meshes[eb.mesh].view;
     const Crew& crew = meshes[eb.mesh].crew;
-    float mn = 1.0f, rs = 0.f;
-    int nbad = 0;
+    EvalAcc acc;
     for (uint32_t i = eb.begin + threadIdx.x; i < eb.end; i += blockDim.x)
     {
         int type;
@@ -266,22 +271,11 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchMesh* meshes
         const int n = MAXK == 4 ? 4 : type_size(type);
 #pragma unroll
         for (int k = 0; k < MAXK; ++k) p[k] = to<float>(__ldg(&m.pos[vid[k < n ? k : 0]]));
-        EQ<float> q = elem_quality<VAR, MAXK, float>(crew, type, p);
-        float qv;
-        if (q.pos)
-        {
-            rs += q.v;
-            qv = __frcp_rn(q.v);
-        }
-        else
-        {
-            ++nbad;
-            qv = q.v;
-        }
-        mn = fminf(mn, qv);
-        atomicAdd(&hist[qv > 0.f ? min((int)(qv * 20.f), 19) : 0], 1);
+        acc.add(elem_quality<VAR, MAXK, float>(crew, type, p), hist);
     }
-    double ds = rs;
+    double ds = acc.rs;
+    float mn = acc.min_quality();
+    int nbad = acc.nbad;
     for (int o = 16; o > 0; o >>= 1)
     {
         ds += __shfl_xor_sync(0xffffffffu, ds, o);

@@ -102,10 +102,39 @@ template <> __device__ __forceinline__ double sqrt_<double>(double x) { return s
 template <class R> __device__ __forceinline__ V3<R> normalize(V3<R> a) { return a * rsqrt_<R>(dot(a, a)); }
 template <class R> __device__ __forceinline__ R length(V3<R> a) { return sqrt_<R>(dot(a, a)); }
 
-// |x|^(-2/3) for x != 0, and |x|^(2/3)
-__device__ __forceinline__ float pow_m23(float x) { return exp2f(-0.666666666666666667f * __log2f(fabsf(x))); }
+// Single-instruction FP32 approximations (PTX ISA: ex2 / lg2 / rcp / sqrt
+// .approx.ftz.f32, relative error of order 2^-22).  Subnormal inputs flush
+// to zero; no quantity of the quality measures is subnormal for meshes whose
+// edges are above 1e-12.
+__device__ __forceinline__ float ex2_fast(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float lg2_fast(float x)
+{
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rcp_fast(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sqrt_fast(float x)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// |x|^(-2/3) for x != 0, and |x|^(2/3): 2^(-+2/3 log2|x|)
+__device__ __forceinline__ float pow_m23(float x) { return ex2_fast(-0.666666666666666667f * lg2_fast(fabsf(x))); }
 __device__ __forceinline__ double pow_m23(double x) { return pow(fabs(x), -2.0 / 3.0); }
-__device__ __forceinline__ float pow_23(float x) { return exp2f(0.666666666666666667f * __log2f(fabsf(x))); }
+__device__ __forceinline__ float pow_23(float x) { return ex2_fast(0.666666666666666667f * lg2_fast(fabsf(x))); }
 __device__ __forceinline__ double pow_23(double x) { return pow(fabs(x), 2.0 / 3.0); }
 __device__ __forceinline__ float cbrt_(float x) { return cbrtf(x); }
 __device__ __forceinline__ double cbrt_(double x) { return cbrt(x); }
@@ -228,10 +257,15 @@ template <int VAR> struct VarTraits
     static constexpr bool diag_metric = VAR == kVarMCDiag;
 };
 
+// MetricFreeMeasurer::riemannianSegment = (b - a) * scaling.  The FP32 path
+// leaves the scaling out: every quantity built from metric-free segments
+// (mean ratio, volume ratios) is invariant to a common scale, so only the
+// FP64 path, which restates the reference operation for operation, applies it.
 template <int VAR, class R>
 __device__ __forceinline__ V3<R> segment(const Crew& c, V3<R> a, V3<R> b)
 {
     if (VarTraits<VAR>::metric_wise) return normalize(b - a) * metric_wise_distance(c, a, b);
+    if (sizeof(R) == sizeof(float)) return b - a;
     return (b - a) * (R)c.scaling;
 }
 

@@ -17,8 +17,7 @@ constexpr int kEvalThreads = 256;
 
 // SET: 4 = tets only, 8 = any element types, 9 = hexes only
 template <int VAR, int SET>
-__device__ __forceinline__ void eval_element(const MeshView& m, const Crew& crew, uint32_t i, float& mn, float& rs,
-                                             int& nbad, int* hist)
+__device__ __forceinline__ void eval_element(const MeshView& m, const Crew& crew, uint32_t i, EvalAcc& acc, int* hist)
 {
     constexpr int MAXK = SET == 4 ? 4 : 8;
     int type;
@@ -59,122 +58,115 @@ __device__ __forceinline__ void eval_element(const MeshView& m, const Crew& crew
     EQ<float> q = SET == 9 ? (VarTraits<VAR>::mean_ratio ? mr_hex<VAR, float>(crew, p)
                                                           : elem_quality<VAR, MAXK, float>(crew, kHex, p))
                            : elem_quality<VAR, MAXK, float>(crew, type, p);
-    float qv;
-    if (q.pos)
-    {
-        rs += q.v;
-        qv = __frcp_rn(q.v);
-    }
-    else
-    {
-        ++nbad;
-        qv = q.v;
-    }
-    mn = fminf(mn, qv);
-    int b = qv > 0.f ? min((int)(qv * 20.f), 19) : 0;
-    atomicAdd(&hist[b], 1);
+    acc.add(q, hist);
 }
 
-template <int VAR, int SET>
-__global__ void __launch_bounds__(kEvalThreads) evaluate_kernel(MeshView m, Crew crew, EvalPartial* parts)
+constexpr int kEvalWarps = kEvalThreads / 32;
+
+// Block-wide sum / min / sum over kEvalThreads threads in a fixed order;
+// thread 0 gets the results.
+__device__ __forceinline__ void block_reduce(double& sum, float& mn, int& bad, double* wsum, float* wmin, int* wbad)
 {
-    __shared__ int hist[20];
-    __shared__ float wmin[kEvalThreads / 32];
-    __shared__ double wsum[kEvalThreads / 32];
-    __shared__ int wbad[kEvalThreads / 32];
-    if (threadIdx.x < 20) hist[threadIdx.x] = 0;
-    __syncthreads();
-    float mn = 1.0f, rs = 0.f;
-    int nbad = 0;
-    const uint32_t total = m.nt + m.np + m.nh;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
-        eval_element<VAR, SET>(m, crew, i, mn, rs, nbad, hist);
-    double ds = rs;
     for (int o = 16; o > 0; o >>= 1)
     {
-        ds += __shfl_xor_sync(0xffffffffu, ds, o);
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
         mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        nbad += __shfl_xor_sync(0xffffffffu, nbad, o);
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
     }
     const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0)
     {
+        wsum[w] = sum;
         wmin[w] = mn;
-        wsum[w] = ds;
-        wbad[w] = nbad;
+        wbad[w] = bad;
     }
     __syncthreads();
-    if (threadIdx.x < 32)
-    {
-        EvalPartial* p = &parts[blockIdx.x];
-        if (threadIdx.x < 20) p->hist[threadIdx.x] = hist[threadIdx.x];
-        if (threadIdx.x == 0)
+    if (threadIdx.x == 0)
+        for (int k = 1; k < kEvalWarps; ++k)
         {
-            float bmin = wmin[0];
-            double bsum = wsum[0];
-            int bbad = wbad[0];
-            for (int k = 1; k < kEvalThreads / 32; ++k)
-            {
-                bmin = fminf(bmin, wmin[k]);
-                bsum += wsum[k];
-                bbad += wbad[k];
-            }
-            p->min = bmin;
-            p->rsum = bsum;
-            p->nbad = bbad;
-            p->pad = 0;
+            sum += wsum[k];
+            mn = fminf(mn, wmin[k]);
+            bad += wbad[k];
         }
-    }
 }
 
-__global__ void __launch_bounds__(256) evaluate_finalize_kernel(const EvalPartial* parts, int nparts, uint32_t count,
-                                                                 Quality* out)
+// One launch per evaluation: every block reduces its elements to a partial;
+// the last block to finish (a ticket taken after a release fence) reduces
+// all partials in a fixed order and writes the Quality, so the result does
+// not depend on which block finishes last.  atomicInc wraps the ticket back
+// to 0, so the scratch is ready for the next launch.
+template <int VAR, int SET>
+__global__ void __launch_bounds__(kEvalThreads) evaluate_kernel(MeshView m, Crew crew, EvalPartial* parts,
+                                                                Quality* out)
 {
-    __shared__ double s_sum[256];
-    __shared__ float s_min[256];
-    __shared__ unsigned long long s_bad[256];
-    __shared__ unsigned long long s_hist[8][20];
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    double sum = 0;
-    float mn = 1.0f;
-    unsigned long long bad = 0;
-    for (int i = t; i < nparts; i += 256)
-    {
-        sum += parts[i].rsum;
-        mn = fminf(mn, parts[i].min);
-        bad += (unsigned long long)parts[i].nbad;
-    }
-    s_sum[t] = sum;
-    s_min[t] = mn;
-    s_bad[t] = bad;
-    // histogram: warp w sums partials w, w + 8, ...; lane b < 20 owns bucket b
-    unsigned long long h = 0;
-    if (lane < 20)
-        for (int i = w; i < nparts; i += 8) h += (unsigned long long)parts[i].hist[lane];
-    if (lane < 20) s_hist[w][lane] = h;
+    __shared__ int hist[20];
+    __shared__ float wmin[kEvalWarps];
+    __shared__ double wsum[kEvalWarps];
+    __shared__ int wbad[kEvalWarps];
+    __shared__ unsigned int whist[kEvalWarps][20];
+    __shared__ bool last;
+    if (threadIdx.x < 20) hist[threadIdx.x] = 0;
     __syncthreads();
-    for (int s = 128; s > 0; s >>= 1)
+    EvalAcc acc;
+    const uint32_t total = m.nt + m.np + m.nh;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
+        eval_element<VAR, SET>(m, crew, i, acc, hist);
+    double sum = acc.rs;
+    float mn = acc.min_quality();
+    int bad = acc.nbad;
+    block_reduce(sum, mn, bad, wsum, wmin, wbad);
+    const int nb = gridDim.x;
+    const EvalScratch S = eval_scratch(parts, nb);
+    if (threadIdx.x < 20) S.hist[threadIdx.x * nb + blockIdx.x] = hist[threadIdx.x];
+    if (threadIdx.x == 0)
     {
-        if (t < s)
-        {
-            s_sum[t] += s_sum[t + s];
-            s_min[t] = fminf(s_min[t], s_min[t + s]);
-            s_bad[t] += s_bad[t + s];
-        }
-        __syncthreads();
+        S.rsum[blockIdx.x] = sum;
+        S.min[blockIdx.x] = mn;
+        S.nbad[blockIdx.x] = bad;
     }
-    if (t < 20)
+    __threadfence();  // every writer publishes its part of the partial
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicInc(S.ticket, (unsigned int)nb - 1u) == (unsigned int)nb - 1u;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // the last block: every partial, coalesced, in a fixed order
+    double tsum = 0;
+    float tmin = 1.0f;
+    int tbad = 0;
+    unsigned int h[20];
+#pragma unroll
+    for (int b = 0; b < 20; ++b) h[b] = 0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x)
+    {
+        tsum += __ldcg(&S.rsum[i]);
+        tmin = fminf(tmin, __ldcg(&S.min[i]));
+        tbad += __ldcg(&S.nbad[i]);
+#pragma unroll
+        for (int b = 0; b < 20; ++b) h[b] += (unsigned int)__ldcg(&S.hist[b * nb + i]);
+    }
+    __syncthreads();  // the shared reduction arrays are reused
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int b = 0; b < 20; ++b)
+    {
+        unsigned int x = h[b];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) whist[w][b] = x;
+    }
+    block_reduce(tsum, tmin, tbad, wsum, wmin, wbad);
+    if (threadIdx.x < 20)
     {
         unsigned long long hb = 0;
-        for (int k = 0; k < 8; ++k) hb += s_hist[k][t];
-        out->buckets[t] = hb;
+        for (int k = 0; k < kEvalWarps; ++k) hb += whist[k][threadIdx.x];
+        out->buckets[threadIdx.x] = hb;
     }
-    if (t == 0)
+    if (threadIdx.x == 0)
     {
-        out->min = (double)s_min[0];
-        out->nbad = s_bad[0];
-        out->inv_sum = s_bad[0] ? (double)INFINITY : s_sum[0];
-        out->count = count;
+        out->min = (double)tmin;
+        out->nbad = (unsigned long long)tbad;
+        out->inv_sum = tbad ? (double)INFINITY : tsum;
+        out->count = total;
     }
 }
 
@@ -187,9 +179,10 @@ int evaluate_blocks(uint32_t total, int sm_count)
 }
 
 template <int VAR, int SET>
-static void launch_eval_t(const MeshView& m, const Crew& crew, EvalPartial* parts, int nblocks, cudaStream_t s)
+static void launch_eval_t(const MeshView& m, const Crew& crew, EvalPartial* parts, int nblocks, Quality* out,
+                          cudaStream_t s)
 {
-    evaluate_kernel<VAR, SET><<<nblocks, kEvalThreads, 0, s>>>(m, crew, parts);
+    evaluate_kernel<VAR, SET><<<nblocks, kEvalThreads, 0, s>>>(m, crew, parts, out);
 }
 
 cudaError_t launch_evaluate(int variant, int maxk, const MeshView& m, const Crew& crew, EvalPartial* parts,
@@ -198,21 +191,20 @@ cudaError_t launch_evaluate(int variant, int maxk, const MeshView& m, const Crew
     switch (variant)
     {
     case kVarMRFree:
-        if (maxk == 4) launch_eval_t<kVarMRFree, 4>(m, crew, parts, nblocks, s);
-        else if (maxk == 9) launch_eval_t<kVarMRFree, 9>(m, crew, parts, nblocks, s);
-        else launch_eval_t<kVarMRFree, 8>(m, crew, parts, nblocks, s);
+        if (maxk == 4) launch_eval_t<kVarMRFree, 4>(m, crew, parts, nblocks, out, s);
+        else if (maxk == 9) launch_eval_t<kVarMRFree, 9>(m, crew, parts, nblocks, out, s);
+        else launch_eval_t<kVarMRFree, 8>(m, crew, parts, nblocks, out, s);
         break;
     case kVarMCDiag:
-        if (maxk == 4) launch_eval_t<kVarMCDiag, 4>(m, crew, parts, nblocks, s);
-        else launch_eval_t<kVarMCDiag, 8>(m, crew, parts, nblocks, s);
+        if (maxk == 4) launch_eval_t<kVarMCDiag, 4>(m, crew, parts, nblocks, out, s);
+        else launch_eval_t<kVarMCDiag, 8>(m, crew, parts, nblocks, out, s);
         break;
-    case kVarMRWise: launch_eval_t<kVarMRWise, 8>(m, crew, parts, nblocks, s); break;
+    case kVarMRWise: launch_eval_t<kVarMRWise, 8>(m, crew, parts, nblocks, out, s); break;
     default:
-        if (maxk == 4) launch_eval_t<kVarMC, 4>(m, crew, parts, nblocks, s);
-        else launch_eval_t<kVarMC, 8>(m, crew, parts, nblocks, s);
+        if (maxk == 4) launch_eval_t<kVarMC, 4>(m, crew, parts, nblocks, out, s);
+        else launch_eval_t<kVarMC, 8>(m, crew, parts, nblocks, out, s);
         break;
     }
-    evaluate_finalize_kernel<<<1, 256, 0, s>>>(parts, nblocks, m.nt + m.np + m.nh, out);
     return cudaGetLastError();
 }
 
@@ -236,10 +228,10 @@ cudaError_t launch_ffma_probe(int blocks, int threads, int iters, float* sink, c
     return cudaGetLastError();
 }
 
-size_t patch_smem_per_warp(int ks, int maxe)
+size_t patch_smem_per_warp(int maxk, int maxe)
 {
-    return (size_t)ks * maxe * sizeof(float4) + (size_t)maxe * sizeof(int) + kMaxCand * sizeof(float4) +
-           kMaxCand * sizeof(float);
+    return (size_t)patch_slots(maxk) * maxe * sizeof(float4) + (size_t)maxe * sizeof(int) +
+           kMaxCand * sizeof(float4) + kMaxCand * sizeof(float);
 }
 
 }  // namespace gm

@@ -105,8 +105,8 @@ __global__ void __launch_bounds__(128) getme_update_kernel(MeshView m, Crew crew
     if (!getme_average(m, corners, v, lane, prim)) return;
     const int cid = m.cid[v];
     if (cid != 0) prim = snap(m, cid, prim);
-    stage_patch(m, v, P, lane);
     const float4 old = m.pos[v];
+    stage_patch_fp32<VAR, MAXK>(m, crew, v, to<float>(old), P, lane);
     if (lane == 0)
     {
         P.cand[0] = old;

@@ -67,15 +67,17 @@ struct DBuf
 {
     T* p = nullptr;
     size_t cap = 0;
-    void reserve(size_t n)
+    // true when the buffer was (re)allocated
+    bool reserve(size_t n)
     {
-        if (n <= cap && p) return;
+        if (n <= cap && p) return false;
         if (p) cudaFree(p);
         p = nullptr;
         cap = 0;
         size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
         GM_CUDA(cudaMalloc(&p, bytes));
         cap = std::max<size_t>(n, 1);
+        return true;
     }
     void release()
     {

@@ -29,6 +29,70 @@ struct EvalPartial
     int pad;
 };
 
+// Scratch of one evaluation launch of nb blocks, carved from nb EvalPartial
+// slots as structure-of-arrays so the last block reads every partial
+// coalesced: a ticket word (8 bytes), then rsum[nb], min[nb], nbad[nb] and
+// hist[20][nb] -- 8 + 96 nb bytes, within nb * sizeof(EvalPartial).
+struct EvalScratch
+{
+    unsigned int* ticket;
+    double* rsum;
+    float* min;
+    int* nbad;
+    int* hist;  // hist[b * nb + block]
+};
+static_assert(sizeof(EvalPartial) >= 104, "evaluation scratch layout");
+
+__host__ __device__ inline EvalScratch eval_scratch(EvalPartial* base, int nb)
+{
+    char* p = reinterpret_cast<char*>(base);
+    EvalScratch s;
+    s.ticket = reinterpret_cast<unsigned int*>(p);
+    p += 8;
+    s.rsum = reinterpret_cast<double*>(p);
+    p += 8 * (size_t)nb;
+    s.min = reinterpret_cast<float*>(p);
+    p += 4 * (size_t)nb;
+    s.nbad = reinterpret_cast<int*>(p);
+    p += 4 * (size_t)nb;
+    s.hist = reinterpret_cast<int*>(p);
+    return s;
+}
+
+// Per-thread accumulation of evaluated elements (QualityHistogram::add,
+// DataStructures/QualityHistogram.cpp:63-76).  The minimum over valid
+// elements is the reciprocal of the maximum 1/q (a correctly rounded
+// reciprocal is monotonic, so this equals the minimum of the elements'
+// rounded qualities) and costs one division per thread, not per element;
+// the bucket of a valid element uses a one-instruction reciprocal.  The
+// minimum starts at 1, as the reference histogram's does; a non-positive
+// quality goes to bucket 0.
+struct EvalAcc
+{
+    float rs = 0.f;
+    float rmax = 0.f;
+    float bmin = 1.0f;
+    int nbad = 0;
+    __device__ __forceinline__ void add(const EQ<float>& q, int* hist)
+    {
+        float qv;
+        if (q.pos)
+        {
+            rs += q.v;
+            rmax = fmaxf(rmax, q.v);
+            qv = rcp_fast(q.v);
+        }
+        else
+        {
+            ++nbad;
+            bmin = fminf(bmin, q.v);
+            qv = q.v;
+        }
+        atomicAdd(&hist[qv > 0.f ? min((int)(qv * 20.f), 19) : 0], 1);
+    }
+    __device__ __forceinline__ float min_quality() const { return nbad ? bmin : fminf(1.0f, __frcp_rn(rmax)); }
+};
+
 // relocation parameters (the reference's file-scope constants, now runtime)
 struct SmoothParams
 {
@@ -64,29 +128,34 @@ struct Counters
 
 // ---------------------------------------------------------------------------
 // warp-level patch: the incident elements of one vertex staged in shared
-// memory as [slot][element] float4 (conflict-free: lane e reads element e)
+// memory as [slot][element] float4 (conflict-free: lane e reads element e).
+// Mixed patches stage the corner positions (8 slots); tet patches stage
+// either the 4 corner positions or the 5-slot canonical form below.
 // ---------------------------------------------------------------------------
+__host__ __device__ constexpr int patch_slots(int maxk) { return maxk == 4 ? 5 : maxk; }
 struct WarpPatch
 {
-    float4* sp;    // ks * maxe
+    float4* sp;    // patch_slots(maxk) * maxe
     int* meta;     // maxe: type | local << 2
     float4* cand;  // kMaxCand candidate positions
     float* res;    // kMaxCand patch qualities
     int maxe;
     int E;
+    V3<float> o;   // canonical tet staging: the origin (the vertex at staging)
 };
 
-__device__ __forceinline__ size_t warp_patch_bytes(int ks, int maxe)
+// maxk: corners of the largest element type (4 tets only, 8 otherwise)
+__device__ __forceinline__ size_t warp_patch_bytes(int maxk, int maxe)
 {
-    return (size_t)ks * maxe * sizeof(float4) + (size_t)maxe * sizeof(int) + kMaxCand * sizeof(float4) +
-           kMaxCand * sizeof(float);
+    return (size_t)patch_slots(maxk) * maxe * sizeof(float4) + (size_t)maxe * sizeof(int) +
+           kMaxCand * sizeof(float4) + kMaxCand * sizeof(float);
 }
 
-__device__ __forceinline__ WarpPatch carve_patch(char* base, int ks, int maxe)
+__device__ __forceinline__ WarpPatch carve_patch(char* base, int maxk, int maxe)
 {
     WarpPatch p;
     p.sp = reinterpret_cast<float4*>(base);
-    base += (size_t)ks * maxe * sizeof(float4);
+    base += (size_t)patch_slots(maxk) * maxe * sizeof(float4);
     p.cand = reinterpret_cast<float4*>(base);
     base += kMaxCand * sizeof(float4);
     p.res = reinterpret_cast<float*>(base);
@@ -94,6 +163,7 @@ __device__ __forceinline__ WarpPatch carve_patch(char* base, int ks, int maxe)
     p.meta = reinterpret_cast<int*>(base);
     p.maxe = maxe;
     p.E = 0;
+    p.o = V3<float>{0.f, 0.f, 0.f};
     return p;
 }
 
@@ -114,6 +184,217 @@ __device__ __forceinline__ void stage_patch(const MeshView& m, uint32_t v, WarpP
         P.meta[i] = type | (loc << 2);
     }
     __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// Canonical tet patches.  With the metric-free mean ratio, or metric
+// conformity under a diagonal metric, on tets only, the FP32 searches stage
+// each patch in a form where one more candidate position costs a few fused
+// operations per element:
+//  * each tet's corners are reordered by the even permutation
+//    new j = old (j xor (3 xor local)), which puts the moving vertex last;
+//    both measures are invariant under it (the regular-tet frame Fr_TET_INV
+//    is symmetric under the rotations of the element, and an even
+//    permutation keeps the orientation, i.e. the sign of det);
+//  * positions are relative to the moving vertex's position at staging, o,
+//    so the staged numbers are edge-sized;
+//  * the frame is applied to the fixed corners once: for a candidate with
+//    d = c - o, the corner-matrix columns [e03 e13 e23] Fr_TET_INV are
+//    kj d - Qj with k = (1, 1/sqrt 3, 1/sqrt 6) and Qj staged per element
+//    (slots 0-2, xyz);
+//  * under the sine-graded metric s^2 diag(1 + 9 sin^2(4 pi x), 1, 1) the
+//    Keast point k has x_k = X_k + w_k c.x with X_k fixed and w_k = 1/4
+//    (centroid), 1/6 (points weighting a fixed corner) or 1/2 (the point
+//    weighting the moving corner).  sin and cos of 4 pi X_k are staged
+//    (slots 0-2 w, 3, 4), so sin(4 pi x_k) follows by angle addition from the
+//    three per-candidate values sincospi(4 w c.x).
+// ---------------------------------------------------------------------------
+template <int VAR, int MAXK>
+struct TetCanon
+{
+    static constexpr bool on = MAXK == 4 && (VAR == kVarMRFree || VAR == kVarMCDiag);
+};
+
+// Fr_TET_INV (AbstractEvaluator.cpp:28-31) and the column sums k1, k2
+constexpr float kFrA = -0.5773502691896257645091f, kFrB = 1.154700538379251529018f;
+constexpr float kFrD = -0.4082482904638630163662f, kFrG = 1.224744871391589049099f;
+constexpr float kK1 = 0.5773502691896257645091f;  // kFrA + kFrB
+constexpr float kK2 = 0.4082482904638630163662f;  // 2 kFrD + kFrG
+// Keast 5-point rule (MetricConformityEvaluator.cpp:38-44)
+constexpr float kKeastH = 0.5f, kKeastQ = (1.0f - 0.5f) / 3.0f;
+
+__device__ __forceinline__ uint32_t tet_corner(uint4 t, int k)
+{
+    return k == 0 ? t.x : k == 1 ? t.y : k == 2 ? t.z : t.w;
+}
+
+__device__ __forceinline__ bool sine_metric(const Crew& c) { return c.sampler == kSamplerSine; }
+
+template <int VAR>
+__device__ __forceinline__ void stage_patch_canonical(const MeshView& m, const Crew& crew, uint32_t v, V3<float> o,
+                                                      WarpPatch& P, int lane)
+{
+    const uint32_t b = m.ve_off[v], e = m.ve_off[v + 1];
+    P.E = (int)(e - b);
+    P.o = o;
+    const bool sine = VAR == kVarMCDiag && sine_metric(crew);
+    for (int i = lane; i < P.E; i += kWarp)
+    {
+        const uint32_t r = m.ve[b + i];
+        const int x = 3 ^ ref_local(r);
+        const uint4 t = m.tets[ref_id(r)];
+        const float4 a0 = __ldcg(&m.pos[tet_corner(t, x)]);
+        const float4 a1 = __ldcg(&m.pos[tet_corner(t, 1 ^ x)]);
+        const float4 a2 = __ldcg(&m.pos[tet_corner(t, 2 ^ x)]);
+        const V3<float> r0 = to<float>(a0) - o, r1 = to<float>(a1) - o, r2 = to<float>(a2) - o;
+        const V3<float> q1 = r0 * kFrA + r1 * kFrB, q2 = (r0 + r1) * kFrD + r2 * kFrG;
+        float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, c[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        if (sine)
+        {
+            const float sum = a0.x + a1.x + a2.x;
+            const float X[5] = {sum * 0.25f, a0.x * kKeastH + (a1.x + a2.x) * kKeastQ,
+                                a1.x * kKeastH + (a0.x + a2.x) * kKeastQ, a2.x * kKeastH + (a0.x + a1.x) * kKeastQ,
+                                sum * kKeastQ};
+#pragma unroll
+            for (int k = 0; k < 5; ++k) sincospif(4.f * X[k], &s[k], &c[k]);
+        }
+        P.sp[0 * P.maxe + i] = make_float4(r0.x, r0.y, r0.z, s[0]);
+        P.sp[1 * P.maxe + i] = make_float4(q1.x, q1.y, q1.z, c[0]);
+        P.sp[2 * P.maxe + i] = make_float4(q2.x, q2.y, q2.z, s[1]);
+        P.sp[3 * P.maxe + i] = make_float4(c[1], s[2], c[2], s[3]);
+        P.sp[4 * P.maxe + i] = make_float4(c[3], s[4], c[4], 0.f);
+        P.meta[i] = kTet;
+    }
+    __syncwarp();
+}
+
+// per-candidate part of a canonical element evaluation
+struct TetCand
+{
+    V3<float> k0, k1, k2;
+    float sa, ca, sq, cq, sh, ch;  // sincospi(4 w c.x) for w = 1/4, 1/6, 1/2
+};
+
+// per-crew constants of the diagonal metric: the y and z entries of the
+// specified metric (constant for both diagonal samplers) and their inverses
+struct TetConst
+{
+    float s2, my, mz, iy, iz;
+};
+
+template <int VAR>
+__device__ __forceinline__ TetConst tet_const(const Crew& crew)
+{
+    TetConst k{};
+    if (VAR == kVarMCDiag)
+    {
+        // specified_metric_diag with metric_diag_at = {., s2, s2}, same operation order
+        const float s2 = (float)crew.scaling2;
+        k.s2 = s2;
+        k.my = s2 * -0.8f + (s2 + s2 + s2 + s2) * 0.45f;
+        k.mz = k.my;
+        k.iy = rcp_fast(k.my);
+        k.iz = k.iy;
+    }
+    return k;
+}
+
+template <int VAR>
+__device__ __forceinline__ TetCand tet_cand(const Crew& crew, V3<float> o, V3<float> c)
+{
+    TetCand t;
+    const V3<float> d = c - o;
+    t.k0 = d;
+    t.k1 = d * kK1;
+    t.k2 = d * kK2;
+    t.sa = t.ca = t.sq = t.cq = t.sh = t.ch = 0.f;
+    if (VAR == kVarMCDiag && sine_metric(crew))
+    {
+        sincospif(c.x, &t.sa, &t.ca);                  // 4 * (1/4) * c.x
+        sincospif(c.x * (2.0f / 3.0f), &t.sq, &t.cq);  // 4 * (1/6) * c.x
+        sincospif(c.x * 2.0f, &t.sh, &t.ch);           // 4 * (1/2) * c.x
+    }
+    return t;
+}
+
+// MetricConformityEvaluator::metricConformity with Ms = diag(m), from the
+// rows R_i of the corner matrix F: the cofactor rows C_i (C0 = R1 x R2, ...)
+// give det F = R0 . C0 and Mk = F^-T F^-1 = (C_i . C_j) / det^2, and
+// F F^T = (R_i . R_j); tNc_ij = (F F^T)_ij m_j + Mk_ij / m_i - 2 delta_ij.
+__device__ __forceinline__ void mc_corner_diag_fast(V3<float> c0, V3<float> c1, V3<float> c2, V3<float> m,
+                                                    const TetConst& k, float& rq, float& q, bool& pos)
+{
+    const V3<float> R0 = mk(c0.x, c1.x, c2.x), R1 = mk(c0.y, c1.y, c2.y), R2 = mk(c0.z, c1.z, c2.z);
+    const V3<float> C0 = cross(R1, R2), C1 = cross(R2, R0), C2 = cross(R0, R1);
+    const float det = dot(R0, C0);
+    const float Axx = dot(R0, R0), Ayy = dot(R1, R1), Azz = dot(R2, R2);
+    const float Axy = dot(R0, R1), Axz = dot(R0, R2), Ayz = dot(R1, R2);
+    const float Nxx = dot(C0, C0), Nyy = dot(C1, C1), Nzz = dot(C2, C2);
+    const float Nxy = dot(C0, C1), Nxz = dot(C0, C2), Nyz = dot(C1, C2);
+    const float id2 = rcp_fast(det * det);
+    const float wx = id2 * rcp_fast(m.x), wy = id2 * k.iy, wz = id2 * k.iz;
+    const float txx = Axx * m.x + Nxx * wx - 2.f, tyy = Ayy * m.y + Nyy * wy - 2.f, tzz = Azz * m.z + Nzz * wz - 2.f;
+    const float txy = Axy * m.y + Nxy * wx, tyx = Axy * m.x + Nxy * wy;
+    const float txz = Axz * m.z + Nxz * wx, tzx = Axz * m.x + Nxz * wz;
+    const float tyz = Ayz * m.z + Nyz * wy, tzy = Ayz * m.y + Nyz * wz;
+    const float f2 = txx * txx + tyy * tyy + tzz * tzz + txy * txy + tyx * tyx + txz * txz + tzx * tzx +
+                     tyz * tyz + tzy * tzy;
+    if (isnan(f2))
+    {
+        pos = false;
+        q = 0.f;
+        return;
+    }
+    const float sg = sgn(det);
+    pos = sg > 0.f;
+    const float r = sqrt_fast(1.f + sqrt_fast(f2));
+    if (pos) rq = r;
+    else q = sg * rcp_fast(r);
+}
+
+// quality of canonical element e for candidate t
+template <int VAR>
+__device__ __forceinline__ EQ<float> canonical_quality(const WarpPatch& P, int e, const TetCand& t, const TetConst& k,
+                                                       bool sine)
+{
+    const float4 A = P.sp[e], B = P.sp[P.maxe + e], C = P.sp[2 * P.maxe + e];
+    const V3<float> c0 = t.k0 - mk(A.x, A.y, A.z), c1 = t.k1 - mk(B.x, B.y, B.z), c2 = t.k2 - mk(C.x, C.y, C.z);
+    float rq = 0.f, q = 0.f;
+    bool pos;
+    if (VAR == kVarMRFree)
+        mr_corner(c0, c1, c2, rq, q, pos);
+    else
+    {
+        V3<float> m = mk(k.my, k.my, k.mz);
+        if (sine)
+        {
+            const float4 D = P.sp[3 * P.maxe + e], F = P.sp[4 * P.maxe + e];
+            // sin(4 pi x_k) at the 5 Keast points; staged S0 C0 S1 C1 S2 C2 S3 C3 S4 C4
+            const float s0 = A.w * t.ca + B.w * t.sa;
+            const float s1 = C.w * t.cq + D.x * t.sq;
+            const float s2 = D.y * t.cq + D.z * t.sq;
+            const float s3 = D.w * t.cq + F.x * t.sq;
+            const float s4 = F.y * t.ch + F.z * t.sh;
+            const float m0 = k.s2 * (1.f + 9.f * s0 * s0), m1 = k.s2 * (1.f + 9.f * s1 * s1);
+            const float m2 = k.s2 * (1.f + 9.f * s2 * s2), m3 = k.s2 * (1.f + 9.f * s3 * s3);
+            const float m4 = k.s2 * (1.f + 9.f * s4 * s4);
+            m.x = m0 * -0.8f + (m1 + m2 + m3 + m4) * 0.45f;
+        }
+        else
+            m.x = k.my;  // uniform: every entry is s2 (-0.8 + 4 * 0.45)
+        mc_corner_diag_fast(c0, c1, c2, m, k, rq, q, pos);
+    }
+    return EQ<float>{pos ? rq : q, pos};
+}
+
+// the staging the FP32 patch functions of this variant expect; o is the
+// moving vertex's current position
+template <int VAR, int MAXK>
+__device__ __forceinline__ void stage_patch_fp32(const MeshView& m, const Crew& crew, uint32_t v, V3<float> o,
+                                                 WarpPatch& P, int lane)
+{
+    if constexpr (TetCanon<VAR, MAXK>::on) stage_patch_canonical<VAR>(m, crew, v, o, P, lane);
+    else stage_patch(m, v, P, lane);
 }
 
 // quality of staged element e with its moving vertex at c
@@ -190,11 +471,23 @@ __device__ __forceinline__ R acc_final(const PatchAcc<R>& a, int E)
 }
 
 // patch quality with the vertex at c (same c on every lane), whole warp
+// (FP32 with a canonical variant: the patch must be staged canonically;
+// FP64 and every other variant: the corner positions)
 template <int VAR, int MAXK, class R>
 __device__ __forceinline__ R patch_uniform(const Crew& crew, const WarpPatch& P, V3<R> c, int lane)
 {
     PatchAcc<R> a{R(0), R(3.0e38), 0};
-    for (int e = lane; e < P.E; e += kWarp) acc_add(a, staged_quality<VAR, MAXK, R>(crew, P, e, c));
+    if constexpr (TetCanon<VAR, MAXK>::on && sizeof(R) == sizeof(float))
+    {
+        const TetConst k = tet_const<VAR>(crew);
+        const bool sine = VAR == kVarMCDiag && sine_metric(crew);
+        const TetCand t = tet_cand<VAR>(crew, P.o, c);
+        for (int e = lane; e < P.E; e += kWarp) acc_add(a, canonical_quality<VAR>(P, e, t, k, sine));
+    }
+    else
+    {
+        for (int e = lane; e < P.E; e += kWarp) acc_add(a, staged_quality<VAR, MAXK, R>(crew, P, e, c));
+    }
     acc_reduce(a, kWarp);
     return acc_final(a, P.E);
 }
@@ -207,6 +500,8 @@ __device__ __forceinline__ void patch_multi(const Crew& crew, WarpPatch& P, int 
     while (S > 1 && K * S > 32) S >>= 1;
     int G = 32 / S;
     int slot = lane / S, sub = lane & (S - 1);
+    const TetConst k = tet_const<VAR>(crew);
+    const bool sine = VAR == kVarMCDiag && sine_metric(crew);
     for (int r = 0; r < K; r += G)
     {
         int c = r + slot;
@@ -215,7 +510,15 @@ __device__ __forceinline__ void patch_multi(const Crew& crew, WarpPatch& P, int 
         {
             float4 cf = P.cand[c];
             V3<R> cp = to<R>(cf);
-            for (int e = sub; e < P.E; e += S) acc_add(a, staged_quality<VAR, MAXK, R>(crew, P, e, cp));
+            if constexpr (TetCanon<VAR, MAXK>::on && sizeof(R) == sizeof(float))
+            {
+                const TetCand t = tet_cand<VAR>(crew, P.o, cp);
+                for (int e = sub; e < P.E; e += S) acc_add(a, canonical_quality<VAR>(P, e, t, k, sine));
+            }
+            else
+            {
+                for (int e = sub; e < P.E; e += S) acc_add(a, staged_quality<VAR, MAXK, R>(crew, P, e, cp));
+            }
         }
         acc_reduce(a, S);
         if (c < K && sub == 0) P.res[c] = (float)acc_final(a, P.E);

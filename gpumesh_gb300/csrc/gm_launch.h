@@ -7,7 +7,8 @@
 
 namespace gm {
 
-size_t patch_smem_per_warp(int ks, int maxe);
+// shared memory of one warp's patch; maxk: 4 = tets only, 8 = any element type
+size_t patch_smem_per_warp(int maxk, int maxe);
 
 int evaluate_blocks(uint32_t total, int sm_count);
 // maxk: 4 = tets only, 8 = any element types, 9 = hexes only

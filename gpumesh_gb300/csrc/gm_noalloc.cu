@@ -10,11 +10,13 @@
 // file-scope device array below.
 //
 // That array is part of this library's image, so every GPU that loads the
-// library holds it (kNoAllocMaxPartials * sizeof(EvalPartial) = 112 KiB)
+// library holds it (kNoAllocMaxPartials * sizeof(EvalPartial) = 104 KiB)
 // until the process exits.  All calls on one device share it and it keeps
-// the last call's contents; each call overwrites every slot it reads, so no
-// clearing is needed, but two calls that overlap on the GPU (for instance on
-// two streams) race on it and must be serialised by the caller.
+// the last call's contents; each call overwrites every partial it reads, and
+// the evaluation kernel returns the array's ticket word (zero when the
+// library is loaded) to zero at the end of every launch, so no clearing is
+// needed, but two calls that overlap on the GPU (for instance on two
+// streams) race on it and must be serialised by the caller.
 #include <cuda_runtime.h>
 
 #include <cmath>

@@ -55,9 +55,9 @@ __global__ void __launch_bounds__(128) relocate_kernel(MeshView m, Crew crew, Sm
     WarpPatch P = carve_patch(smem + wib * warp_patch_bytes(MAXK, maxe), MAXK, maxe);
     const uint32_t v = members[w];
     const int cid = m.cid[v];
-    stage_patch(m, v, P, lane);
     const float4 old = m.pos[v];
     const V3<float> pos = to<float>(old);
+    stage_patch_fp32<VAR, MAXK>(m, crew, v, pos, P, lane);
     int evals = 1;
     const float q0 = patch_uniform<VAR, MAXK, float>(crew, P, pos, lane);
     V3<float> out;

@@ -276,7 +276,7 @@ gm_status gm_batch_info(gm_batch* batch, uint32_t* out4);
  * pos = nv float4 (x, y, z, unused; 16-byte aligned), tets / hexs = 4 / 8
  * uint32 per element (16-byte aligned), pris = 6 uint32 per element (8-byte
  * aligned); *out receives the gm_quality on the device, asynchronously on
- * `stream`.  The only scratch is a 112 KiB array inside this library that
+ * `stream`.  The only scratch is a 104 KiB array inside this library that
  * every GPU which loads the library holds until exit; meshes above
  * 16,777,216 elements are rejected with GM_ERR_UNSUPPORTED.  The first call
  * on a device looks up that array's device address, so make it before any

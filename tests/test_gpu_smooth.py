@@ -169,3 +169,32 @@ def test_fp64_acceptance_on_degenerate_patches():
     c = dev.counters()
     assert c["fp64_vertices"] > 0
     assert c["patch_evals"] > 0
+
+
+def test_host_mirror_api_matches_the_c_abi_path():
+    """The reference-named host API (Mesh.compileTopology, MeshCrew,
+    NelderMeadSmoother.smoothMesh, MeanRatioEvaluator.evaluateMesh) runs the
+    same kernels as the C ABI calls: identical final positions and
+    histograms, and one pass per scheduled relocation."""
+    from gpumesh_gb300 import mesh as M
+
+    raw = meshgen.box_mesh(6, "tet", 0.3, 11)
+    m = M.Mesh(raw)
+    m.compileTopology()
+    crew = M.MeshCrew()
+    crew.setSampler(m, M.UniformSampler())
+    crew.setEvaluator(m, M.MeanRatioEvaluator())
+    sm = M.NelderMeadSmoother()
+    sm.smoothMesh(m, crew, "CUDA", M.Schedule(relocationPassCount=3))
+    assert len(sm.passes) == 4
+    hist = M.QualityHistogram()
+    M.MeanRatioEvaluator().evaluateMesh(m, crew.sampler(), crew.measurer(), hist, "CUDA")
+
+    r2, g2 = coloured(raw)
+    dev = device_for(r2, g2, MR)
+    for _ in range(3):
+        dev.smooth_pass("nelder_mead")
+    assert np.array_equal(m.verts, dev.fetch_positions())
+    h2 = dev.evaluate()
+    assert hist.minimumQuality() == h2.minimumQuality() and hist.harmonicMean() == h2.harmonicMean()
+    assert hist.harmonicMean() > sm.passes[0].histogram.harmonicMean()
