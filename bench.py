@@ -38,14 +38,32 @@ sys.path.insert(0, ROOT)
 METRIC = "vertex relocations/s"
 UNIT = "relocations/s"
 
-# FP32 operations per element-quality evaluation (an add, multiply or
-# transcendental counts 1, an FMA counts 2), counted from the measures in
-# gpumesh_gb300/csrc/gm_device.cuh by hand.
+# FP32 operations per element-quality evaluation as the relocation kernels
+# execute it (an add, multiply, reciprocal, square root or exp2/log2 counts
+# 1, an FMA counts 2), counted by hand from gm_kernels.cuh / gm_device.cuh:
+#   mean ratio, canonical tet (canonical_quality): 9 column subtractions,
+#     det 14, |F|^2 17, power 3, 1/q 2, accumulate 1                     = 46
+#   metric conformity, canonical tet, sine-graded metric: 9 columns, 5
+#     Keast sines by angle addition 15, 5 metric values 20, quadrature 6,
+#     cofactors + det + F F^T + cofactor products 92, weights 6, tNc 30,
+#     |tNc|^2 17, two square roots + add 3, accumulate 1                    = 199
+#   the same under the uniform metric (no quadrature work)                 = 158
+#   mean ratio, hex (mr_hex): 12 edges 36, 8 corners x 36, combination 9  = 333
+# Per-candidate work (the frame columns, 3 sincospi) is shared by all the
+# elements of a patch and not counted.
 FLOPS_PER_ELEM_EVAL = {
-    ("mean_ratio", "tet"): 78,
-    ("mean_ratio", "hex"): 369,
-    ("metric_conformity", "tet"): 272,  # diagonal (uniform / sine-graded) metric
+    ("mean_ratio", "tet"): 46,
+    ("mean_ratio", "hex"): 333,
+    ("metric_conformity", "tet", "sine"): 199,
+    ("metric_conformity", "tet", "uniform"): 158,
 }
+
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
+# captures of the same kernels on the same workloads: one evaluation of the
+# 128^3 hex mesh, and the first spawn-search colour of the C2 sphere (61,699
+# vertices), scaled to a pass by vertices.
+EVAL_HEX128_TRAFFIC_BYTES = 101_564_928 + 3_570_432
+SPAWN_C2_TRAFFIC_PER_VERTEX = (39_982_848 + 16_128) / 61_699
 
 
 def parse():
@@ -207,8 +225,10 @@ def l2_flush(torch, buf, stream):
 
 
 def flops_per_elem(w, raw):
-    key = (w.evaluator, "tet" if raw.tets.shape[0] else "hex")
-    return FLOPS_PER_ELEM_EVAL.get(key)
+    etype = "tet" if raw.tets.shape[0] else "hex"
+    if w.evaluator == "metric_conformity":
+        return FLOPS_PER_ELEM_EVAL.get((w.evaluator, etype, w.sampler))
+    return FLOPS_PER_ELEM_EVAL.get((w.evaluator, etype))
 
 
 def eval_roofline(torch, stream, hbm_peak, steps=10):
@@ -239,7 +259,8 @@ def eval_roofline(torch, stream, hbm_peak, steps=10):
     h = dev.read_quality(0)
     dev.close()
     return {"bound": "hbm", "kernel": "evaluate_kernel (mean ratio, 128^3 hexes)", "achieved": round(achieved, 1),
-            "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": None,
+            "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+            "traffic": EVAL_HEX128_TRAFFIC_BYTES,
             "algorithmic_bytes": algo, "us_per_launch": round(t * 1e6, 2),
             "min": h.minimumQuality(), "mean": h.harmonicMean(), "note": "of measured"}
 
@@ -381,9 +402,13 @@ def bench_gpu(args, rank, world, local):
             dev.smooth_pass(smoother, params)
     dom_pass_s = statistics.median(per[dom])
     achieved = dc["elem_evals"] * fpe / dom_pass_s / 1e12 if fpe else None
+    traffic = None
+    if args.workload == "C2" and dom == "spawn_search":
+        traffic = int(SPAWN_C2_TRAFFIC_PER_VERTEX * reloc / w.passes())
     roofline = {"bound": "fp32", "kernel": f"relocate_kernel ({dom}, {w.evaluator})",
                 "achieved": round(achieved, 3) if achieved else None, "peak": round(fp32.value, 2),
-                "unit": "TFLOP/s", "frac": round(achieved / fp32.value, 4) if achieved else None, "traffic": None,
+                "unit": "TFLOP/s", "frac": round(achieved / fp32.value, 4) if achieved else None, "traffic": traffic,
+                "traffic_note": "DRAM bytes per pass (8 launches), ncu capture of one colour scaled by vertices",
                 "flops_per_element_eval": fpe, "element_evals_per_pass": dc["elem_evals"],
                 "ms_per_pass": round(dom_pass_s * 1e3, 3),
                 "note": "peak = FFMA probe measured in this run (no FP32 entry in MEASURED_PEAKS.json)"}

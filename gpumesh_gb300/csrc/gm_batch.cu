@@ -121,10 +121,191 @@ __device__ __forceinline__ void batch_one(const BatchMesh& bm, const SmoothParam
     count_work(ctr, evals, P.E, MAXK == 4 ? kTet : kHex, fp64, lane);
 }
 
+// Nelder-Mead on canonical tet patches in lockstep (gm_nm_lockstep.cuh):
+// the warp claims chunks of the queue and hands items to its idle groups in
+// queue order; a group whose mesh has not finished the item's earlier
+// colours waits without holding up the other groups (one poll per step,
+// bounded by spin_limit).  The FP64 acceptance test of a near-degenerate
+// patch runs warp-wide, one group at a time, on a corner-position copy of
+// that group's patch.  Deadlock freedom is the queue's: an item waits only
+// for items earlier in the queue, which were handed out before it.
+template <int VAR>
+__device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, char* wsm, int lane)
+{
+    const int gi = lane / kNMGroup, sub = lane & (kNMGroup - 1), leader = gi * kNMGroup;
+    WarpPatch P = nm_group_patch(wsm, gi, a.maxe);
+    NMGroup g;
+    g.phase = kNMIdle;
+    g.E = 0;
+    const BatchMesh* bm = a.meshes;  // the group's mesh (any valid entry while idle)
+    uint32_t mesh = 0, need = 0;
+    unsigned long long spins = 0;
+    TetConst kc = tet_const<VAR>(bm->crew);
+    bool sine = false;
+    uint32_t cur = 0, last = 0, seg = 0;  // the warp's chunk [cur, last) and the segment of cur
+    bool exhausted = false;
+    unsigned long long n_evals = 0, n_elems = 0, n_fp64 = 0;
+    while (true)
+    {
+        // (1) idle groups take the next items, in group order
+        const bool idle = g.phase == kNMIdle;
+        const unsigned ball = __ballot_sync(kFullMask, idle && sub == 0);
+        if (ball && cur >= last && !exhausted)
+        {
+            uint32_t first = 0;
+            if (lane == 0) first = atomicAdd(&a.ctl->next, kClaimChunk);
+            first = __shfl_sync(kFullMask, first, 0);
+            if (first >= a.total) exhausted = true;
+            else
+            {
+                cur = first;
+                last = min(first + kClaimChunk, a.total);
+                seg = find_segment(a.seg_start, a.nseg, first);
+            }
+        }
+        const uint32_t rank = __popc(ball & ((1u << leader) - 1u));
+        const uint32_t avail = cur < last ? last - cur : 0u;
+        if (idle && rank < avail)
+        {
+            const uint32_t item = cur + rank;
+            uint32_t s = seg;
+            while (item >= __ldg(&a.seg_start[s + 1])) ++s;
+            const Segment sg = a.segs[s];
+            bm = &a.meshes[sg.mesh];
+            mesh = sg.mesh;
+            need = sg.need;
+            spins = 0;
+            g.v = bm->members[sg.member_begin + (item - __ldg(&a.seg_start[s]))];
+            g.phase = kNMWait;
+        }
+        cur += min((uint32_t)__popc(ball), avail);
+        while (cur < last && cur >= __ldg(&a.seg_start[seg + 1])) ++seg;
+        if (!__any_sync(kFullMask, g.phase != kNMIdle))
+        {
+            if (exhausted) break;
+            continue;
+        }
+        // (2) a waiting group starts once its mesh's earlier colours are done
+        int ok = 0, give_up = 0;
+        if (g.phase == kNMWait && sub == 0)
+        {
+            if (need == 0 || __ldcv(&a.done[mesh]) >= need) ok = 1;
+            else if (++spins > a.spin_limit || __ldcv(&a.ctl->error))
+            {
+                atomicOr(&a.ctl->error, 1u);
+                give_up = 1;
+            }
+        }
+        ok = __shfl_sync(kFullMask, ok, leader);
+        give_up = __shfl_sync(kFullMask, give_up, leader);
+        if (ok)
+        {
+            __threadfence();
+            nm_begin<VAR>(g, bm->view, bm->crew, P, g.v, sub);
+            kc = tet_const<VAR>(bm->crew);
+            sine = VAR == kVarMCDiag && sine_metric(bm->crew);
+        }
+        __syncwarp();
+        if (__any_sync(kFullMask, ok)) nm_local_size(g, bm->view, sp, ok, sub);
+        // (3) one evaluation per busy group
+        const bool busy = g.phase >= kNMQ0;
+        if (!__any_sync(kFullMask, busy)) __nanosleep(100);
+        const float f = nm_group_quality<VAR>(bm->crew, P, busy ? g.E : 0, g.cand, kc, sine, sub);
+        bool finishing = false, need64 = false, accept = true;
+        if (busy)
+        {
+            ++g.evals;
+            if (g.phase != kNMFinal) nm_step(g, f, sp, bm->view);
+            else
+            {
+                finishing = true;
+                need64 = !(g.q0 >= sp.accept_q && f >= sp.accept_q);
+            }
+        }
+        // (4) near-degenerate patches: the acceptance test in FP64, warp-wide
+        unsigned m64;
+        while ((m64 = __ballot_sync(kFullMask, need64 && sub == 0)) != 0u)
+        {
+            const int src = __ffs(m64) - 1;
+            const BatchMesh* bx =
+                reinterpret_cast<const BatchMesh*>(__shfl_sync(kFullMask, reinterpret_cast<unsigned long long>(bm), src));
+            const uint32_t vx = __shfl_sync(kFullMask, g.v, src);
+            const double ox = __shfl_sync(kFullMask, g.old.x, src), oy = __shfl_sync(kFullMask, g.old.y, src);
+            const double oz = __shfl_sync(kFullMask, g.old.z, src);
+            const double nx = __shfl_sync(kFullMask, g.cand.x, src), ny = __shfl_sync(kFullMask, g.cand.y, src);
+            const double nz = __shfl_sync(kFullMask, g.cand.z, src);
+            WarpPatch X = nm_fp64_patch(wsm, a.maxe);
+            stage_patch(bx->view, vx, X, lane);
+            const double d0 = patch_uniform<VAR, 4, double>(bx->crew, X, mk(ox, oy, oz), lane);
+            const double d1 = patch_uniform<VAR, 4, double>(bx->crew, X, mk(nx, ny, nz), lane);
+            if (gi == src / kNMGroup)
+            {
+                accept = !(d1 < d0);
+                need64 = false;
+            }
+            __syncwarp();
+        }
+        // (5) finished vertices: commit, count the vertex done for its mesh
+        if (finishing || give_up)
+        {
+            if (sub == 0)
+            {
+                if (finishing)
+                {
+                    if (accept) bm->view.pos[g.v] = make_float4(g.cand.x, g.cand.y, g.cand.z, g.old.w);
+                    n_evals += (unsigned long long)g.evals;
+                    n_elems += (unsigned long long)g.evals * (unsigned long long)g.E;
+                    n_fp64 += (g.q0 >= sp.accept_q && f >= sp.accept_q) ? 0ull : 1ull;
+                }
+                __threadfence();
+                const unsigned int d = atomicAdd(&a.done[mesh], 1u) + 1u;
+                if (d == bm->nmembers)
+                {
+                    unsigned long long now;
+                    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+                    a.finish[mesh] = now;
+                }
+            }
+            g.phase = kNMIdle;
+        }
+    }
+    nm_flush_counters(a.ctr, n_evals, n_elems, n_fp64, lane);
+}
+
 template <int SMOOTHER, int VAR, int MAXK>
-__global__ void __launch_bounds__(256, MAXK == 4 ? 3 : 1) batch_relocate_kernel(BatchArgs a, SmoothParams sp)
+struct BatchLockstep
+{
+    static constexpr bool on = SMOOTHER == kSmoothNM && TetCanon<VAR, MAXK>::on;
+};
+
+template <int SMOOTHER, int VAR, int MAXK>
+__device__ __forceinline__ void batch_queue_loop(const BatchArgs& a, const SmoothParams& sp, char* smem);
+
+template <int SMOOTHER, int VAR, int MAXK>
+__global__ void __launch_bounds__(256, BatchLockstep<SMOOTHER, VAR, MAXK>::on ? 2 : (MAXK == 4 ? 3 : 1))
+    batch_relocate_kernel(BatchArgs a, SmoothParams sp)
 {
     extern __shared__ __align__(16) char smem[];
+    if constexpr (BatchLockstep<SMOOTHER, VAR, MAXK>::on)
+    {
+        const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+        if (threadIdx.x == 0)
+        {
+            unsigned long long now;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+            atomicCAS(&a.ctl->t0, 0ull, now);
+        }
+        nm_lockstep_batch<VAR>(a, sp, smem + wib * nm_warp_bytes(a.maxe), lane);
+    }
+    else
+        batch_queue_loop<SMOOTHER, VAR, MAXK>(a, sp, smem);
+}
+
+// one warp per vertex: claim chunks of the queue, wait for each item's
+// dependencies, relocate it
+template <int SMOOTHER, int VAR, int MAXK>
+__device__ __forceinline__ void batch_queue_loop(const BatchArgs& a, const SmoothParams& sp, char* smem)
+{
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WarpPatch P = carve_patch(smem + wib * warp_patch_bytes(MAXK, a.maxe), MAXK, a.maxe);
     if (threadIdx.x == 0)
@@ -198,7 +379,8 @@ static cudaError_t launch_batch_t(const BatchArgs& a, const SmoothParams& sp, in
                                   cudaStream_t s)
 {
     auto kern = batch_relocate_kernel<SMOOTHER, VAR, MAXK>;
-    size_t smem = patch_smem_per_warp(MAXK, a.maxe) * wpb;
+    size_t smem = (BatchLockstep<SMOOTHER, VAR, MAXK>::on ? nm_warp_bytes(a.maxe) : patch_smem_per_warp(MAXK, a.maxe)) *
+                  wpb;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int occ = 0;

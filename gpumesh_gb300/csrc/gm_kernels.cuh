@@ -230,15 +230,16 @@ __device__ __forceinline__ uint32_t tet_corner(uint4 t, int k)
 
 __device__ __forceinline__ bool sine_metric(const Crew& c) { return c.sampler == kSamplerSine; }
 
+// stage elements first, first + stride, ... of v's patch in canonical form
 template <int VAR>
-__device__ __forceinline__ void stage_patch_canonical(const MeshView& m, const Crew& crew, uint32_t v, V3<float> o,
-                                                      WarpPatch& P, int lane)
+__device__ __forceinline__ void stage_canonical_range(const MeshView& m, const Crew& crew, uint32_t v, V3<float> o,
+                                                      WarpPatch& P, int first, int stride)
 {
     const uint32_t b = m.ve_off[v], e = m.ve_off[v + 1];
     P.E = (int)(e - b);
     P.o = o;
     const bool sine = VAR == kVarMCDiag && sine_metric(crew);
-    for (int i = lane; i < P.E; i += kWarp)
+    for (int i = first; i < P.E; i += stride)
     {
         const uint32_t r = m.ve[b + i];
         const int x = 3 ^ ref_local(r);
@@ -263,8 +264,14 @@ __device__ __forceinline__ void stage_patch_canonical(const MeshView& m, const C
         P.sp[2 * P.maxe + i] = make_float4(q2.x, q2.y, q2.z, s[1]);
         P.sp[3 * P.maxe + i] = make_float4(c[1], s[2], c[2], s[3]);
         P.sp[4 * P.maxe + i] = make_float4(c[3], s[4], c[4], 0.f);
-        P.meta[i] = kTet;
     }
+}
+
+template <int VAR>
+__device__ __forceinline__ void stage_patch_canonical(const MeshView& m, const Crew& crew, uint32_t v, V3<float> o,
+                                                      WarpPatch& P, int lane)
+{
+    stage_canonical_range<VAR>(m, crew, v, o, P, lane, kWarp);
     __syncwarp();
 }
 

@@ -7,6 +7,7 @@
 
 #include "gm_kernels.cuh"
 #include "gm_launch.h"
+#include "gm_nm_lockstep.cuh"
 
 namespace gm {
 
@@ -71,20 +72,62 @@ __global__ void __launch_bounds__(128) relocate_kernel(MeshView m, Crew crew, Sm
     count_work(ctr, evals, P.E, MAXK == 4 ? kTet : kHex, deferred, lane);
 }
 
-template <int SMOOTHER, int VAR, int MAXK>
-static cudaError_t launch_relocate_t(const RelocLaunch& L)
+// Nelder-Mead on canonical tet patches: kNMGroups vertices per warp in
+// lockstep (gm_nm_lockstep.cuh); each warp owns kNMWarpVertices consecutive
+// members of the colour.
+constexpr uint32_t kNMWarpVertices = 4 * kNMGroups;
+constexpr int kNMWarpsPerBlock = 4;
+
+template <int VAR>
+__global__ void __launch_bounds__(kNMWarpsPerBlock * 32, 4)
+    relocate_nm_lockstep_kernel(MeshView m, Crew crew, SmoothParams sp, const uint32_t* members, uint32_t count,
+                                int maxe, Counters* ctr, Deferred def, uint32_t slot_base)
 {
-    size_t smem = patch_smem_per_warp(MAXK, L.maxe) * L.warps_per_block;
+    extern __shared__ __align__(16) char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t begin = (blockIdx.x * (blockDim.x >> 5) + wib) * kNMWarpVertices;
+    if (begin >= count) return;
+    const uint32_t end = min(begin + kNMWarpVertices, count);
+    nm_lockstep_plain<VAR>(m, crew, sp, members, begin, end, smem + wib * nm_warp_bytes(maxe), maxe, ctr, def,
+                           slot_base, lane);
+}
+
+template <int VAR>
+static cudaError_t launch_nm_lockstep(const RelocLaunch& L)
+{
+    const size_t smem = nm_warp_bytes(L.maxe) * kNMWarpsPerBlock;
     if (smem > 48 * 1024)
     {
-        cudaError_t e = cudaFuncSetAttribute(relocate_kernel<SMOOTHER, VAR, MAXK>,
+        cudaError_t e = cudaFuncSetAttribute(relocate_nm_lockstep_kernel<VAR>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    unsigned blocks = (L.count + L.warps_per_block - 1) / L.warps_per_block;
-    relocate_kernel<SMOOTHER, VAR, MAXK><<<blocks, 32 * L.warps_per_block, smem, L.stream>>>(
+    const uint32_t per_block = kNMWarpVertices * kNMWarpsPerBlock;
+    const unsigned blocks = (L.count + per_block - 1) / per_block;
+    relocate_nm_lockstep_kernel<VAR><<<blocks, 32 * kNMWarpsPerBlock, smem, L.stream>>>(
         L.m, L.crew, L.sp, L.members, L.count, L.maxe, L.ctr, L.def, L.slot_base);
     return cudaGetLastError();
+}
+
+template <int SMOOTHER, int VAR, int MAXK>
+static cudaError_t launch_relocate_t(const RelocLaunch& L)
+{
+    if constexpr (SMOOTHER == kSmoothNM && TetCanon<VAR, MAXK>::on)
+        return launch_nm_lockstep<VAR>(L);
+    else
+    {
+        size_t smem = patch_smem_per_warp(MAXK, L.maxe) * L.warps_per_block;
+        if (smem > 48 * 1024)
+        {
+            cudaError_t e = cudaFuncSetAttribute(relocate_kernel<SMOOTHER, VAR, MAXK>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        unsigned blocks = (L.count + L.warps_per_block - 1) / L.warps_per_block;
+        relocate_kernel<SMOOTHER, VAR, MAXK><<<blocks, 32 * L.warps_per_block, smem, L.stream>>>(
+            L.m, L.crew, L.sp, L.members, L.count, L.maxe, L.ctr, L.def, L.slot_base);
+        return cudaGetLastError();
+    }
 }
 
 template <int SMOOTHER>
