@@ -80,7 +80,7 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="C5: arrival window")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="C5: mean arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0, help="C5: HBM admission budget")
-    ap.add_argument("--only", choices=["eval", "relocate"], default=None,
+    ap.add_argument("--only", choices=["eval", "relocate", "batch"], default=None,
                     help="profiling driver: a few launches of one kernel family, no JSON line")
     return ap.parse_args()
 
@@ -466,11 +466,12 @@ def bench_gpu(args, rank, world, local):
 def profile_driver(args):
     """A few launches of one kernel family, for ncu: `eval` = the evaluation
     kernel on the 128^3 hex mesh (4 launches); `relocate` = one pass of each
-    smoother of the workload's schedule."""
+    smoother of the workload's schedule; `batch` = two batched Nelder-Mead
+    passes over the first --batch-meshes meshes of C4."""
     import torch
 
     from gpumesh_gb300 import mesh as M
-    from gpumesh_gb300 import meshgen
+    from gpumesh_gb300 import meshgen, workloads
 
     if args.only == "eval":
         raw = meshgen.box_mesh(128, "hex", 0.15, 2, gaussian=True)
@@ -479,6 +480,23 @@ def profile_driver(args):
         for _ in range(4):
             h = dev.evaluate()
         print("eval", h.minimumQuality(), h.harmonicMean())
+    elif args.only == "batch":
+        # the first --batch-meshes meshes of the C4 stream, 8 warps per block,
+        # two Nelder-Mead passes of the persistent kernel
+        sizes = meshgen.batch_sizes(args.batch_meshes, 4, 24, 3)
+        devs = []
+        for i, n in enumerate(sizes):
+            raw = meshgen.box_mesh(int(n), "tet", 0.3, 3 * 1000003 + i)
+            perm, groups = M.node_groups_build(raw)
+            d = M.DeviceMesh(M.permute_mesh(raw, perm), groups)
+            d.set_crew("uniform", "metric_free", "mean_ratio")
+            devs.append(d)
+        batch = M.Batch(devs)
+        batch.set_config(8, 0)
+        for _ in range(2):
+            batch.smooth_pass("nelder_mead", workloads.NM_PARAMS)
+            batch.sync()
+        print("batch", batch.status(), batch.counters())
     else:
         w, raw, groups = prepare(args.workload)
         dev = M.DeviceMesh(raw, groups)

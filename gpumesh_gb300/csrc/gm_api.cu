@@ -191,6 +191,7 @@ void relocate_group(gm_mesh* m, int smoother, const SmoothParams& sp, uint32_t b
     L.count = count;
     L.maxe = m->maxe;
     L.warps_per_block = m->warps_per_block;
+    L.sm_count = m->sm_count;
     L.ctr = m->ctr.p;
     L.def = Deferred{m->def_v.p, m->def_old.p, m->def_new.p, m->def_count.p + slot};
     L.slot_base = base;

@@ -127,18 +127,22 @@ __device__ __forceinline__ void batch_one(const BatchMesh& bm, const SmoothParam
 // colours waits without holding up the other groups (one poll per step,
 // bounded by spin_limit).  The FP64 acceptance test of a near-degenerate
 // patch runs warp-wide, one group at a time, on a corner-position copy of
-// that group's patch.  Deadlock freedom is the queue's: an item waits only
+// that group's patch staged over the group's own (finished) canonical
+// patch.  Deadlock freedom is the queue's: an item waits only
 // for items earlier in the queue, which were handed out before it.
 template <int VAR>
 __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, char* wsm, int lane)
 {
     const int gi = lane / kNMGroup, sub = lane & (kNMGroup - 1), leader = gi * kNMGroup;
     WarpPatch P = nm_group_patch(wsm, gi, a.maxe);
+    float* con = nm_group_con(wsm, gi, a.maxe);
     NMGroup g;
     g.phase = kNMIdle;
     g.E = 0;
+    g.cid = 0;
     const BatchMesh* bm = a.meshes;  // the group's mesh (any valid entry while idle)
     uint32_t mesh = 0, need = 0;
+    unsigned int seen = 0;  // the mesh's done count, polled one step ahead of its use
     unsigned long long spins = 0;
     TetConst kc = tet_const<VAR>(bm->crew);
     bool sine = false;
@@ -175,6 +179,7 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
             mesh = sg.mesh;
             need = sg.need;
             spins = 0;
+            seen = 0;
             g.v = bm->members[sg.member_begin + (item - __ldg(&a.seg_start[s]))];
             g.phase = kNMWait;
         }
@@ -186,10 +191,11 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
             continue;
         }
         // (2) a waiting group starts once its mesh's earlier colours are done
+        // (the done count was loaded at the end of the previous step)
         int ok = 0, give_up = 0;
         if (g.phase == kNMWait && sub == 0)
         {
-            if (need == 0 || __ldcv(&a.done[mesh]) >= need) ok = 1;
+            if (need == 0 || seen >= need) ok = 1;
             else if (++spins > a.spin_limit || __ldcv(&a.ctl->error))
             {
                 atomicOr(&a.ctl->error, 1u);
@@ -198,24 +204,32 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
         }
         ok = __shfl_sync(kFullMask, ok, leader);
         give_up = __shfl_sync(kFullMask, give_up, leader);
-        if (ok)
+        if (__any_sync(kFullMask, ok))
         {
-            __threadfence();
-            nm_begin<VAR>(g, bm->view, bm->crew, P, g.v, sub);
-            kc = tet_const<VAR>(bm->crew);
-            sine = VAR == kVarMCDiag && sine_metric(bm->crew);
+            float ls = 0.f;
+            uint32_t nvv = 1;
+            if (ok)
+            {
+                __threadfence();
+                sine = VAR == kVarMCDiag && sine_metric(bm->crew);
+                kc = tet_const<VAR>(bm->crew);
+                ls = nm_begin<VAR>(g, bm->view, sine, P, con, g.v, sub, nvv);
+            }
+            __syncwarp();
+            nm_finish_begin(g, sp, ok, ls, nvv);
         }
-        __syncwarp();
-        if (__any_sync(kFullMask, ok)) nm_local_size(g, bm->view, sp, ok, sub);
         // (3) one evaluation per busy group
         const bool busy = g.phase >= kNMQ0;
         if (!__any_sync(kFullMask, busy)) __nanosleep(100);
-        const float f = nm_group_quality<VAR>(bm->crew, P, busy ? g.E : 0, g.cand, kc, sine, sub);
+        // poll for the still-waiting groups; the value is used at the next
+        // step, so the load's latency overlaps this step's evaluation
+        if (g.phase == kNMWait && sub == 0 && !give_up && need) seen = __ldcv(&a.done[mesh]);
+        const float f = nm_group_quality<VAR>(P, busy ? g.E : 0, g.cand, kc, sine, sub);
         bool finishing = false, need64 = false, accept = true;
         if (busy)
         {
             ++g.evals;
-            if (g.phase != kNMFinal) nm_step(g, f, sp, bm->view);
+            if (g.phase != kNMFinal) nm_step(g, f, sp, con);
             else
             {
                 finishing = true;
@@ -234,7 +248,7 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
             const double oz = __shfl_sync(kFullMask, g.old.z, src);
             const double nx = __shfl_sync(kFullMask, g.cand.x, src), ny = __shfl_sync(kFullMask, g.cand.y, src);
             const double nz = __shfl_sync(kFullMask, g.cand.z, src);
-            WarpPatch X = nm_fp64_patch(wsm, a.maxe);
+            WarpPatch X = nm_fp64_patch(wsm, src / kNMGroup, a.maxe);
             stage_patch(bx->view, vx, X, lane);
             const double d0 = patch_uniform<VAR, 4, double>(bx->crew, X, mk(ox, oy, oz), lane);
             const double d1 = patch_uniform<VAR, 4, double>(bx->crew, X, mk(nx, ny, nz), lane);

@@ -230,6 +230,34 @@ __device__ __forceinline__ uint32_t tet_corner(uint4 t, int k)
 
 __device__ __forceinline__ bool sine_metric(const Crew& c) { return c.sampler == kSamplerSine; }
 
+// element i of a canonical patch from its fixed corners a0, a1, a2 (in
+// canonical order) and the origin o
+template <int VAR>
+__device__ __forceinline__ void stage_canonical_element(WarpPatch& P, int i, float4 a0, float4 a1, float4 a2,
+                                                        V3<float> o, bool sine)
+{
+    const V3<float> r0 = to<float>(a0) - o, r1 = to<float>(a1) - o, r2 = to<float>(a2) - o;
+    const V3<float> q1 = r0 * kFrA + r1 * kFrB, q2 = (r0 + r1) * kFrD + r2 * kFrG;
+    float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, c[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (VAR == kVarMCDiag && sine)
+    {
+        const float sum = a0.x + a1.x + a2.x;
+        const float X[5] = {sum * 0.25f, a0.x * kKeastH + (a1.x + a2.x) * kKeastQ,
+                            a1.x * kKeastH + (a0.x + a2.x) * kKeastQ, a2.x * kKeastH + (a0.x + a1.x) * kKeastQ,
+                            sum * kKeastQ};
+#pragma unroll
+        for (int k = 0; k < 5; ++k) sincospif(4.f * X[k], &s[k], &c[k]);
+    }
+    P.sp[0 * P.maxe + i] = make_float4(r0.x, r0.y, r0.z, s[0]);
+    P.sp[1 * P.maxe + i] = make_float4(q1.x, q1.y, q1.z, c[0]);
+    P.sp[2 * P.maxe + i] = make_float4(q2.x, q2.y, q2.z, s[1]);
+    if (VAR == kVarMCDiag)
+    {
+        P.sp[3 * P.maxe + i] = make_float4(c[1], s[2], c[2], s[3]);
+        P.sp[4 * P.maxe + i] = make_float4(c[3], s[4], c[4], 0.f);
+    }
+}
+
 // stage elements first, first + stride, ... of v's patch in canonical form
 template <int VAR>
 __device__ __forceinline__ void stage_canonical_range(const MeshView& m, const Crew& crew, uint32_t v, V3<float> o,
@@ -247,23 +275,7 @@ __device__ __forceinline__ void stage_canonical_range(const MeshView& m, const C
         const float4 a0 = __ldcg(&m.pos[tet_corner(t, x)]);
         const float4 a1 = __ldcg(&m.pos[tet_corner(t, 1 ^ x)]);
         const float4 a2 = __ldcg(&m.pos[tet_corner(t, 2 ^ x)]);
-        const V3<float> r0 = to<float>(a0) - o, r1 = to<float>(a1) - o, r2 = to<float>(a2) - o;
-        const V3<float> q1 = r0 * kFrA + r1 * kFrB, q2 = (r0 + r1) * kFrD + r2 * kFrG;
-        float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, c[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-        if (sine)
-        {
-            const float sum = a0.x + a1.x + a2.x;
-            const float X[5] = {sum * 0.25f, a0.x * kKeastH + (a1.x + a2.x) * kKeastQ,
-                                a1.x * kKeastH + (a0.x + a2.x) * kKeastQ, a2.x * kKeastH + (a0.x + a1.x) * kKeastQ,
-                                sum * kKeastQ};
-#pragma unroll
-            for (int k = 0; k < 5; ++k) sincospif(4.f * X[k], &s[k], &c[k]);
-        }
-        P.sp[0 * P.maxe + i] = make_float4(r0.x, r0.y, r0.z, s[0]);
-        P.sp[1 * P.maxe + i] = make_float4(q1.x, q1.y, q1.z, c[0]);
-        P.sp[2 * P.maxe + i] = make_float4(q2.x, q2.y, q2.z, s[1]);
-        P.sp[3 * P.maxe + i] = make_float4(c[1], s[2], c[2], s[3]);
-        P.sp[4 * P.maxe + i] = make_float4(c[3], s[4], c[4], 0.f);
+        stage_canonical_element<VAR>(P, i, a0, a1, a2, o, sine);
     }
 }
 
@@ -306,8 +318,9 @@ __device__ __forceinline__ TetConst tet_const(const Crew& crew)
     return k;
 }
 
+// sine: the crew's sampler is the sine-graded one (metric conformity only)
 template <int VAR>
-__device__ __forceinline__ TetCand tet_cand(const Crew& crew, V3<float> o, V3<float> c)
+__device__ __forceinline__ TetCand tet_cand(bool sine, V3<float> o, V3<float> c)
 {
     TetCand t;
     const V3<float> d = c - o;
@@ -315,7 +328,7 @@ __device__ __forceinline__ TetCand tet_cand(const Crew& crew, V3<float> o, V3<fl
     t.k1 = d * kK1;
     t.k2 = d * kK2;
     t.sa = t.ca = t.sq = t.cq = t.sh = t.ch = 0.f;
-    if (VAR == kVarMCDiag && sine_metric(crew))
+    if (VAR == kVarMCDiag && sine)
     {
         sincospif(c.x, &t.sa, &t.ca);                  // 4 * (1/4) * c.x
         sincospif(c.x * (2.0f / 3.0f), &t.sq, &t.cq);  // 4 * (1/6) * c.x
@@ -488,7 +501,7 @@ __device__ __forceinline__ R patch_uniform(const Crew& crew, const WarpPatch& P,
     {
         const TetConst k = tet_const<VAR>(crew);
         const bool sine = VAR == kVarMCDiag && sine_metric(crew);
-        const TetCand t = tet_cand<VAR>(crew, P.o, c);
+        const TetCand t = tet_cand<VAR>(sine, P.o, c);
         for (int e = lane; e < P.E; e += kWarp) acc_add(a, canonical_quality<VAR>(P, e, t, k, sine));
     }
     else
@@ -519,7 +532,7 @@ __device__ __forceinline__ void patch_multi(const Crew& crew, WarpPatch& P, int 
             V3<R> cp = to<R>(cf);
             if constexpr (TetCanon<VAR, MAXK>::on && sizeof(R) == sizeof(float))
             {
-                const TetCand t = tet_cand<VAR>(crew, P.o, cp);
+                const TetCand t = tet_cand<VAR>(sine, P.o, cp);
                 for (int e = sub; e < P.E; e += S) acc_add(a, canonical_quality<VAR>(P, e, t, k, sine));
             }
             else

@@ -27,6 +27,7 @@ struct RelocLaunch
     uint32_t count;
     int maxe;
     int warps_per_block;
+    int sm_count;
     Counters* ctr;
     Deferred def;
     uint32_t slot_base;  // this group's region of the deferred arrays

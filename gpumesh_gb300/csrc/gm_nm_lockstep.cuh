@@ -11,6 +11,8 @@
 // (elements over the group's lanes, 3-step reduction), then advances each
 // group's state.  A group whose vertex is done takes the warp's next vertex
 // at the next step, so the groups stay busy until the warp's work runs out.
+// Everything a step needs is in registers or shared memory: the patch, and
+// the vertex's boundary constraint copied next to it when the vertex starts.
 //
 // Each vertex follows nelder_mead() (NelderMeadSmoother.cpp:100-260)
 // decision for decision: initial simplex, sort, reflection / expansion /
@@ -24,6 +26,7 @@ namespace gm {
 
 constexpr int kNMGroup = 8;                   // lanes per vertex
 constexpr int kNMGroups = kWarp / kNMGroup;   // vertices per warp
+constexpr int kNMConWords = 16;               // constraint record per group
 constexpr unsigned kFullMask = 0xffffffffu;
 
 enum : int { kNMIdle = 0, kNMWait, kNMQ0, kNMInit, kNMReflect, kNMProbe, kNMFinal };
@@ -47,11 +50,11 @@ struct NMGroup
     V3<float> c, xr, cand;
 };
 
-// shared memory of one warp: the groups' canonical patches, then a
-// corner-position patch for the FP64 acceptance test of the batched path
+// shared memory of one warp: the groups' canonical patches (5 slots of
+// maxe float4 each), then one constraint record per group
 __host__ __device__ constexpr size_t nm_warp_bytes(int maxe)
 {
-    return ((size_t)kNMGroups * patch_slots(4) * maxe + 4 * (size_t)maxe) * 16 + (size_t)maxe * 4;
+    return (size_t)kNMGroups * patch_slots(4) * maxe * 16 + (size_t)kNMGroups * kNMConWords * 4;
 }
 
 __device__ __forceinline__ WarpPatch nm_group_patch(char* wsm, int gi, int maxe)
@@ -67,80 +70,122 @@ __device__ __forceinline__ WarpPatch nm_group_patch(char* wsm, int gi, int maxe)
     return P;
 }
 
-__device__ __forceinline__ WarpPatch nm_fp64_patch(char* wsm, int maxe)
+__device__ __forceinline__ float* nm_group_con(char* wsm, int gi, int maxe)
 {
-    WarpPatch P = nm_group_patch(wsm, kNMGroups, maxe);
+    return reinterpret_cast<float*>(wsm + (size_t)kNMGroups * patch_slots(4) * maxe * 16) + gi * kNMConWords;
+}
+
+// the corner-position patch (4 slots + element meta) of a finished group's
+// vertex, staged over that group's own region for an FP64 acceptance test
+__device__ __forceinline__ WarpPatch nm_fp64_patch(char* wsm, int gi, int maxe)
+{
+    WarpPatch P = nm_group_patch(wsm, gi, maxe);
     P.meta = reinterpret_cast<int*>(P.sp + 4 * (size_t)maxe);
     return P;
 }
 
-__device__ __forceinline__ V3<float> nm_snap(const MeshView& m, int cid, V3<float> x)
+// project() on a constraint record copied from a Constraint's FP32 head
+// (kind, a, b, u, len), the same formulas
+__device__ __forceinline__ V3<float> project_rec(const float* r, V3<float> p)
 {
-    return cid != 0 ? snap(m, cid, x) : x;
+    const V3<float> a = mk(r[1], r[2], r[3]);
+    switch (__float_as_int(r[0]))
+    {
+    case kConPlane:
+    {
+        const V3<float> n = mk(r[4], r[5], r[6]);
+        const float l = dot(p - a, n);
+        return p - n * l;
+    }
+    case kConSegment:
+    {
+        const V3<float> u = mk(r[7], r[8], r[9]);
+        const V3<float> dist = p - a;
+        const float l = dot(dist, u);
+        if (l < 0.f) return a;
+        if (l > r[10]) return mk(r[4], r[5], r[6]);
+        return p - (dist - u * l);
+    }
+    case kConSphere: return normalize(p);
+    case kConPoint: return a;
+    default: return p;
+    }
+}
+
+__device__ __forceinline__ V3<float> nm_snap(const NMGroup& g, const float* con, V3<float> x)
+{
+    return g.cid != 0 ? project_rec(con, x) : x;
 }
 
 // patch quality of the group's candidate (E = 0: an idle group, result unused)
 template <int VAR>
-__device__ __forceinline__ float nm_group_quality(const Crew& crew, const WarpPatch& P, int E, V3<float> c,
-                                                  const TetConst& kc, bool sine, int sub)
+__device__ __forceinline__ float nm_group_quality(const WarpPatch& P, int E, V3<float> c, const TetConst& kc, bool sine,
+                                                  int sub)
 {
-    const TetCand t = tet_cand<VAR>(crew, P.o, c);
+    const TetCand t = tet_cand<VAR>(sine, P.o, c);
     PatchAcc<float> a{0.f, 3.0e38f, 0};
     for (int e = sub; e < E; e += kNMGroup) acc_add(a, canonical_quality<VAR>(P, e, t, kc, sine));
     acc_reduce(a, kNMGroup);
     return acc_final(a, E);
 }
 
-// the next cycle: reflection, or the final point, or the reset simplex
-__device__ __forceinline__ void nm_next_cycle(NMGroup& g, const SmoothParams& sp, const MeshView& m)
+// Advance the group with the quality f of its candidate.  The groups of a
+// warp are usually in different phases, and SIMT runs each distinct path
+// once for the groups on it, so the phase-specific parts are short and the
+// common tail (insertion, convergence test, next cycle, projection of the
+// next candidate) is one block shared by every group that reaches it.
+__device__ __forceinline__ void nm_step(NMGroup& g, float f, const SmoothParams& sp, const float* con)
 {
-    if (g.cycle < sp.cycles)
+    bool insert = false, next = false, snap_next = true;
+    S4 vx{g.cand, f};
+    V3<float> x = g.cand;  // the next candidate before projection
+    const int phase = g.phase;
+    if (phase == kNMReflect)
     {
-        g.c = (g.s1.p + g.s2.p + g.s3.p) * (1.f / 3.f);
-        g.cand = nm_snap(m, g.cid, g.c + (g.c - g.s0.p) * sp.alpha);
-        g.phase = kNMReflect;
+        g.fr = f;
+        g.xr = g.cand;
+        if (g.s3.w < f)  // expand
+        {
+            x = g.c + (g.xr - g.c) * sp.gamma;
+            g.phase = kNMProbe;
+        }
+        else if (g.s1.w >= f)  // contract
+        {
+            x = g.c + ((f > g.s0.w ? g.xr : g.s0.p) - g.c) * sp.beta;
+            g.phase = kNMProbe;
+        }
+        else  // accept the reflection
+        {
+            insert = true;
+            snap_next = false;
+        }
     }
-    else if (g.reset)
+    else if (phase == kNMProbe)
     {
-        g.cand = nm_snap(m, g.cid, g.s3.p);
-        g.phase = kNMFinal;
+        if (g.s3.w < g.fr && f <= g.fr) vx = S4{g.xr, g.fr};
+        insert = true;
+        snap_next = false;
     }
-    else
+    else if (phase == kNMInit)
     {
-        g.s0 = S4{g.vo.p - mk(g.ns, 0.f, 0.f), g.vo.w};
-        g.s1 = S4{g.vo.p - mk(0.f, g.ns, 0.f), g.vo.w};
-        g.s2 = S4{g.vo.p - mk(0.f, 0.f, g.ns), g.vo.w};
-        g.s3 = g.vo;
-        g.reset = true;
-        g.cycle = 0;
-        g.k = 0;
-        g.cand = nm_snap(m, g.cid, g.s0.p);
-        g.phase = kNMInit;
+        if (g.k == 0) g.s0 = vx;
+        else if (g.k == 1) g.s1 = vx;
+        else g.s2 = vx;
+        ++g.k;
+        if (g.k < 3) x = g.k == 1 ? g.s1.p : g.s2.p;
+        else
+        {
+            if (g.s0.w > g.s1.w) swp(g.s0, g.s1);
+            if (g.s1.w > g.s2.w) swp(g.s1, g.s2);
+            if (g.s2.w > g.s3.w) swp(g.s2, g.s3);
+            if (g.s0.w > g.s1.w) swp(g.s0, g.s1);
+            if (g.s1.w > g.s2.w) swp(g.s1, g.s2);
+            if (g.s0.w > g.s1.w) swp(g.s0, g.s1);
+            next = true;
+            snap_next = false;
+        }
     }
-}
-
-__device__ __forceinline__ void nm_insert(NMGroup& g, S4 vx, const SmoothParams& sp, const MeshView& m)
-{
-    if (vx.w > g.s3.w) swp(g.s3, vx);
-    if (vx.w > g.s2.w) swp(g.s2, vx);
-    if (vx.w > g.s1.w) swp(g.s1, vx);
-    if (vx.w > g.s0.w) swp(g.s0, vx);
-    if ((g.s3.w - g.s1.w) < sp.convergence)
-    {
-        g.cand = nm_snap(m, g.cid, g.s3.p);
-        g.phase = kNMFinal;
-        return;
-    }
-    ++g.cycle;
-    nm_next_cycle(g, sp, m);
-}
-
-// advance the group with the quality f of its candidate
-__device__ __forceinline__ void nm_step(NMGroup& g, float f, const SmoothParams& sp, const MeshView& m)
-{
-    switch (g.phase)
-    {
-    case kNMQ0:
+    else  // kNMQ0
     {
         const V3<float> pos = to<float>(g.old);
         g.q0 = f;
@@ -152,90 +197,109 @@ __device__ __forceinline__ void nm_step(NMGroup& g, float f, const SmoothParams&
         g.cycle = 0;
         g.reset = false;
         g.k = 0;
-        g.cand = nm_snap(m, g.cid, g.s0.p);
+        x = g.s0.p;
         g.phase = kNMInit;
-        break;
     }
-    case kNMInit:
+    if (insert)
     {
-        const S4 nv{g.cand, f};
-        if (g.k == 0) g.s0 = nv;
-        else if (g.k == 1) g.s1 = nv;
-        else g.s2 = nv;
-        ++g.k;
-        if (g.k < 3)
+        if (vx.w > g.s3.w) swp(g.s3, vx);
+        if (vx.w > g.s2.w) swp(g.s2, vx);
+        if (vx.w > g.s1.w) swp(g.s1, vx);
+        if (vx.w > g.s0.w) swp(g.s0, vx);
+        if ((g.s3.w - g.s1.w) < sp.convergence)
         {
-            g.cand = nm_snap(m, g.cid, g.k == 1 ? g.s1.p : g.s2.p);
-            break;
-        }
-        if (g.s0.w > g.s1.w) swp(g.s0, g.s1);
-        if (g.s1.w > g.s2.w) swp(g.s1, g.s2);
-        if (g.s2.w > g.s3.w) swp(g.s2, g.s3);
-        if (g.s0.w > g.s1.w) swp(g.s0, g.s1);
-        if (g.s1.w > g.s2.w) swp(g.s1, g.s2);
-        if (g.s0.w > g.s1.w) swp(g.s0, g.s1);
-        nm_next_cycle(g, sp, m);
-        break;
-    }
-    case kNMReflect:
-    {
-        g.fr = f;
-        g.xr = g.cand;
-        V3<float> x = g.xr;
-        bool probe = true;
-        if (g.s3.w < f) x = g.c + (g.xr - g.c) * sp.gamma;                                 // expand
-        else if (g.s1.w >= f) x = g.c + ((f > g.s0.w ? g.xr : g.s0.p) - g.c) * sp.beta;  // contract
-        else probe = false;                                                               // accept
-        if (probe)
-        {
-            g.cand = nm_snap(m, g.cid, x);
-            g.phase = kNMProbe;
+            x = g.s3.p;
+            g.phase = kNMFinal;
+            snap_next = true;
         }
         else
-            nm_insert(g, S4{g.xr, f}, sp, m);
-        break;
+        {
+            ++g.cycle;
+            next = true;
+        }
     }
-    case kNMProbe:
+    if (next)
     {
-        S4 vx{g.cand, f};
-        if (g.s3.w < g.fr && f <= g.fr) vx = S4{g.xr, g.fr};
-        nm_insert(g, vx, sp, m);
-        break;
+        snap_next = true;
+        if (g.cycle < sp.cycles)
+        {
+            g.c = (g.s1.p + g.s2.p + g.s3.p) * (1.f / 3.f);
+            x = g.c + (g.c - g.s0.p) * sp.alpha;
+            g.phase = kNMReflect;
+        }
+        else if (g.reset)
+        {
+            x = g.s3.p;
+            g.phase = kNMFinal;
+        }
+        else
+        {
+            g.s0 = S4{g.vo.p - mk(g.ns, 0.f, 0.f), g.vo.w};
+            g.s1 = S4{g.vo.p - mk(0.f, g.ns, 0.f), g.vo.w};
+            g.s2 = S4{g.vo.p - mk(0.f, 0.f, g.ns), g.vo.w};
+            g.s3 = g.vo;
+            g.reset = true;
+            g.cycle = 0;
+            g.k = 0;
+            x = g.s0.p;
+            g.phase = kNMInit;
+        }
     }
-    default: break;
-    }
+    if (snap_next) g.cand = nm_snap(g, con, x);
 }
 
-// a group takes vertex v: canonical patch over its lanes, start position
+// A group takes vertex v: canonical patch and constraint record over its
+// lanes, start position; returns this lane's part of the local element size
+// sum (AbstractMeasurer::computeLocalElementSize), reduced by nm_finish_begin.
+// The element and neighbour loads go out in the same loop so that their
+// latencies overlap.
 template <int VAR>
-__device__ __forceinline__ void nm_begin(NMGroup& g, const MeshView& m, const Crew& crew, WarpPatch& P, uint32_t v,
-                                         int sub)
+__device__ __forceinline__ float nm_begin(NMGroup& g, const MeshView& m, bool sine, WarpPatch& P, float* con,
+                                          uint32_t v, int sub, uint32_t& nvv)
 {
     g.v = v;
     g.cid = m.cid[v];
     g.old = __ldcg(&m.pos[v]);
-    stage_canonical_range<VAR>(m, crew, v, to<float>(g.old), P, sub, kNMGroup);
+    const uint32_t eb = m.ve_off[v], ee = m.ve_off[v + 1];
+    const uint32_t vb = m.vv_off[v], ve = m.vv_off[v + 1];
+    const V3<float> o = to<float>(g.old);
+    P.E = (int)(ee - eb);
+    P.o = o;
+    nvv = ve - vb;
+    float ls = 0.f;
+    const uint32_t n = max(ee - eb, ve - vb);
+    for (uint32_t i = sub; i < n; i += kNMGroup)
+    {
+        if (i < ve - vb) ls += length(to<float>(__ldcg(&m.pos[m.vv[vb + i]])) - o);
+        if (i < ee - eb)
+        {
+            const uint32_t r = m.ve[eb + i];
+            const int x = 3 ^ ref_local(r);
+            const uint4 t = m.tets[ref_id(r)];
+            const float4 a0 = __ldcg(&m.pos[tet_corner(t, x)]);
+            const float4 a1 = __ldcg(&m.pos[tet_corner(t, 1 ^ x)]);
+            const float4 a2 = __ldcg(&m.pos[tet_corner(t, 2 ^ x)]);
+            stage_canonical_element<VAR>(P, (int)i, a0, a1, a2, o, sine);
+        }
+    }
+    // the FP32 head of the vertex's Constraint (identity for a free vertex or
+    // an id outside the table, as project() treats them)
+    const bool has = g.cid > 0 && g.cid < m.ncon;
+    for (int w = sub; w < 11; w += kNMGroup)
+        con[w] = has ? reinterpret_cast<const float*>(&m.con[g.cid])[w] : __int_as_float(kConVolume);
     g.E = P.E;
     g.evals = 0;
-    g.cand = to<float>(g.old);
+    g.cand = o;
     g.phase = kNMQ0;
+    return ls;
 }
 
-// local element size of the starting groups' vertices (all lanes take part)
-__device__ __forceinline__ void nm_local_size(NMGroup& g, const MeshView& m, const SmoothParams& sp, bool start,
-                                              int sub)
+// reduce the local size sums of starting groups (all lanes take part)
+__device__ __forceinline__ void nm_finish_begin(NMGroup& g, const SmoothParams& sp, bool start, float ls,
+                                                uint32_t nvv)
 {
-    float s = 0.f;
-    uint32_t b = 0, e = 0;
-    if (start)
-    {
-        b = m.vv_off[g.v];
-        e = m.vv_off[g.v + 1];
-        const V3<float> pos = to<float>(g.old);
-        for (uint32_t i = b + sub; i < e; i += kNMGroup) s += length(to<float>(__ldcg(&m.pos[m.vv[i]])) - pos);
-    }
-    for (int o = kNMGroup / 2; o > 0; o >>= 1) s += __shfl_xor_sync(kFullMask, s, o);
-    if (start) g.ns = s / (float)(e - b) * sp.shift;
+    for (int o = kNMGroup / 2; o > 0; o >>= 1) ls += __shfl_xor_sync(kFullMask, ls, o);
+    if (start) g.ns = ls / (float)nvv * sp.shift;
 }
 
 __device__ __forceinline__ void nm_flush_counters(Counters* ctr, unsigned long long evals,
@@ -266,11 +330,13 @@ __device__ void nm_lockstep_plain(const MeshView& m, const Crew& crew, const Smo
 {
     const int gi = lane / kNMGroup, sub = lane & (kNMGroup - 1);
     WarpPatch P = nm_group_patch(wsm, gi, maxe);
+    float* con = nm_group_con(wsm, gi, maxe);
     const TetConst kc = tet_const<VAR>(crew);
     const bool sine = VAR == kVarMCDiag && sine_metric(crew);
     NMGroup g;
     g.phase = kNMIdle;
     g.E = 0;
+    g.cid = 0;
     uint32_t next = begin;
     unsigned long long n_evals = 0, n_elems = 0, n_fp64 = 0;
     while (true)
@@ -283,17 +349,22 @@ __device__ void nm_lockstep_plain(const MeshView& m, const Crew& crew, const Smo
         const bool start = idle && base + rank < end;
         next += __popc(ball);
         if (!__any_sync(kFullMask, start || !idle)) break;
-        if (start) nm_begin<VAR>(g, m, crew, P, members[base + rank], sub);
-        __syncwarp();
-        if (__any_sync(kFullMask, start)) nm_local_size(g, m, sp, start, sub);
+        if (__any_sync(kFullMask, start))
+        {
+            float ls = 0.f;
+            uint32_t nvv = 1;
+            if (start) ls = nm_begin<VAR>(g, m, sine, P, con, members[base + rank], sub, nvv);
+            __syncwarp();
+            nm_finish_begin(g, sp, start, ls, nvv);
+        }
         // one evaluation per busy group
         const bool busy = g.phase != kNMIdle;
-        const float f = nm_group_quality<VAR>(crew, P, busy ? g.E : 0, g.cand, kc, sine, sub);
+        const float f = nm_group_quality<VAR>(P, busy ? g.E : 0, g.cand, kc, sine, sub);
         if (!busy) continue;
         ++g.evals;
         if (g.phase != kNMFinal)
         {
-            nm_step(g, f, sp, m);
+            nm_step(g, f, sp, con);
             continue;
         }
         // done: commit, or defer to the FP64 acceptance kernel

@@ -73,21 +73,24 @@ __global__ void __launch_bounds__(128) relocate_kernel(MeshView m, Crew crew, Sm
 }
 
 // Nelder-Mead on canonical tet patches: kNMGroups vertices per warp in
-// lockstep (gm_nm_lockstep.cuh); each warp owns kNMWarpVertices consecutive
-// members of the colour.
-constexpr uint32_t kNMWarpVertices = 4 * kNMGroups;
+// lockstep (gm_nm_lockstep.cuh); each warp owns `per_warp` consecutive
+// members of the colour.  A colour too small to give every SM 16 warps gets
+// one vertex per warp (the launch is latency bound: every vertex starts at
+// once and no group waits for another's search); a large one up to four per
+// group, so the groups of a warp refill and the tail where some groups idle
+// is short against the warp's work.
 constexpr int kNMWarpsPerBlock = 4;
 
 template <int VAR>
 __global__ void __launch_bounds__(kNMWarpsPerBlock * 32, 4)
     relocate_nm_lockstep_kernel(MeshView m, Crew crew, SmoothParams sp, const uint32_t* members, uint32_t count,
-                                int maxe, Counters* ctr, Deferred def, uint32_t slot_base)
+                                uint32_t per_warp, int maxe, Counters* ctr, Deferred def, uint32_t slot_base)
 {
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint32_t begin = (blockIdx.x * (blockDim.x >> 5) + wib) * kNMWarpVertices;
+    const uint32_t begin = (blockIdx.x * (blockDim.x >> 5) + wib) * per_warp;
     if (begin >= count) return;
-    const uint32_t end = min(begin + kNMWarpVertices, count);
+    const uint32_t end = min(begin + per_warp, count);
     nm_lockstep_plain<VAR>(m, crew, sp, members, begin, end, smem + wib * nm_warp_bytes(maxe), maxe, ctr, def,
                            slot_base, lane);
 }
@@ -102,10 +105,14 @@ static cudaError_t launch_nm_lockstep(const RelocLaunch& L)
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    const uint32_t per_block = kNMWarpVertices * kNMWarpsPerBlock;
-    const unsigned blocks = (L.count + per_block - 1) / per_block;
+    // enough warps for every SM to hold 16, then more vertices per warp
+    const uint64_t target_warps = (uint64_t)(L.sm_count > 0 ? L.sm_count : 152) * 16;
+    uint32_t per_warp = (uint32_t)((L.count + target_warps - 1) / target_warps);
+    per_warp = per_warp > 4u * kNMGroups ? 4u * kNMGroups : per_warp;
+    const uint64_t per_block = (uint64_t)per_warp * kNMWarpsPerBlock;
+    const unsigned blocks = (unsigned)((L.count + per_block - 1) / per_block);
     relocate_nm_lockstep_kernel<VAR><<<blocks, 32 * kNMWarpsPerBlock, smem, L.stream>>>(
-        L.m, L.crew, L.sp, L.members, L.count, L.maxe, L.ctr, L.def, L.slot_base);
+        L.m, L.crew, L.sp, L.members, L.count, per_warp, L.maxe, L.ctr, L.def, L.slot_base);
     return cudaGetLastError();
 }
 

@@ -141,13 +141,15 @@ class ServeStats:
     peak_active: int
     peak_bytes: int
     results: dict
+    phase_s: dict = dataclasses.field(default_factory=dict)  # host time by loop phase
 
     def summary(self) -> dict:
         lat = np.array(self.latencies_s) if self.latencies_s else np.zeros(1)
         return {"jobs": self.jobs, "relocations": self.relocations, "wall_s": round(self.wall_s, 3),
                 "relocations_per_s": self.relocations / max(self.wall_s, 1e-9),
                 "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-                "ticks": self.ticks, "peak_active_jobs": self.peak_active, "peak_device_bytes": self.peak_bytes}
+                "ticks": self.ticks, "peak_active_jobs": self.peak_active, "peak_device_bytes": self.peak_bytes,
+                "phase_s": {k: round(v, 4) for k, v in self.phase_s.items()}}
 
 
 class Server:
@@ -185,6 +187,7 @@ class Server:
         active: list[Job] = []
         lat, results = [], {}
         relocations, ticks, peak_active, peak_bytes, used = 0, 0, 0, 0, 0
+        phase = {"admit_s": 0.0, "batch_setup_s": 0.0, "pass_s": 0.0, "batch_close_s": 0.0, "retire_s": 0.0}
         i = 0
         t0 = time.perf_counter()
         busy = 0.0
@@ -201,6 +204,7 @@ class Server:
             # (a job is charged its template's footprint on admission and the
             # same amount is released when it retires, so the books balance
             # even though its per-pass buffers grow once it runs)
+            ta = time.perf_counter()
             while pending:
                 need = self.template(pending[0]).bytes
                 if active and used + need > self.budget:
@@ -209,6 +213,7 @@ class Server:
                 job.charged = max(need, job.device.device_bytes())
                 used += job.charged
                 active.append(job)
+            phase["admit_s"] += time.perf_counter() - ta
             peak_active = max(peak_active, len(active))
             peak_bytes = max(peak_bytes, used)
             # one pass of every active job: one batch per smoother
@@ -217,13 +222,20 @@ class Server:
                 jobs = [j for j in active if j.spec.smoother == sm]
                 if not jobs:
                     continue
+                t1 = time.perf_counter()
                 b = M.Batch([j.device for j in jobs])
+                t2 = time.perf_counter()
                 b.smooth_pass(sm, self.params[sm])
                 b.evaluate(0)
                 qs = b.read_quality(0)
                 if b.status() != 0:
                     raise RuntimeError("batched pass reported a dependency timeout")
+                t3 = time.perf_counter()
                 b.close()
+                t4 = time.perf_counter()
+                phase["batch_setup_s"] += t2 - t1
+                phase["pass_s"] += t3 - t2
+                phase["batch_close_s"] += t4 - t3
                 for j, q in zip(jobs, qs):
                     j.passes += 1
                     j.relocations += j.template.movable
@@ -235,6 +247,7 @@ class Server:
             busy += time.perf_counter() - tb
             ticks += 1
             still = []
+            tr = time.perf_counter()
             for j in active:
                 if j.done_at is None:
                     still.append(j)
@@ -246,6 +259,7 @@ class Server:
                                               "min": j.final_min, "mean": j.final_mean}
                 used -= j.charged
                 j.device.close()
+            phase["retire_s"] += time.perf_counter() - tr
             active = still
         wall = time.perf_counter() - t0
-        return ServeStats(len(stream), relocations, wall, busy, ticks, lat, peak_active, peak_bytes, results)
+        return ServeStats(len(stream), relocations, wall, busy, ticks, lat, peak_active, peak_bytes, results, phase)

@@ -80,16 +80,38 @@ def test_one_colour_metric_conformity_sphere():
         assert np.median(err) < 1e-5
 
 
+def oracle_sensitivity(raw, groups, crew, schedule, runs=4, seed=5):
+    """Spread of the FP64 oracle's final harmonic mean when its input moves
+    by one FP32 rounding (relative 2^-24 per coordinate, random sign): the
+    resolution at which a pass of this schedule is reproducible at all."""
+    base = raw.pos.astype(np.float32).astype(np.float64)
+    rng = np.random.default_rng(seed)
+    means = []
+    for _ in range(runs + 1):
+        orc = oracle_for(raw, crew)
+        orc.pos = base if not means else base * (1.0 + rng.choice([-1.0, 1.0], base.shape) * 2.0 ** -24)
+        for smoother, passes, params in schedule:
+            for _ in range(passes):
+                orc.smooth_pass(smoother, groups.group_base, groups.members, params=params, nthreads=4)
+        means.append(orc.evaluate()["mean"])
+    return means[0], max(abs(m - means[0]) for m in means[1:])
+
+
 def test_c1_nelder_mead_pass_quality():
-    """C1 (10^3-cell tet cube, NM 1 pass, workloads.NM_PARAMS): harmonic mean within 1e-4 of the FP64
-    oracle.  The minimum is set by one element; with these parameters an FP32
-    rounding two colours earlier sends one vertex of that element to another
-    optimum (min 0.6146 vs 0.6223 -- the same 0.6146 that an FP32 build of the
-    oracle reaches), so the min gate here is 1e-2."""
+    """C1 (10^3-cell tet cube, NM 1 pass, workloads.NM_PARAMS): the harmonic
+    mean within 1e-4 of the FP64 oracle, or within the oracle's own spread
+    under one-rounding input perturbations if that is wider.  With these
+    parameters (32 cycles, convergence 1e-4) the FP64 search itself is
+    chaotic at that level: a rounding in one vertex changes its neighbours'
+    starting patches in later colours and the searches end in nearby optima
+    (the oracle's mean moves by up to ~1.5e-4).  The minimum is set by one
+    element (min 0.6146 on FP32 inputs vs 0.6223 on FP64 inputs, the same
+    0.6146 that an FP32 build of the oracle reaches), so its gate is 1e-2."""
     w = workloads.WORKLOADS["C1"]
     raw, groups = coloured(w.mesh())
     gpos, opos, gq, oq, dev = run_both(raw, groups, w.crew(raw), w.schedule)
-    assert abs(gq["mean"] - oq["mean"]) <= 1e-4, (gq["mean"], oq["mean"])
+    ref, spread = oracle_sensitivity(raw, groups, w.crew(raw), w.schedule)
+    assert abs(gq["mean"] - ref) <= max(1e-4, 1.5 * spread), (gq["mean"], ref, spread)
     assert abs(gq["min"] - oq["min"]) <= 1e-2, (gq["min"], oq["min"])
     err = rel_err(raw, gpos, opos)
     assert np.median(err) < 1e-4 and np.mean(err < 1e-3) > 0.9
