@@ -80,7 +80,7 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="C5: arrival window")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="C5: mean arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0, help="C5: HBM admission budget")
-    ap.add_argument("--only", choices=["eval", "relocate", "batch"], default=None,
+    ap.add_argument("--only", choices=["eval", "eval_tet", "relocate", "batch"], default=None,
                     help="profiling driver: a few launches of one kernel family, no JSON line")
     return ap.parse_args()
 
@@ -231,13 +231,21 @@ def flops_per_elem(w, raw):
     return FLOPS_PER_ELEM_EVAL.get((w.evaluator, etype))
 
 
-def eval_roofline(torch, stream, hbm_peak, steps=10):
-    """HBM roofline of the evaluation kernel on the 128^3 hex mesh, L2 flushed
-    between launches: algorithmic bytes = 32 B/hex connectivity + 16 B/vertex."""
+def eval_roofline(torch, stream, hbm_peak, kind="hex", steps=10):
+    """HBM roofline of the evaluation kernel, L2 flushed between launches:
+    kind "hex" = the 128^3 hex mesh (C3: Gaussian jitter 0.15 h, seed 2),
+    algorithmic bytes = 32 B/hex connectivity + 16 B/vertex; kind "tet" =
+    the 128^3-cell tet cube (6 Kuhn tets per cell, jitter U(+-0.3 h), seed
+    0), 16 B/tet + 16 B/vertex.  Metric-free mean ratio."""
     from gpumesh_gb300 import mesh as M
     from gpumesh_gb300 import meshgen
 
-    raw = meshgen.box_mesh(128, "hex", 0.15, 2, gaussian=True)
+    if kind == "hex":
+        raw = meshgen.box_mesh(128, "hex", 0.15, 2, gaussian=True)
+        algo = raw.hexs.shape[0] * 32 + raw.nv * 16
+    else:
+        raw = meshgen.box_mesh(128, "tet", 0.3, 0)
+        algo = raw.tets.shape[0] * 16 + raw.nv * 16
     dev = M.DeviceMesh(raw, None)
     dev.set_stream(stream.cuda_stream)
     dev.set_crew("uniform", "metric_free", "mean_ratio")
@@ -253,14 +261,14 @@ def eval_roofline(torch, stream, hbm_peak, steps=10):
         b.record(stream)
         b.synchronize()
         times.append(a.elapsed_time(b) * 1e-3)
-    algo = raw.hexs.shape[0] * 32 + raw.nv * 16
     t = statistics.median(times)
     achieved = algo / t / 1e9
     h = dev.read_quality(0)
     dev.close()
-    return {"bound": "hbm", "kernel": "evaluate_kernel (mean ratio, 128^3 hexes)", "achieved": round(achieved, 1),
+    mesh = "128^3 hexes" if kind == "hex" else "128^3 x 6 tets"
+    return {"bound": "hbm", "kernel": f"evaluate_kernel (mean ratio, {mesh})", "achieved": round(achieved, 1),
             "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
-            "traffic": EVAL_HEX128_TRAFFIC_BYTES,
+            "traffic": EVAL_HEX128_TRAFFIC_BYTES if kind == "hex" else None,
             "algorithmic_bytes": algo, "us_per_launch": round(t * 1e6, 2),
             "min": h.minimumQuality(), "mean": h.harmonicMean(), "note": "of measured"}
 
@@ -452,7 +460,8 @@ def bench_gpu(args, rank, world, local):
         launches_per_step += sum(p for s, p, _ in w.schedule if s == "getme")
     line["gpu_launches"] = launches_per_step * args.steps
     if not args.no_eval_roofline and rank == 0:
-        line["roofline_eval"] = eval_roofline(torch, stream, hbm_peak)
+        line["roofline_eval"] = eval_roofline(torch, stream, hbm_peak, "hex")
+        line["roofline_eval_tet"] = eval_roofline(torch, stream, hbm_peak, "tet")
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, frac, n, t = cpu_sample_run(w, raw, groups, args.cpu_seconds, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
@@ -465,7 +474,8 @@ def bench_gpu(args, rank, world, local):
 
 def profile_driver(args):
     """A few launches of one kernel family, for ncu: `eval` = the evaluation
-    kernel on the 128^3 hex mesh (4 launches); `relocate` = one pass of each
+    kernel on the 128^3 hex mesh (4 launches), `eval_tet` = the same on the
+    128^3 x 6 tet cube; `relocate` = one pass of each
     smoother of the workload's schedule; `batch` = two batched Nelder-Mead
     passes over the first --batch-meshes meshes of C4."""
     import torch
@@ -473,8 +483,11 @@ def profile_driver(args):
     from gpumesh_gb300 import mesh as M
     from gpumesh_gb300 import meshgen, workloads
 
-    if args.only == "eval":
-        raw = meshgen.box_mesh(128, "hex", 0.15, 2, gaussian=True)
+    if args.only in ("eval", "eval_tet"):
+        if args.only == "eval":
+            raw = meshgen.box_mesh(128, "hex", 0.15, 2, gaussian=True)
+        else:
+            raw = meshgen.box_mesh(128, "tet", 0.3, 0)
         dev = M.DeviceMesh(raw, None)
         dev.set_crew("uniform", "metric_free", "mean_ratio")
         for _ in range(4):

@@ -454,20 +454,26 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchMesh* meshes
     const MeshView& m = meshes[eb.mesh].view;
     const Crew& crew = meshes[eb.mesh].crew;
     EvalAcc acc;
-    for (uint32_t i = eb.begin + threadIdx.x; i < eb.end; i += blockDim.x)
+    for (uint32_t base = eb.begin; base < eb.end; base += blockDim.x)  // block-uniform trip count
     {
-        int type;
-        uint32_t id;
-        if (MAXK == 4 || i < m.nt) { type = kTet; id = i; }
-        else if (i < m.nt + m.np) { type = kPri; id = i - m.nt; }
-        else { type = kHex; id = i - m.nt - m.np; }
-        uint32_t vid[8];
-        elem_vertices(m, type, id, vid);
-        V3<float> p[MAXK];
-        const int n = MAXK == 4 ? 4 : type_size(type);
+        const uint32_t i = base + threadIdx.x;
+        int b = -1;
+        if (i < eb.end)
+        {
+            int type;
+            uint32_t id;
+            if (MAXK == 4 || i < m.nt) { type = kTet; id = i; }
+            else if (i < m.nt + m.np) { type = kPri; id = i - m.nt; }
+            else { type = kHex; id = i - m.nt - m.np; }
+            uint32_t vid[8];
+            elem_vertices(m, type, id, vid);
+            V3<float> p[MAXK];
+            const int n = MAXK == 4 ? 4 : type_size(type);
 #pragma unroll
-        for (int k = 0; k < MAXK; ++k) p[k] = to<float>(__ldg(&m.pos[vid[k < n ? k : 0]]));
-        acc.add(elem_quality<VAR, MAXK, float>(crew, type, p), hist);
+            for (int k = 0; k < MAXK; ++k) p[k] = to<float>(__ldg(&m.pos[vid[k < n ? k : 0]]));
+            b = acc.add(elem_quality<VAR, MAXK, float>(crew, type, p));
+        }
+        hist_add_warp(hist, b);
     }
     double ds = acc.rs;
     float mn = acc.min_quality();

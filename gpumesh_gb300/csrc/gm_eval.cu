@@ -14,10 +14,17 @@
 namespace gm {
 
 constexpr int kEvalThreads = 256;
+constexpr int kEvalUnroll = 1;  // elements per thread per iteration of the single-type streams
+// resident blocks per SM the register allocation aims for: the gather
+// streams are latency bound, so they trade registers for resident warps
+template <int VAR, int SET>
+constexpr int kEvalMinBlocks = VAR == kVarMRFree ? (SET == 9 ? 4 : SET == 4 ? 6 : 1)
+                               : VAR == kVarMCDiag ? (SET == 4 ? 4 : 1) : 1;
 
 // SET: 4 = tets only, 8 = any element types, 9 = hexes only
+// returns the element's histogram bucket
 template <int VAR, int SET>
-__device__ __forceinline__ void eval_element(const MeshView& m, const Crew& crew, uint32_t i, EvalAcc& acc, int* hist)
+__device__ __forceinline__ int eval_element(const MeshView& m, const Crew& crew, uint32_t i, EvalAcc& acc)
 {
     constexpr int MAXK = SET == 4 ? 4 : 8;
     int type;
@@ -55,10 +62,11 @@ __device__ __forceinline__ void eval_element(const MeshView& m, const Crew& crew
 #pragma unroll
         for (int k = 0; k < MAXK; ++k) p[k] = to<float>(__ldg(&m.pos[vid[k < n ? k : 0]]));
     }
-    EQ<float> q = SET == 9 ? (VarTraits<VAR>::mean_ratio ? mr_hex<VAR, float>(crew, p)
-                                                          : elem_quality<VAR, MAXK, float>(crew, kHex, p))
-                           : elem_quality<VAR, MAXK, float>(crew, type, p);
-    acc.add(q, hist);
+    EQ<float> q;
+    if constexpr (SET == 9 && VAR == kVarMRFree) q = mr_hex_fast(p);
+    else if constexpr (SET == 9) q = elem_quality<VAR, MAXK, float>(crew, kHex, p);
+    else q = elem_quality<VAR, MAXK, float>(crew, type, p);
+    return acc.add(q);
 }
 
 constexpr int kEvalWarps = kEvalThreads / 32;
@@ -95,22 +103,143 @@ __device__ __forceinline__ void block_reduce(double& sum, float& mn, int& bad, d
 // all partials in a fixed order and writes the Quality, so the result does
 // not depend on which block finishes last.  atomicInc wraps the ticket back
 // to 0, so the scratch is ready for the next launch.
+struct EvalShared
+{
+    int hist[20];
+    float wmin[kEvalWarps];
+    double wsum[kEvalWarps];
+    int wbad[kEvalWarps];
+    unsigned int whist[kEvalWarps][20];
+    bool last;
+};
+
+__device__ __forceinline__ void eval_prologue(EvalShared& sh)
+{
+    if (threadIdx.x < 20) sh.hist[threadIdx.x] = 0;
+    __syncthreads();
+}
+
+// the block's partial, then (last block only) the final reduction
+__device__ __noinline__ void eval_epilogue(const EvalAcc& acc, EvalShared& sh, EvalPartial* parts, Quality* out,
+                                              uint32_t total);
+
+// connectivity of a tet (SET 4) or a hex (SET 9): 1 or 2 uint4
+template <int SET>
+struct Conn
+{
+    uint4 a, b;
+};
+
+template <int SET>
+__device__ __forceinline__ Conn<SET> load_conn(const MeshView& m, uint32_t i)
+{
+    Conn<SET> c;
+    if (SET == 9)
+    {
+        c.a = __ldg(&m.hexs[2 * (size_t)i]);
+        c.b = __ldg(&m.hexs[2 * (size_t)i + 1]);
+    }
+    else
+    {
+        c.a = __ldg(&m.tets[i]);
+        c.b = c.a;
+    }
+    return c;
+}
+
+// quality of a tet or hex from its connectivity; returns the bucket
 template <int VAR, int SET>
-__global__ void __launch_bounds__(kEvalThreads) evaluate_kernel(MeshView m, Crew crew, EvalPartial* parts,
+__device__ __forceinline__ int eval_conn(const MeshView& m, const Crew& crew, const Conn<SET>& c, EvalAcc& acc)
+{
+    constexpr int MAXK = SET == 4 ? 4 : 8;
+    V3<float> p[MAXK];
+    p[0] = to<float>(__ldg(&m.pos[c.a.x]));
+    p[1] = to<float>(__ldg(&m.pos[c.a.y]));
+    p[2] = to<float>(__ldg(&m.pos[c.a.z]));
+    p[3] = to<float>(__ldg(&m.pos[c.a.w]));
+    if constexpr (SET == 9)
+    {
+        p[4] = to<float>(__ldg(&m.pos[c.b.x]));
+        p[5] = to<float>(__ldg(&m.pos[c.b.y]));
+        p[6] = to<float>(__ldg(&m.pos[c.b.z]));
+        p[7] = to<float>(__ldg(&m.pos[c.b.w]));
+    }
+    EQ<float> q;
+    if constexpr (SET == 9 && VAR == kVarMRFree) q = mr_hex_fast(p);
+    else if constexpr (SET == 9) q = elem_quality<VAR, MAXK, float>(crew, kHex, p);
+    else q = elem_quality<VAR, MAXK, float>(crew, kTet, p);
+    return acc.add(q);
+}
+
+template <int VAR, int SET>
+__global__ void __launch_bounds__(kEvalThreads, kEvalMinBlocks<VAR, SET>) evaluate_kernel(MeshView m, Crew crew, EvalPartial* parts,
                                                                 Quality* out)
 {
-    __shared__ int hist[20];
-    __shared__ float wmin[kEvalWarps];
-    __shared__ double wsum[kEvalWarps];
-    __shared__ int wbad[kEvalWarps];
-    __shared__ unsigned int whist[kEvalWarps][20];
-    __shared__ bool last;
-    if (threadIdx.x < 20) hist[threadIdx.x] = 0;
-    __syncthreads();
+    __shared__ EvalShared sh;
+    eval_prologue(sh);
     EvalAcc acc;
     const uint32_t total = m.nt + m.np + m.nh;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
-        eval_element<VAR, SET>(m, crew, i, acc, hist);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    if constexpr (SET == 4 || SET == 9)
+    {
+        // single-type stream: U elements per thread per iteration (independent
+        // gather chains), and their successors' connectivity loaded one
+        // iteration ahead, so only the position gathers (mostly L2 hits) are
+        // on each iteration's critical path.  (U = 2 measured no faster: the
+        // gathers are limited by L1 wavefronts, ~9 per warp-wide gather.)
+        constexpr int U = kEvalUnroll;
+        const uint32_t step = stride * U;
+        uint32_t base = blockIdx.x * blockDim.x * U;
+        Conn<SET> cur[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (base + u * blockDim.x + threadIdx.x < total) cur[u] = load_conn<SET>(m, base + u * blockDim.x + threadIdx.x);
+        for (; base < total; base += step)  // block-uniform trip count
+        {
+            Conn<SET> next[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+            {
+                const uint32_t nxt = base + step + u * blockDim.x + threadIdx.x;
+                next[u] = cur[u];
+                if (nxt < total) next[u] = load_conn<SET>(m, nxt);
+            }
+            int b[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+            {
+                const uint32_t i = base + u * blockDim.x + threadIdx.x;
+                b[u] = i < total ? eval_conn<VAR, SET>(m, crew, cur[u], acc) : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+            {
+                hist_add_warp(sh.hist, b[u]);
+                cur[u] = next[u];
+            }
+        }
+    }
+    else
+    {
+        // block-uniform trip count, so every lane takes part in the histogram vote
+        for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += stride)
+        {
+            const uint32_t i = base + threadIdx.x;
+            hist_add_warp(sh.hist, i < total ? eval_element<VAR, SET>(m, crew, i, acc) : -1);
+        }
+    }
+    eval_epilogue(acc, sh, parts, out, total);
+}
+
+__device__ __noinline__ void eval_epilogue(const EvalAcc& acc, EvalShared& sh, EvalPartial* parts, Quality* out,
+                                              uint32_t total)
+{
+    int* hist = sh.hist;
+    float* wmin = sh.wmin;
+    double* wsum = sh.wsum;
+    int* wbad = sh.wbad;
+    auto& whist = sh.whist;
+    bool& last = sh.last;
     double sum = acc.rs;
     float mn = acc.min_quality();
     int bad = acc.nbad;
@@ -178,11 +307,31 @@ int evaluate_blocks(uint32_t total, int sm_count)
     return n < 1 ? 1 : (int)n;
 }
 
+// nblocks is the partial buffer's capacity; the grid is one wave: the
+// kernel's resident blocks per SM times the SMs, or fewer for a small mesh
 template <int VAR, int SET>
 static void launch_eval_t(const MeshView& m, const Crew& crew, EvalPartial* parts, int nblocks, Quality* out,
                           cudaStream_t s)
 {
-    evaluate_kernel<VAR, SET><<<nblocks, kEvalThreads, 0, s>>>(m, crew, parts, out);
+    static int per_sm = 0, sms = 0;
+    if (per_sm == 0)
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, evaluate_kernel<VAR, SET>, kEvalThreads, 0) !=
+                cudaSuccess || per_sm < 1)
+        {
+            per_sm = 8;
+            sms = 152;
+        }
+    }
+    const uint32_t total = m.nt + m.np + m.nh;
+    const long per_block = (long)kEvalThreads * kEvalUnroll;  // elements a block covers per iteration
+    long grid = ((long)total + per_block - 1) / per_block;
+    grid = grid < (long)per_sm * sms ? grid : (long)per_sm * sms;
+    grid = grid < nblocks ? grid : nblocks;
+    evaluate_kernel<VAR, SET><<<(unsigned)(grid < 1 ? 1 : grid), kEvalThreads, 0, s>>>(m, crew, parts, out);
 }
 
 cudaError_t launch_evaluate(int variant, int maxk, const MeshView& m, const Crew& crew, EvalPartial* parts,

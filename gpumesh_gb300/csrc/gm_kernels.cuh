@@ -73,7 +73,8 @@ struct EvalAcc
     float rmax = 0.f;
     float bmin = 1.0f;
     int nbad = 0;
-    __device__ __forceinline__ void add(const EQ<float>& q, int* hist)
+    // returns the element's bucket
+    __device__ __forceinline__ int add(const EQ<float>& q)
     {
         float qv;
         if (q.pos)
@@ -88,10 +89,19 @@ struct EvalAcc
             bmin = fminf(bmin, q.v);
             qv = q.v;
         }
-        atomicAdd(&hist[qv > 0.f ? min((int)(qv * 20.f), 19) : 0], 1);
+        return qv > 0.f ? min((int)(qv * 20.f), 19) : 0;
     }
     __device__ __forceinline__ float min_quality() const { return nbad ? bmin : fminf(1.0f, __frcp_rn(rmax)); }
 };
+
+// Add each lane's bucket b (-1: no element) to a shared histogram; lanes
+// with the same bucket are counted by one atomic.  Every lane of the warp
+// must call it.
+__device__ __forceinline__ void hist_add_warp(int* hist, int b)
+{
+    const unsigned same = __match_any_sync(0xffffffffu, b);
+    if (b >= 0 && (threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&hist[b], __popc(same));
+}
 
 // relocation parameters (the reference's file-scope constants, now runtime)
 struct SmoothParams
