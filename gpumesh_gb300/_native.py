@@ -101,6 +101,11 @@ def lib():
         "gm_batch_inject_stall": [vp, u32],
         "gm_batch_counters": [vp, vp, i32],
         "gm_batch_info": [vp, vp],
+        "gm_mesh_upload_gpu_verts_async": [vp, u32, vp],
+        "gm_job_prepare": [vp, i32, vp, u32, ctypes.c_double],
+        "gm_job_launch": [vp],
+        "gm_job_query": [vp, vp],
+        "gm_job_result": [vp, vp, vp, vp],
         "gm_batch_latencies": [vp, vp],
         "gm_evaluate_noalloc": [u32, vp, u32, vp, u32, vp, u32, vp, i32, i32, i32, ctypes.c_double,
                                 ctypes.c_double, vp, vp],

@@ -206,6 +206,78 @@ void relocate_group(gm_mesh* m, int smoother, const SmoothParams& sp, uint32_t b
     GM_CUDA(launch_accept(L));
 }
 
+// one relocation pass: every colour in order (GETMe: the element pass first)
+void enqueue_pass(gm_mesh* m, int smoother, const SmoothParams& sp)
+{
+    ensure_deferred(m);
+    size_t ng = m->group_base.size() - 1;
+    GM_CUDA(cudaMemsetAsync(m->def_count.p, 0, (ng + 2) * sizeof(uint32_t), m->stream));
+    if (smoother == GM_SMOOTH_GETME)
+    {
+        m->corners.reserve(4 * (size_t)m->nt + 6 * (size_t)m->np + 8 * (size_t)m->nh);
+        GM_CUDA(launch_getme_elements(m->element_variant(), m->view(), m->crew, sp.lambda, m->corners.p, m->sm_count,
+                                      m->stream));
+    }
+    for (size_t g = 0; g < ng; ++g)
+        relocate_group(m, smoother, sp, m->group_base[g], m->group_base[g + 1] - m->group_base[g], (uint32_t)g);
+}
+
+// at least n quality slots, keeping the recorded ones (synchronises on growth)
+void ensure_quality_slots(gm_mesh* m, uint32_t n)
+{
+    if (n <= m->n_quality_slots) return;
+    n = std::max<uint32_t>(n, 2 * m->n_quality_slots);
+    Quality* fresh = nullptr;
+    GM_CUDA(cudaMalloc(&fresh, n * sizeof(Quality)));
+    if (m->quality.p && m->n_quality_slots)
+        GM_CUDA(cudaMemcpyAsync(fresh, m->quality.p, m->n_quality_slots * sizeof(Quality), cudaMemcpyDeviceToDevice,
+                                m->stream));
+    GM_CUDA(cudaStreamSynchronize(m->stream));
+    m->quality.release();
+    m->quality.p = fresh;
+    m->quality.cap = n;
+    m->n_quality_slots = n;
+}
+
+// one evaluation into `out` (device)
+void enqueue_evaluate(gm_mesh* m, Quality* out)
+{
+    uint32_t total = m->nt + m->np + m->nh;
+    int nb = evaluate_blocks(total, m->sm_count);
+    if (m->parts.reserve(nb))  // a fresh scratch starts with its ticket at 0
+        GM_CUDA(cudaMemsetAsync(m->parts.p, 0, sizeof(EvalPartial), m->stream));
+    GM_CUDA(launch_evaluate(m->variant(), m->elem_set(), m->view(), m->crew, m->parts.p, nb, out, m->stream));
+}
+
+void drop_job(gm_mesh* m)
+{
+    if (m->job_exec) cudaGraphExecDestroy(m->job_exec);
+    if (m->job_graph) cudaGraphDestroy(m->job_graph);
+    m->job_exec = nullptr;
+    m->job_graph = nullptr;
+    m->job_max_passes = 0;
+}
+
+// The stop test of a device-resident job, one warp: store the evaluation of
+// the pass just run in the next slot, count the pass, and continue while
+// fewer than max_passes passes are done and the minimum quality rose by at
+// least min_gain (the served workload's stop rule).
+__global__ void job_rule_kernel(Quality* slots, const Quality* fresh, int* counter, double min_gain, int max_passes,
+                                cudaGraphConditionalHandle loop)
+{
+    const int lane = threadIdx.x;
+    const int c = __shfl_sync(0xffffffffu, lane == 0 ? *counter + 1 : 0, 0);
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(fresh);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(slots + c);
+    if (lane < (int)(sizeof(Quality) / 8)) dst[lane] = src[lane];
+    if (lane == 0)
+    {
+        *counter = c;
+        const double gain = fresh->min - slots[c - 1].min;
+        cudaGraphSetConditional(loop, (c < max_passes && gain >= min_gain) ? 1u : 0u);
+    }
+}
+
 }  // namespace
 
 namespace gm {
@@ -287,6 +359,9 @@ gm_status gm_mesh_destroy(gm_mesh* m)
     return guarded([&] {
         if (!m) return;
         cudaStreamSynchronize(m->stream);
+        drop_job(m);
+        m->job_counter.release();
+        m->job_fresh.release();
         m->pos.release();
         m->tets.release();
         m->pris.release();
@@ -332,6 +407,7 @@ gm_status gm_mesh_upload(gm_mesh* m, uint32_t nv, const double* xyz, const int32
 {
     return guarded([&] {
         require(m && xyz && cid && nv > 0, "null argument");
+        drop_job(m);
         require((nt == 0 || tets) && (np == 0 || pris) && (nh == 0 || hexs), "null connectivity");
         require((uint64_t)nt + np + nh <= kMaxElemId, "too many elements");
         check_conn(tets, (size_t)nt * 4, nv, "tet");
@@ -382,11 +458,21 @@ gm_status gm_mesh_upload_gpu_verts(gm_mesh* m, uint32_t nv, const void* gpu_vert
     });
 }
 
+gm_status gm_mesh_upload_gpu_verts_async(gm_mesh* m, uint32_t nv, const void* gpu_verts)
+{
+    return guarded([&] {
+        require(m && gpu_verts, "null argument");
+        require(m->nv == nv && m->pos.p && m->pos.cap >= nv, "vertex count differs from the uploaded vertices");
+        GM_CUDA(cudaMemcpyAsync(m->pos.p, gpu_verts, (size_t)nv * sizeof(float4), cudaMemcpyHostToDevice, m->stream));
+    });
+}
+
 #define GM_UPLOAD_ELEMS(NAME, K, FIELD, COUNT, VEC)                                                       \
     gm_status NAME(gm_mesh* m, uint32_t n, const uint32_t* words, uint32_t stride)                       \
     {                                                                                                    \
         return guarded([&] {                                                                             \
             require(m && (n == 0 || words), "null argument");                                            \
+            drop_job(m);                                                                                 \
             std::vector<uint32_t> packed;                                                                \
             upload_conn<K>(m, n, words, stride, packed);                                                 \
             if (m->nv) check_conn(packed.data(), packed.size(), m->nv, #FIELD);                          \
@@ -406,6 +492,7 @@ gm_status gm_mesh_upload_topo(gm_mesh* m, uint32_t nv, const int32_t* topo5, uin
 {
     return guarded([&] {
         require(m && topo5 && (n_nv == 0 || neig_verts) && (n_ne == 0 || neig_elems3), "null argument");
+        drop_job(m);
         require(m->nv == 0 || m->nv == nv, "vertex count differs from the uploaded vertices");
         std::vector<int32_t> cid(nv);
         std::vector<uint32_t> ve_off((size_t)nv + 1, 0), vv_off((size_t)nv + 1, 0), ve, vv;
@@ -444,6 +531,7 @@ gm_status gm_mesh_upload_groups(gm_mesh* m, uint32_t n_members, const uint32_t* 
 {
     return guarded([&] {
         require(m && (n_members == 0 || members) && group_base, "null argument");
+        drop_job(m);
         require(group_base[0] == 0 && group_base[ngroups] == n_members, "group bases must span the members");
         for (uint32_t g = 0; g < ngroups; ++g) require(group_base[g] <= group_base[g + 1], "group bases must ascend");
         for (uint32_t i = 0; i < n_members; ++i) require(members[i] < m->nv, "group member out of range");
@@ -458,6 +546,7 @@ gm_status gm_mesh_set_constraints(gm_mesh* m, uint32_t n, const int32_t* kind, c
 {
     return guarded([&] {
         require(m && kind && params && n > 0, "null argument");
+        drop_job(m);
         std::vector<Constraint> table(n);
         for (uint32_t i = 0; i < n; ++i)
         {
@@ -505,6 +594,7 @@ gm_status gm_mesh_set_crew(gm_mesh* m, int32_t sampler, int32_t measurer, int32_
 {
     return guarded([&] {
         require(m != nullptr, "null mesh");
+        drop_job(m);
         set_crew(m, sampler, measurer, evaluator, scaling, aspect_ratio);
     });
 }
@@ -514,6 +604,7 @@ gm_status gm_mesh_clone(gm_mesh* dst, const gm_mesh* src)
     return guarded([&] {
         require(dst && src && dst != src, "invalid argument");
         require(src->nv > 0 && src->cid.p, "source mesh has no topology");
+        drop_job(dst);
         cudaStream_t s = dst->stream;
         GM_CUDA(cudaStreamSynchronize(src->stream));
         auto copy = [&](auto& d, const auto& from, size_t n) {
@@ -615,25 +706,10 @@ gm_status gm_evaluate_async(gm_mesh* m, uint32_t slot)
         require(slot < 65536, "quality slot out of range");
         if (slot >= m->n_quality_slots)
         {
-            // grow, keeping the recorded slots
-            uint32_t n = std::max<uint32_t>(slot + 1, 2 * m->n_quality_slots);
-            Quality* fresh = nullptr;
-            GM_CUDA(cudaMalloc(&fresh, n * sizeof(Quality)));
-            if (m->quality.p && m->n_quality_slots)
-                GM_CUDA(cudaMemcpyAsync(fresh, m->quality.p, m->n_quality_slots * sizeof(Quality),
-                                        cudaMemcpyDeviceToDevice, m->stream));
-            GM_CUDA(cudaStreamSynchronize(m->stream));
-            m->quality.release();
-            m->quality.p = fresh;
-            m->quality.cap = n;
-            m->n_quality_slots = n;
+            if (m->job_exec) drop_job(m);  // the job graph captured the old slots
+            ensure_quality_slots(m, slot + 1);
         }
-        uint32_t total = m->nt + m->np + m->nh;
-        int nb = evaluate_blocks(total, m->sm_count);
-        if (m->parts.reserve(nb))  // a fresh scratch starts with its ticket at 0
-            GM_CUDA(cudaMemsetAsync(m->parts.p, 0, sizeof(EvalPartial), m->stream));
-        GM_CUDA(launch_evaluate(m->variant(), m->elem_set(), m->view(), m->crew, m->parts.p, nb, m->quality.p + slot,
-                                m->stream));
+        enqueue_evaluate(m, m->quality.p + slot);
     });
 }
 
@@ -700,17 +776,10 @@ gm_status gm_smooth_pass(gm_mesh* m, int32_t smoother, const double* params)
         require_mesh(m);
         require_groups(m);
         SmoothParams sp = parse_params(smoother, params);
-        ensure_deferred(m);
-        size_t ng = m->group_base.size() - 1;
-        GM_CUDA(cudaMemsetAsync(m->def_count.p, 0, (ng + 2) * sizeof(uint32_t), m->stream));
-        if (smoother == GM_SMOOTH_GETME)
-        {
-            m->corners.reserve(4 * (size_t)m->nt + 6 * (size_t)m->np + 8 * (size_t)m->nh);
-            GM_CUDA(launch_getme_elements(m->element_variant(), m->view(), m->crew, sp.lambda, m->corners.p,
-                                          m->sm_count, m->stream));
-        }
-        for (size_t g = 0; g < ng; ++g)
-            relocate_group(m, smoother, sp, m->group_base[g], m->group_base[g + 1] - m->group_base[g], (uint32_t)g);
+        if (smoother == GM_SMOOTH_GETME && m->job_exec &&
+            m->corners.cap < 4 * (size_t)m->nt + 6 * (size_t)m->np + 8 * (size_t)m->nh)
+            drop_job(m);  // the corner buffer is about to be allocated
+        enqueue_pass(m, smoother, sp);
     });
 }
 
@@ -727,6 +796,120 @@ gm_status gm_mesh_counters(gm_mesh* m, uint64_t* out5, int32_t reset)
         out5[3] = c.elem_evals[3];
         out5[4] = c.fp64_vertices;
         if (reset) GM_CUDA(cudaMemsetAsync(m->ctr.p, 0, sizeof(Counters), m->stream));
+    });
+}
+
+// ---- device-resident jobs ----
+// The graph: a conditional WHILE node whose body is one relocation pass, one
+// evaluation into job_fresh, and job_rule_kernel, which files the evaluation
+// in the next quality slot and sets the loop condition.  gm_job_launch puts
+// the counter reset and the first evaluation (slot 0) in front of it.
+gm_status gm_job_prepare(gm_mesh* m, int32_t smoother, const double* params, uint32_t max_passes, double min_gain)
+{
+    return guarded([&] {
+        require_mesh(m);
+        require_groups(m);
+        require(max_passes >= 1 && max_passes < 65535, "max_passes out of range");
+        drop_job(m);
+        const SmoothParams sp = parse_params(smoother, params);
+        // allocate everything the graph refers to before capturing it, and run
+        // one evaluation so that the launch configuration is cached
+        ensure_deferred(m);
+        if (smoother == GM_SMOOTH_GETME)
+            m->corners.reserve(4 * (size_t)m->nt + 6 * (size_t)m->np + 8 * (size_t)m->nh);
+        ensure_quality_slots(m, max_passes + 1);
+        m->job_counter.reserve(1);
+        m->job_fresh.reserve(1);
+        enqueue_evaluate(m, m->job_fresh.p);
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+
+        cudaGraph_t g = nullptr;
+        GM_CUDA(cudaGraphCreate(&g, 0));
+        cudaGraphConditionalHandle loop;
+        cudaError_t e = cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams p{};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = loop;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p);
+        if (e == cudaSuccess)
+            e = cudaStreamBeginCaptureToGraph(m->stream, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess)
+        {
+            cudaGraphDestroy(g);
+            throw ApiError(GM_ERR_CUDA, std::string("job graph: ") + cudaGetErrorString(e));
+        }
+        try
+        {
+            enqueue_pass(m, smoother, sp);
+            enqueue_evaluate(m, m->job_fresh.p);
+            job_rule_kernel<<<1, 32, 0, m->stream>>>(m->quality.p, m->job_fresh.p, m->job_counter.p, min_gain,
+                                                     (int)max_passes, loop);
+            GM_CUDA(cudaGetLastError());
+        }
+        catch (...)
+        {
+            cudaGraph_t body = nullptr;
+            cudaStreamEndCapture(m->stream, &body);
+            cudaGraphDestroy(g);
+            throw;
+        }
+        cudaGraph_t body = nullptr;
+        e = cudaStreamEndCapture(m->stream, &body);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&m->job_exec, g, 0);
+        if (e != cudaSuccess)
+        {
+            cudaGraphDestroy(g);
+            m->job_exec = nullptr;
+            throw ApiError(GM_ERR_CUDA, std::string("job graph: ") + cudaGetErrorString(e));
+        }
+        m->job_graph = g;
+        m->job_max_passes = max_passes;
+    });
+}
+
+gm_status gm_job_launch(gm_mesh* m)
+{
+    return guarded([&] {
+        require(m && m->job_exec, "no job prepared on this mesh");
+        GM_CUDA(cudaMemsetAsync(m->job_counter.p, 0, sizeof(int), m->stream));
+        enqueue_evaluate(m, m->quality.p);
+        GM_CUDA(cudaGraphLaunch(m->job_exec, m->stream));
+    });
+}
+
+gm_status gm_job_query(gm_mesh* m, int32_t* done)
+{
+    return guarded([&] {
+        require(m && done, "null argument");
+        cudaError_t e = cudaStreamQuery(m->stream);
+        if (e == cudaErrorNotReady)
+        {
+            *done = 0;
+            return;
+        }
+        GM_CUDA(e);
+        *done = 1;
+    });
+}
+
+gm_status gm_job_result(gm_mesh* m, uint32_t* passes, gm_quality* first, gm_quality* last)
+{
+    return guarded([&] {
+        require(m && m->job_exec && passes, "no job prepared on this mesh");
+        int c = 0;
+        GM_CUDA(cudaMemcpyAsync(&c, m->job_counter.p, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+        require(c >= 0 && (uint32_t)c <= m->job_max_passes, "job counter out of range");
+        *passes = (uint32_t)c;
+        if (first)
+            GM_CUDA(cudaMemcpyAsync(first, m->quality.p, sizeof(Quality), cudaMemcpyDeviceToHost, m->stream));
+        if (last)
+            GM_CUDA(cudaMemcpyAsync(last, m->quality.p + c, sizeof(Quality), cudaMemcpyDeviceToHost, m->stream));
+        GM_CUDA(cudaStreamSynchronize(m->stream));
     });
 }
 

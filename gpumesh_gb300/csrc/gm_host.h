@@ -133,6 +133,14 @@ struct gm_mesh
     int maxe = 32;
     int warps_per_block = 4;
     std::vector<float4> staging;  // host conversion buffer
+    // device-resident job (gm_job_*): a CUDA graph running a whole stop-rule
+    // schedule; it captures the buffers and crew above, so anything that
+    // changes them drops it
+    cudaGraph_t job_graph = nullptr;
+    cudaGraphExec_t job_exec = nullptr;
+    DBuf<int> job_counter;    // passes done
+    DBuf<Quality> job_fresh;  // evaluation of the pass just run
+    uint32_t job_max_passes = 0;
 
     MeshView view() const
     {

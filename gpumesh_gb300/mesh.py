@@ -305,6 +305,26 @@ class DeviceMesh:
         N.check(N.lib().gm_mesh_device_bytes(self.h, ctypes.byref(b)))
         return int(b.value)
 
+    # device-resident job: the whole stop-rule schedule as one graph launch
+    def job_prepare(self, smoother: str, params=None, max_passes: int = 20, min_gain: float = 1e-3):
+        p = N.params_array(params)
+        N.check(N.lib().gm_job_prepare(self.h, N.SMOOTHERS[smoother], N.ptr(p), int(max_passes), float(min_gain)))
+
+    def job_launch(self):
+        N.check(N.lib().gm_job_launch(self.h))
+
+    def job_done(self) -> bool:
+        d = ctypes.c_int32()
+        N.check(N.lib().gm_job_query(self.h, ctypes.byref(d)))
+        return bool(d.value)
+
+    def job_result(self):
+        """(passes run, quality before the first pass, quality after the last)"""
+        n = ctypes.c_uint32()
+        first, last = N.Quality(), N.Quality()
+        N.check(N.lib().gm_job_result(self.h, ctypes.byref(n), ctypes.byref(first), ctypes.byref(last)))
+        return int(n.value), QualityHistogram.from_native(first), QualityHistogram.from_native(last)
+
     def save_positions(self):
         N.check(N.lib().gm_mesh_save_positions(self.h))
 
@@ -314,6 +334,11 @@ class DeviceMesh:
     def upload_gpu_verts(self, buf: np.ndarray):
         """positions in the reference's GpuVert layout (float x, y, z, uint c)"""
         N.check(N.lib().gm_mesh_upload_gpu_verts(self.h, self.nv, N.ptr(buf)))
+
+    def upload_gpu_verts_async(self, buf: np.ndarray):
+        """GpuVert positions from pinned host memory, asynchronous on the mesh's
+        stream: keep `buf` unchanged until the stream has passed the copy"""
+        N.check(N.lib().gm_mesh_upload_gpu_verts_async(self.h, self.nv, N.ptr(buf)))
 
     def fetch_gpu_verts(self, buf: np.ndarray):
         N.check(N.lib().gm_mesh_fetch_gpu_verts(self.h, self.nv, N.ptr(buf)))

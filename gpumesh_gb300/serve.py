@@ -1,4 +1,4 @@
-"""Served smoothing: a continuous-batching request loop.
+"""Served smoothing: a continuous request loop over device-resident jobs.
 
 Jobs arrive over time (a Poisson stream).  Each job is a jittered cube or
 sphere tet mesh with its own seed and a smoother (Nelder-Mead, gradient
@@ -7,19 +7,20 @@ drops below a threshold or a pass cap is reached (the stop rule of the
 served workload; the reference's autopilot compares mean and min gains,
 Smoothers/AbstractSmoother.cpp:182-193).
 
-The loop works in ticks.  At each tick it admits arrived jobs while their
-device footprint fits the HBM budget, then runs ONE pass for every active
-job: the active jobs of each smoother form a gm_batch relocated by one
-persistent launch and evaluated per mesh by one launch.  Jobs join and
-leave between ticks, so requests that arrive while others are on the GPU
-share the next launches with them, and every job's mesh stays resident on
-the device from admission to completion.
+Each job runs as ONE launch of a CUDA graph (gm_job_*): the evaluation,
+then a conditional loop of (relocation pass, evaluation, stop test) that the
+device drives, on the job's own stream.  Jobs that arrive while others are
+on the GPU are admitted as soon as a slot (a stream) and HBM budget are
+free, and their kernels overlap with the running jobs' on the device, so a
+small job finishes in its own service time instead of waiting for the
+passes of larger ones.  The host only admits, launches and polls.
 
-Job meshes reuse resident topology templates: all jobs of one (kind, cells
-per axis) share the connectivity, constraints and colouring, which are
-built once; a job is a device-to-device clone of its template plus its own
-positions, identical to what meshgen.box_mesh / sphere_mesh produce for the
-job's seed.
+Job meshes come from resident slots: a slot is a device mesh of one
+(kind, cells per axis) with its prepared job graph for one smoother, cloned
+once from a topology template (connectivity, constraints, colouring built
+once per (kind, n)); a job uploads only its own positions into a free slot
+of its key.  Finished jobs return their slot to the pool; idle slots are
+freed when the HBM budget needs room.
 """
 
 from __future__ import annotations
@@ -107,27 +108,48 @@ class Template:
         self.bytes = self.device.device_bytes()
 
     def positions(self, seed: int) -> np.ndarray:
+        """The job's positions as float32 GpuVert records (x, y, z, 0)."""
         if self.kind == "cube":
             p = meshgen.box_positions(self.n, 0.3, seed)
         else:
             p = meshgen.sphere_positions(self.n, 0.25, seed, self.layout)
-        return np.ascontiguousarray(p[self.perm])
+        out = np.zeros((p.shape[0], 4), np.float32)
+        out[:, :3] = p[self.perm]
+        return out
+
+
+class Slot:
+    """A device mesh of one template on its own stream, with the job graph
+    of one smoother prepared."""
+
+    def __init__(self, template: Template, smoother: str, params, max_passes: int, min_gain: float):
+        import torch
+
+        self.template = template
+        self.stream = torch.cuda.Stream()
+        self.device = M.DeviceMesh(None, stream=self.stream.cuda_stream, clone_of=template.device)
+        self.device.job_prepare(smoother, params, max_passes, min_gain)
+        self.bytes = self.device.device_bytes()
+        # pinned staging of the job's positions: the upload is asynchronous,
+        # and the slot's next job reuses the buffer only after this one ends
+        self._pinned = torch.empty((template.raw.nv, 4), dtype=torch.float32, pin_memory=True)
+        self.pinned = self._pinned.numpy()
+
+    def launch(self, payload: np.ndarray):
+        np.copyto(self.pinned, payload)
+        self.device.upload_gpu_verts_async(self.pinned)
+        self.device.job_launch()
+
+    def close(self):
+        self.device.close()
 
 
 @dataclasses.dataclass
 class Job:
     spec: JobSpec
-    template: Template
-    device: M.DeviceMesh
+    slot: Slot
     admitted: float
-    passes: int = 0
-    last_min: float = 0.0
-    first_min: float = 0.0
     done_at: float | None = None
-    final_min: float = 0.0
-    final_mean: float = 0.0
-    relocations: int = 0
-    charged: int = 0  # bytes counted against the budget while the job is active
 
 
 @dataclasses.dataclass
@@ -135,32 +157,37 @@ class ServeStats:
     jobs: int
     relocations: int
     wall_s: float
-    busy_s: float
-    ticks: int
     latencies_s: list
     peak_active: int
     peak_bytes: int
     results: dict
     phase_s: dict = dataclasses.field(default_factory=dict)  # host time by loop phase
+    slots_created: int = 0
 
     def summary(self) -> dict:
         lat = np.array(self.latencies_s) if self.latencies_s else np.zeros(1)
         return {"jobs": self.jobs, "relocations": self.relocations, "wall_s": round(self.wall_s, 3),
                 "relocations_per_s": self.relocations / max(self.wall_s, 1e-9),
                 "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-                "ticks": self.ticks, "peak_active_jobs": self.peak_active, "peak_device_bytes": self.peak_bytes,
-                "phase_s": {k: round(v, 4) for k, v in self.phase_s.items()}}
+                "peak_active_jobs": self.peak_active, "peak_device_bytes": self.peak_bytes,
+                "slots_created": self.slots_created, "phase_s": {k: round(v, 4) for k, v in self.phase_s.items()}}
 
 
 class Server:
     def __init__(self, hbm_budget_bytes: int = 64 << 30, max_passes: int = 20, min_gain: float = 1e-3,
-                 params: dict | None = None, keep_results: bool = False):
+                 params: dict | None = None, keep_results: bool = False, max_concurrent: int = 64):
         self.budget = int(hbm_budget_bytes)
         self.max_passes = max_passes
         self.min_gain = min_gain
         self.params = dict(DEFAULT_PARAMS, **(params or {}))
         self.keep_results = keep_results
+        self.max_concurrent = max_concurrent
         self.templates: dict = {}
+        self.payloads: dict = {}
+        self.idle: dict = collections.defaultdict(list)  # (kind, n, smoother) -> [Slot]
+        self.idle_order: collections.OrderedDict = collections.OrderedDict()  # Slot -> key, least recent first
+        self.used = 0  # device bytes of every slot, busy or idle
+        self.slots_created = 0
 
     def template(self, spec: JobSpec) -> Template:
         key = (spec.kind, spec.n)
@@ -169,97 +196,144 @@ class Server:
         return self.templates[key]
 
     def prepare(self, stream):
-        """Build every template the stream needs (topology set-up, not timed)."""
+        """Build every template and the jobs' input positions (what a client
+        would send); not part of serving."""
         for s in stream:
-            self.template(s)
+            t = self.template(s)
+            self.payloads[s.job_id] = t.positions(s.seed)
 
-    def _admit(self, spec: JobSpec, now: float) -> Job:
+    def _take_slot(self, spec: JobSpec, busy: int):
+        """A free slot for the job, or None when the budget has no room."""
+        key = (spec.kind, spec.n, spec.smoother)
+        if self.idle[key]:
+            slot = self.idle[key].pop()
+            self.idle_order.pop(slot, None)
+            return slot
         t = self.template(spec)
-        d = M.DeviceMesh(None, clone_of=t.device)
-        d.upload_positions(t.positions(spec.seed))
-        q = d.evaluate()
-        return Job(spec, t, d, now, last_min=q.minimumQuality(), first_min=q.minimumQuality())
+        need = t.bytes
+        while self.used + need > self.budget and self.idle_order:
+            old, okey = self.idle_order.popitem(last=False)  # evict the least recently used idle slot
+            self.idle[okey].remove(old)
+            self.used -= old.bytes
+            old.close()
+        if busy and self.used + need > self.budget:
+            return None  # wait for running jobs to free memory (an empty GPU always admits)
+        slot = Slot(t, spec.smoother, self.params[spec.smoother], self.max_passes, self.min_gain)
+        self.used += slot.bytes
+        self.slots_created += 1
+        return slot
+
+    def _release(self, spec: JobSpec, slot: Slot):
+        key = (spec.kind, spec.n, spec.smoother)
+        self.idle[key].append(slot)
+        self.idle_order[slot] = key
 
     def run(self, stream: list[JobSpec], realtime: bool = True) -> ServeStats:
         """Serve the stream.  realtime=False admits each job as soon as the
         loop reaches it (arrival times only order the jobs)."""
         pending = collections.deque()
-        active: list[Job] = []
+        running: list[Job] = []
         lat, results = [], {}
-        relocations, ticks, peak_active, peak_bytes, used = 0, 0, 0, 0, 0
-        phase = {"admit_s": 0.0, "batch_setup_s": 0.0, "pass_s": 0.0, "batch_close_s": 0.0, "retire_s": 0.0}
+        relocations, peak_active, peak_bytes = 0, 0, 0
+        phase = {"admit_s": 0.0, "poll_s": 0.0, "retire_s": 0.0}
         i = 0
         t0 = time.perf_counter()
-        busy = 0.0
-        while i < len(stream) or pending or active:
+        while i < len(stream) or pending or running:
             now = time.perf_counter() - t0
             while i < len(stream) and (not realtime or stream[i].arrival <= now):
                 pending.append(stream[i])
                 i += 1
-            if not active and not pending:
-                if realtime and i < len(stream):
-                    time.sleep(max(0.0, min(0.01, stream[i].arrival - now)))
-                continue
-            # admission against the HBM budget
-            # (a job is charged its template's footprint on admission and the
-            # same amount is released when it retires, so the books balance
-            # even though its per-pass buffers grow once it runs)
+            # admission: a free stream slot and room in the HBM budget
             ta = time.perf_counter()
-            while pending:
-                need = self.template(pending[0]).bytes
-                if active and used + need > self.budget:
+            while pending and len(running) < self.max_concurrent:
+                spec = pending[0]
+                slot = self._take_slot(spec, len(running))
+                if slot is None:
                     break
-                job = self._admit(pending.popleft(), time.perf_counter() - t0)
-                job.charged = max(need, job.device.device_bytes())
-                used += job.charged
-                active.append(job)
+                pending.popleft()
+                payload = self.payloads.get(spec.job_id)
+                if payload is None:
+                    payload = slot.template.positions(spec.seed)
+                slot.launch(payload)
+                running.append(Job(spec, slot, time.perf_counter() - t0))
             phase["admit_s"] += time.perf_counter() - ta
-            peak_active = max(peak_active, len(active))
-            peak_bytes = max(peak_bytes, used)
-            # one pass of every active job: one batch per smoother
-            tb = time.perf_counter()
-            for sm in SMOOTHERS + ("spawn_search",):
-                jobs = [j for j in active if j.spec.smoother == sm]
-                if not jobs:
-                    continue
-                t1 = time.perf_counter()
-                b = M.Batch([j.device for j in jobs])
-                t2 = time.perf_counter()
-                b.smooth_pass(sm, self.params[sm])
-                b.evaluate(0)
-                qs = b.read_quality(0)
-                if b.status() != 0:
-                    raise RuntimeError("batched pass reported a dependency timeout")
-                t3 = time.perf_counter()
-                b.close()
-                t4 = time.perf_counter()
-                phase["batch_setup_s"] += t2 - t1
-                phase["pass_s"] += t3 - t2
-                phase["batch_close_s"] += t4 - t3
-                for j, q in zip(jobs, qs):
-                    j.passes += 1
-                    j.relocations += j.template.movable
-                    gain = q.minimumQuality() - j.last_min
-                    j.last_min = q.minimumQuality()
-                    if j.passes >= self.max_passes or gain < self.min_gain:
-                        j.done_at = time.perf_counter() - t0
-                        j.final_min, j.final_mean = q.minimumQuality(), q.harmonicMean()
-            busy += time.perf_counter() - tb
-            ticks += 1
+            peak_active = max(peak_active, len(running))
+            peak_bytes = max(peak_bytes, self.used)
+            # completions
+            tp = time.perf_counter()
             still = []
-            tr = time.perf_counter()
-            for j in active:
-                if j.done_at is None:
+            finished = []
+            for j in running:
+                if j.slot.device.job_done():
+                    j.done_at = time.perf_counter() - t0
+                    finished.append(j)
+                else:
                     still.append(j)
-                    continue
-                relocations += j.relocations
+            phase["poll_s"] += time.perf_counter() - tp
+            tr = time.perf_counter()
+            for j in finished:
+                passes, first, last = j.slot.device.job_result()
+                relocations += passes * j.slot.template.movable
                 lat.append(j.done_at - j.spec.arrival if realtime else j.done_at - j.admitted)
                 if self.keep_results:
-                    results[j.spec.job_id] = {"pos": j.device.fetch_positions(), "passes": j.passes,
-                                              "min": j.final_min, "mean": j.final_mean}
-                used -= j.charged
-                j.device.close()
+                    results[j.spec.job_id] = {"pos": j.slot.device.fetch_positions(), "passes": passes,
+                                              "min": last.minimumQuality(), "mean": last.harmonicMean()}
+                self._release(j.spec, j.slot)
             phase["retire_s"] += time.perf_counter() - tr
-            active = still
+            running = still
+            if not finished and (not pending or len(running) >= self.max_concurrent):
+                time.sleep(50e-6)
         wall = time.perf_counter() - t0
-        return ServeStats(len(stream), relocations, wall, busy, ticks, lat, peak_active, peak_bytes, results, phase)
+        return ServeStats(len(stream), relocations, wall, lat, peak_active, peak_bytes, results, phase,
+                          self.slots_created)
+
+    def close(self):
+        for slots in self.idle.values():
+            for s in slots:
+                s.close()
+        self.idle.clear()
+        self.idle_order.clear()
+        self.used = 0
+
+
+def run_plain(server: Server, stream: list[JobSpec], realtime: bool = True) -> ServeStats:
+    """The plain path under the same stream: one job at a time in arrival
+    order, each pass launched from the host (one launch per colour), the
+    evaluation read back after every pass for the stop rule.  A device mesh
+    per (kind, n) is kept across jobs, so only positions are uploaded."""
+    meshes: dict = {}
+    lat, relocations, results = [], 0, {}
+    t0 = time.perf_counter()
+    for spec in stream:
+        if realtime:
+            wait = spec.arrival - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+        start = time.perf_counter() - t0
+        t = server.template(spec)
+        d = meshes.get((spec.kind, spec.n))
+        if d is None:
+            d = meshes[(spec.kind, spec.n)] = M.DeviceMesh(None, clone_of=t.device)
+        payload = server.payloads.get(spec.job_id)
+        d.upload_gpu_verts(payload if payload is not None else t.positions(spec.seed))
+        last = d.evaluate().minimumQuality()
+        passes = 0
+        q = None
+        for _ in range(server.max_passes):
+            d.smooth_pass(spec.smoother, server.params[spec.smoother])
+            q = d.evaluate()
+            passes += 1
+            gain = q.minimumQuality() - last
+            last = q.minimumQuality()
+            if gain < server.min_gain:
+                break
+        relocations += passes * t.movable
+        done = time.perf_counter() - t0
+        lat.append(done - spec.arrival if realtime else done - start)
+        if server.keep_results:
+            results[spec.job_id] = {"pos": d.fetch_positions(), "passes": passes, "min": q.minimumQuality(),
+                                    "mean": q.harmonicMean()}
+    wall = time.perf_counter() - t0
+    for d in meshes.values():
+        d.close()
+    return ServeStats(len(stream), relocations, wall, lat, 1, 0, results)

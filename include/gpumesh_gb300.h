@@ -138,6 +138,10 @@ gm_status gm_mesh_upload_verts(gm_mesh* mesh, uint32_t nv, const double* xyz);
 /* Replaces updateCudaVerts with the reference's GpuVert layout
  * {vec3 p; uint c} (16 bytes per vertex, DataStructures/GpuMesh.h:11-19). */
 gm_status gm_mesh_upload_gpu_verts(gm_mesh* mesh, uint32_t nv, const void* gpu_verts);
+/* The same, asynchronous on the mesh's stream, for a mesh whose vertices
+ * are already uploaded (nv must match): `gpu_verts` should be pinned host
+ * memory and must stay unchanged until the stream has passed the copy. */
+gm_status gm_mesh_upload_gpu_verts_async(gm_mesh* mesh, uint32_t nv, const void* gpu_verts);
 /* Replace updateCudaTets / updateCudaPris / updateCudaHexs
  * (resources/cuda/Mesh.cu:100,126,152).  stride_words = 32-bit words per
  * element record: 4/6/8 for bare connectivity, 5/12/16 for GpuTet, GpuPri,
@@ -268,6 +272,26 @@ gm_status gm_batch_counters(gm_batch* batch, uint64_t* out5, int32_t reset);
 gm_status gm_batch_latencies(gm_batch* batch, double* out_ms_per_mesh);
 /* [meshes, queued vertices, segments, evaluation blocks] */
 gm_status gm_batch_info(gm_batch* batch, uint32_t* out4);
+
+/* ---- device-resident jobs --------------------------------------------------
+ * No single counterpart in the reference, whose pass loop runs on the host
+ * (AbstractSmoother::smoothMesh, Smoothers/AbstractSmoother.cpp:103-211).
+ * A job is a whole smoothing schedule under a stop rule: an evaluation, then
+ * relocation passes, each followed by an evaluation, until the minimum
+ * quality rises by less than min_gain or max_passes passes are done.
+ * gm_job_prepare captures it as one CUDA graph whose loop is a conditional
+ * node that the device drives, so a job costs one launch and no host round
+ * trip per pass.  Re-uploading the mesh's topology, groups, constraints or
+ * crew drops the prepared job; new positions of the same size do not.  The
+ * quality after pass p is in result slot p (gm_quality_read). */
+gm_status gm_job_prepare(gm_mesh* mesh, int32_t smoother, const double* params, uint32_t max_passes,
+                         double min_gain);
+/* asynchronous, on the mesh's stream */
+gm_status gm_job_launch(gm_mesh* mesh);
+/* *done = 1 once the mesh's stream has no work left */
+gm_status gm_job_query(gm_mesh* mesh, int32_t* done);
+/* passes run, quality before the first pass and after the last; synchronous */
+gm_status gm_job_result(gm_mesh* mesh, uint32_t* passes, gm_quality* first, gm_quality* last);
 
 /* No counterpart in the reference.  Quality evaluation that allocates
  * nothing, for callers that cannot call cudaMalloc (a host framework that
