@@ -126,16 +126,16 @@ __device__ __forceinline__ void batch_one(const BatchMesh& bm, const SmoothParam
 // queue order; a group whose mesh has not finished the item's earlier
 // colours waits without holding up the other groups (one poll per step,
 // bounded by spin_limit).  The FP64 acceptance test of a near-degenerate
-// patch runs warp-wide, one group at a time, on a corner-position copy of
-// that group's patch staged over the group's own (finished) canonical
-// patch.  Deadlock freedom is the queue's: an item waits only
+// patch runs warp-wide, one group at a time, with the positions read from
+// the mesh (patch_quality_global: the arithmetic of the acceptance kernel of
+// the plain path).  Deadlock freedom is the queue's: an item waits only
 // for items earlier in the queue, which were handed out before it.
 template <int VAR>
 __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, char* wsm, int lane)
 {
     const int gi = lane / kNMGroup, sub = lane & (kNMGroup - 1), leader = gi * kNMGroup;
-    WarpPatch P = nm_group_patch(wsm, gi, a.maxe);
-    float* con = nm_group_con(wsm, gi, a.maxe);
+    WarpPatch P = nm_group_patch<VAR>(wsm, gi, a.maxe);
+    float* con = nm_group_con<VAR>(wsm, gi, a.maxe);
     NMGroup g;
     g.phase = kNMIdle;
     g.E = 0;
@@ -143,12 +143,13 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
     const BatchMesh* bm = a.meshes;  // the group's mesh (any valid entry while idle)
     uint32_t mesh = 0, need = 0;
     unsigned int seen = 0;  // the mesh's done count, polled one step ahead of its use
-    unsigned long long spins = 0;
+    unsigned int spins = 0;
+    const unsigned int spin_limit = a.spin_limit < 0xffffffffull ? (unsigned int)a.spin_limit : 0xffffffffu;
     TetConst kc = tet_const<VAR>(bm->crew);
     bool sine = false;
     uint32_t cur = 0, last = 0, seg = 0;  // the warp's chunk [cur, last) and the segment of cur
     bool exhausted = false;
-    unsigned long long n_evals = 0, n_elems = 0, n_fp64 = 0;
+    unsigned int n_evals = 0, n_elems = 0, n_fp64 = 0;
     while (true)
     {
         // (1) idle groups take the next items, in group order
@@ -196,7 +197,7 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
         if (g.phase == kNMWait && sub == 0)
         {
             if (need == 0 || seen >= need) ok = 1;
-            else if (++spins > a.spin_limit || __ldcv(&a.ctl->error))
+            else if (++spins > spin_limit || __ldcv(&a.ctl->error))
             {
                 atomicOr(&a.ctl->error, 1u);
                 give_up = 1;
@@ -224,7 +225,7 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
         // poll for the still-waiting groups; the value is used at the next
         // step, so the load's latency overlaps this step's evaluation
         if (g.phase == kNMWait && sub == 0 && !give_up && need) seen = __ldcv(&a.done[mesh]);
-        const float f = nm_group_quality<VAR>(P, busy ? g.E : 0, g.cand, kc, sine, sub);
+        const float f = nm_group_quality<VAR>(P, busy ? g.E : 0, g.vo.p, g.cand, kc, sine, sub);
         bool finishing = false, need64 = false, accept = true;
         if (busy)
         {
@@ -244,14 +245,12 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
             const BatchMesh* bx =
                 reinterpret_cast<const BatchMesh*>(__shfl_sync(kFullMask, reinterpret_cast<unsigned long long>(bm), src));
             const uint32_t vx = __shfl_sync(kFullMask, g.v, src);
-            const double ox = __shfl_sync(kFullMask, g.old.x, src), oy = __shfl_sync(kFullMask, g.old.y, src);
-            const double oz = __shfl_sync(kFullMask, g.old.z, src);
+            const double ox = __shfl_sync(kFullMask, g.vo.p.x, src), oy = __shfl_sync(kFullMask, g.vo.p.y, src);
+            const double oz = __shfl_sync(kFullMask, g.vo.p.z, src);
             const double nx = __shfl_sync(kFullMask, g.cand.x, src), ny = __shfl_sync(kFullMask, g.cand.y, src);
             const double nz = __shfl_sync(kFullMask, g.cand.z, src);
-            WarpPatch X = nm_fp64_patch(wsm, src / kNMGroup, a.maxe);
-            stage_patch(bx->view, vx, X, lane);
-            const double d0 = patch_uniform<VAR, 4, double>(bx->crew, X, mk(ox, oy, oz), lane);
-            const double d1 = patch_uniform<VAR, 4, double>(bx->crew, X, mk(nx, ny, nz), lane);
+            const double d0 = patch_quality_global<VAR, 4>(bx->view, bx->crew, vx, mk(ox, oy, oz), lane);
+            const double d1 = patch_quality_global<VAR, 4>(bx->view, bx->crew, vx, mk(nx, ny, nz), lane);
             if (gi == src / kNMGroup)
             {
                 accept = !(d1 < d0);
@@ -266,10 +265,10 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
             {
                 if (finishing)
                 {
-                    if (accept) bm->view.pos[g.v] = make_float4(g.cand.x, g.cand.y, g.cand.z, g.old.w);
-                    n_evals += (unsigned long long)g.evals;
-                    n_elems += (unsigned long long)g.evals * (unsigned long long)g.E;
-                    n_fp64 += (g.q0 >= sp.accept_q && f >= sp.accept_q) ? 0ull : 1ull;
+                    if (accept) bm->view.pos[g.v] = make_float4(g.cand.x, g.cand.y, g.cand.z, g.ow);
+                    n_evals += (unsigned int)g.evals;
+                    n_elems += (unsigned int)(g.evals * g.E);
+                    n_fp64 += (g.q0 >= sp.accept_q && f >= sp.accept_q) ? 0u : 1u;
                 }
                 __threadfence();
                 const unsigned int d = atomicAdd(&a.done[mesh], 1u) + 1u;
@@ -296,7 +295,8 @@ template <int SMOOTHER, int VAR, int MAXK>
 __device__ __forceinline__ void batch_queue_loop(const BatchArgs& a, const SmoothParams& sp, char* smem);
 
 template <int SMOOTHER, int VAR, int MAXK>
-__global__ void __launch_bounds__(256, BatchLockstep<SMOOTHER, VAR, MAXK>::on ? 2 : (MAXK == 4 ? 3 : 1))
+__global__ void __launch_bounds__(256, BatchLockstep<SMOOTHER, VAR, MAXK>::on ? (VAR == kVarMRFree ? 3 : 2)
+                                                                              : (MAXK == 4 ? 3 : 1))
     batch_relocate_kernel(BatchArgs a, SmoothParams sp)
 {
     extern __shared__ __align__(16) char smem[];
@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(256, BatchLockstep<SMOOTHER, VAR, MAXK>::on ? 
             asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
             atomicCAS(&a.ctl->t0, 0ull, now);
         }
-        nm_lockstep_batch<VAR>(a, sp, smem + wib * nm_warp_bytes(a.maxe), lane);
+        nm_lockstep_batch<VAR>(a, sp, smem + wib * nm_warp_bytes<VAR>(a.maxe), lane);
     }
     else
         batch_queue_loop<SMOOTHER, VAR, MAXK>(a, sp, smem);
@@ -393,8 +393,8 @@ static cudaError_t launch_batch_t(const BatchArgs& a, const SmoothParams& sp, in
                                   cudaStream_t s)
 {
     auto kern = batch_relocate_kernel<SMOOTHER, VAR, MAXK>;
-    size_t smem = (BatchLockstep<SMOOTHER, VAR, MAXK>::on ? nm_warp_bytes(a.maxe) : patch_smem_per_warp(MAXK, a.maxe)) *
-                  wpb;
+    size_t smem =
+        (BatchLockstep<SMOOTHER, VAR, MAXK>::on ? nm_warp_bytes<VAR>(a.maxe) : patch_smem_per_warp(MAXK, a.maxe)) * wpb;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int occ = 0;

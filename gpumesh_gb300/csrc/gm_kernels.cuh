@@ -556,6 +556,37 @@ __device__ __forceinline__ void patch_multi(const Crew& crew, WarpPatch& P, int 
     __syncwarp();
 }
 
+// Patch quality in FP64 straight from the mesh, without staging: lanes over
+// the incident elements and the per-element arithmetic of patch_uniform, so
+// it equals patch_uniform<VAR, MAXK, double> on a patch staged from the same
+// positions.  For the rare FP64 acceptance test of a vertex whose patch is
+// staged in a form the FP64 measures do not read.
+template <int VAR, int MAXK>
+__device__ double patch_quality_global(const MeshView& m, const Crew& crew, uint32_t v, V3<double> c, int lane)
+{
+    const uint32_t b = m.ve_off[v], e = m.ve_off[v + 1];
+    const int E = (int)(e - b);
+    PatchAcc<double> a{0.0, 3.0e38, 0};
+    for (int i = lane; i < E; i += kWarp)
+    {
+        const uint32_t r = m.ve[b + i];
+        const int type = MAXK == 4 ? kTet : ref_type(r), loc = ref_local(r);
+        uint32_t vid[8];
+        elem_vertices(m, type, ref_id(r), vid);
+        const int n = MAXK == 4 ? 4 : type_size(type);
+        V3<double> p[MAXK];
+#pragma unroll
+        for (int k = 0; k < MAXK; ++k)
+        {
+            if (k < n) p[k] = (k == loc) ? c : to<double>(__ldcg(&m.pos[vid[k]]));
+            else p[k] = c;
+        }
+        acc_add(a, elem_quality<VAR, MAXK, double>(crew, type, p));
+    }
+    acc_reduce(a, kWarp);
+    return acc_final(a, E);
+}
+
 template <class R>
 __device__ __forceinline__ V3<R> snap(const MeshView& m, int cid, V3<R> p)
 {

@@ -45,22 +45,32 @@ struct NMGroup
     float ns;   // node shift
     float q0;
     float fr;   // reflection value of the current cycle
-    float4 old;
-    S4 s0, s1, s2, s3, vo;
+    float ow;   // the w word of the vertex's position record, kept on commit
+    S4 s0, s1, s2, s3, vo;  // vo.p: the position at the start (the patch origin)
     V3<float> c, xr, cand;
 };
 
-// shared memory of one warp: the groups' canonical patches (5 slots of
-// maxe float4 each), then one constraint record per group
-__host__ __device__ constexpr size_t nm_warp_bytes(int maxe)
+// canonical slots per element: mean ratio reads the three frame columns,
+// metric conformity also the staged sines and cosines
+template <int VAR>
+__host__ __device__ constexpr int nm_slots()
 {
-    return (size_t)kNMGroups * patch_slots(4) * maxe * 16 + (size_t)kNMGroups * kNMConWords * 4;
+    return VAR == kVarMRFree ? 3 : patch_slots(4);
 }
 
+// shared memory of one warp: the groups' canonical patches, then one
+// constraint record per group
+template <int VAR>
+__host__ __device__ constexpr size_t nm_warp_bytes(int maxe)
+{
+    return (size_t)kNMGroups * nm_slots<VAR>() * maxe * 16 + (size_t)kNMGroups * kNMConWords * 4;
+}
+
+template <int VAR>
 __device__ __forceinline__ WarpPatch nm_group_patch(char* wsm, int gi, int maxe)
 {
     WarpPatch P;
-    P.sp = reinterpret_cast<float4*>(wsm) + (size_t)gi * patch_slots(4) * maxe;
+    P.sp = reinterpret_cast<float4*>(wsm) + (size_t)gi * nm_slots<VAR>() * maxe;
     P.meta = nullptr;
     P.cand = nullptr;
     P.res = nullptr;
@@ -70,18 +80,10 @@ __device__ __forceinline__ WarpPatch nm_group_patch(char* wsm, int gi, int maxe)
     return P;
 }
 
+template <int VAR>
 __device__ __forceinline__ float* nm_group_con(char* wsm, int gi, int maxe)
 {
-    return reinterpret_cast<float*>(wsm + (size_t)kNMGroups * patch_slots(4) * maxe * 16) + gi * kNMConWords;
-}
-
-// the corner-position patch (4 slots + element meta) of a finished group's
-// vertex, staged over that group's own region for an FP64 acceptance test
-__device__ __forceinline__ WarpPatch nm_fp64_patch(char* wsm, int gi, int maxe)
-{
-    WarpPatch P = nm_group_patch(wsm, gi, maxe);
-    P.meta = reinterpret_cast<int*>(P.sp + 4 * (size_t)maxe);
-    return P;
+    return reinterpret_cast<float*>(wsm + (size_t)kNMGroups * nm_slots<VAR>() * maxe * 16) + gi * kNMConWords;
 }
 
 // project() on a constraint record copied from a Constraint's FP32 head
@@ -119,10 +121,10 @@ __device__ __forceinline__ V3<float> nm_snap(const NMGroup& g, const float* con,
 
 // patch quality of the group's candidate (E = 0: an idle group, result unused)
 template <int VAR>
-__device__ __forceinline__ float nm_group_quality(const WarpPatch& P, int E, V3<float> c, const TetConst& kc, bool sine,
-                                                  int sub)
+__device__ __forceinline__ float nm_group_quality(const WarpPatch& P, int E, V3<float> origin, V3<float> c,
+                                                  const TetConst& kc, bool sine, int sub)
 {
-    const TetCand t = tet_cand<VAR>(sine, P.o, c);
+    const TetCand t = tet_cand<VAR>(sine, origin, c);
     PatchAcc<float> a{0.f, 3.0e38f, 0};
     for (int e = sub; e < E; e += kNMGroup) acc_add(a, canonical_quality<VAR>(P, e, t, kc, sine));
     acc_reduce(a, kNMGroup);
@@ -187,7 +189,7 @@ __device__ __forceinline__ void nm_step(NMGroup& g, float f, const SmoothParams&
     }
     else  // kNMQ0
     {
-        const V3<float> pos = to<float>(g.old);
+        const V3<float> pos = g.vo.p;
         g.q0 = f;
         g.vo = S4{pos, f};
         g.s0 = S4{pos + mk(g.ns, 0.f, 0.f), 0.f};
@@ -259,12 +261,13 @@ __device__ __forceinline__ float nm_begin(NMGroup& g, const MeshView& m, bool si
 {
     g.v = v;
     g.cid = m.cid[v];
-    g.old = __ldcg(&m.pos[v]);
+    const float4 old = __ldcg(&m.pos[v]);
+    g.ow = old.w;
     const uint32_t eb = m.ve_off[v], ee = m.ve_off[v + 1];
     const uint32_t vb = m.vv_off[v], ve = m.vv_off[v + 1];
-    const V3<float> o = to<float>(g.old);
+    const V3<float> o = to<float>(old);
+    g.vo.p = o;
     P.E = (int)(ee - eb);
-    P.o = o;
     nvv = ve - vb;
     float ls = 0.f;
     const uint32_t n = max(ee - eb, ve - vb);
@@ -302,21 +305,22 @@ __device__ __forceinline__ void nm_finish_begin(NMGroup& g, const SmoothParams& 
     if (start) g.ns = ls / (float)nvv * sp.shift;
 }
 
-__device__ __forceinline__ void nm_flush_counters(Counters* ctr, unsigned long long evals,
-                                                  unsigned long long elems, unsigned long long fp64, int lane)
+__device__ __forceinline__ void nm_flush_counters(Counters* ctr, unsigned int evals, unsigned int elems,
+                                                  unsigned int fp64, int lane)
 {
     if (!ctr) return;
+    unsigned long long e = evals, el = elems, f = fp64;
     for (int o = 16; o > 0; o >>= 1)
     {
-        evals += __shfl_xor_sync(kFullMask, evals, o);
-        elems += __shfl_xor_sync(kFullMask, elems, o);
-        fp64 += __shfl_xor_sync(kFullMask, fp64, o);
+        e += __shfl_xor_sync(kFullMask, e, o);
+        el += __shfl_xor_sync(kFullMask, el, o);
+        f += __shfl_xor_sync(kFullMask, f, o);
     }
     if (lane == 0)
     {
-        atomicAdd(&ctr->patch_evals, evals);
-        atomicAdd(&ctr->elem_evals[kTet], elems);
-        if (fp64) atomicAdd(&ctr->fp64_vertices, fp64);
+        atomicAdd(&ctr->patch_evals, e);
+        atomicAdd(&ctr->elem_evals[kTet], el);
+        if (f) atomicAdd(&ctr->fp64_vertices, f);
     }
 }
 
@@ -329,8 +333,8 @@ __device__ void nm_lockstep_plain(const MeshView& m, const Crew& crew, const Smo
                                   Counters* ctr, const Deferred& def, uint32_t slot_base, int lane)
 {
     const int gi = lane / kNMGroup, sub = lane & (kNMGroup - 1);
-    WarpPatch P = nm_group_patch(wsm, gi, maxe);
-    float* con = nm_group_con(wsm, gi, maxe);
+    WarpPatch P = nm_group_patch<VAR>(wsm, gi, maxe);
+    float* con = nm_group_con<VAR>(wsm, gi, maxe);
     const TetConst kc = tet_const<VAR>(crew);
     const bool sine = VAR == kVarMCDiag && sine_metric(crew);
     NMGroup g;
@@ -338,7 +342,7 @@ __device__ void nm_lockstep_plain(const MeshView& m, const Crew& crew, const Smo
     g.E = 0;
     g.cid = 0;
     uint32_t next = begin;
-    unsigned long long n_evals = 0, n_elems = 0, n_fp64 = 0;
+    unsigned int n_evals = 0, n_elems = 0, n_fp64 = 0;  // per warp: well within 32 bits
     while (true)
     {
         // idle groups take the next vertices, in group order
@@ -359,7 +363,7 @@ __device__ void nm_lockstep_plain(const MeshView& m, const Crew& crew, const Smo
         }
         // one evaluation per busy group
         const bool busy = g.phase != kNMIdle;
-        const float f = nm_group_quality<VAR>(P, busy ? g.E : 0, g.cand, kc, sine, sub);
+        const float f = nm_group_quality<VAR>(P, busy ? g.E : 0, g.vo.p, g.cand, kc, sine, sub);
         if (!busy) continue;
         ++g.evals;
         if (g.phase != kNMFinal)
@@ -371,19 +375,19 @@ __device__ void nm_lockstep_plain(const MeshView& m, const Crew& crew, const Smo
         const bool defer = !(g.q0 >= sp.accept_q && f >= sp.accept_q);
         if (sub == 0)
         {
-            const float4 nw = make_float4(g.cand.x, g.cand.y, g.cand.z, g.old.w);
+            const float4 nw = make_float4(g.cand.x, g.cand.y, g.cand.z, g.ow);
             if (defer)
             {
                 const uint32_t k = atomicAdd(def.count, 1u);
                 def.v[slot_base + k] = g.v;
-                def.oldp[slot_base + k] = g.old;
+                def.oldp[slot_base + k] = make_float4(g.vo.p.x, g.vo.p.y, g.vo.p.z, g.ow);
                 def.newp[slot_base + k] = nw;
             }
             else
                 m.pos[g.v] = nw;
-            n_evals += (unsigned long long)g.evals;
-            n_elems += (unsigned long long)g.evals * (unsigned long long)g.E;
-            n_fp64 += defer ? 1ull : 0ull;
+            n_evals += (unsigned int)g.evals;
+            n_elems += (unsigned int)(g.evals * g.E);
+            n_fp64 += defer ? 1u : 0u;
         }
         g.phase = kNMIdle;
     }

@@ -91,14 +91,14 @@ __global__ void __launch_bounds__(kNMWarpsPerBlock * 32, 4)
     const uint32_t begin = (blockIdx.x * (blockDim.x >> 5) + wib) * per_warp;
     if (begin >= count) return;
     const uint32_t end = min(begin + per_warp, count);
-    nm_lockstep_plain<VAR>(m, crew, sp, members, begin, end, smem + wib * nm_warp_bytes(maxe), maxe, ctr, def,
+    nm_lockstep_plain<VAR>(m, crew, sp, members, begin, end, smem + wib * nm_warp_bytes<VAR>(maxe), maxe, ctr, def,
                            slot_base, lane);
 }
 
 template <int VAR>
 static cudaError_t launch_nm_lockstep(const RelocLaunch& L)
 {
-    const size_t smem = nm_warp_bytes(L.maxe) * kNMWarpsPerBlock;
+    const size_t smem = nm_warp_bytes<VAR>(L.maxe) * kNMWarpsPerBlock;
     if (smem > 48 * 1024)
     {
         cudaError_t e = cudaFuncSetAttribute(relocate_nm_lockstep_kernel<VAR>,
