@@ -20,7 +20,6 @@
 #include <cstdint>
 #include <cstring>
 #include <numeric>
-#include <set>
 #include <vector>
 
 #include "gm_internal.h"
@@ -139,14 +138,19 @@ Topology build_topology(const HostMeshView& in, bool permute)
     }
 
     // ---- greedy breadth-first colouring ----
+    // The reference copies the set of existing colours for every vertex and
+    // erases its neighbours' colours; the first remaining colour (or a new
+    // one) is taken.  A bitmask of the neighbours' colours gives the same
+    // first-fit choice without the set copies.
     const int NO_GROUP = -2, UNSET = -1;
     std::vector<int> groups(nv, NO_GROUP);
     {
         size_t seek = 0;
-        std::set<uint32_t> existing;
+        uint32_t ncolours = 0;
+        std::vector<uint64_t> used;  // colours taken by the current vertex's neighbours
         std::vector<uint32_t> queue;
         queue.reserve(nv);
-        auto visit = [&](uint32_t w, std::set<uint32_t>& avail) {
+        auto visit = [&](uint32_t w) {
             int& g = groups[w];
             if (g == NO_GROUP)
             {
@@ -154,7 +158,7 @@ Topology build_topology(const HostMeshView& in, bool permute)
                 queue.push_back(w);
             }
             else if (g != UNSET)
-                avail.erase((uint32_t)g);
+                used[(uint32_t)g >> 6] |= 1ull << ((uint32_t)g & 63);
         };
         while (queue.size() < nv)
         {
@@ -172,7 +176,7 @@ Topology build_topology(const HostMeshView& in, bool permute)
             for (size_t qi = first; qi < queue.size(); ++qi)
             {
                 uint32_t v = queue[qi];
-                std::set<uint32_t> avail = existing;
+                std::fill(used.begin(), used.end(), 0ull);
                 for (const ElemRef& r : nb.elems[v])
                 {
                     const uint32_t* e;
@@ -180,17 +184,26 @@ Topology build_topology(const HostMeshView& in, bool permute)
                     if (r.type == kTypeTet) { e = in.tets + 4 * (size_t)r.id; k = 4; }
                     else if (r.type == kTypePri) { e = in.pris + 6 * (size_t)r.id; k = 6; }
                     else { e = in.hexs + 8 * (size_t)r.id; k = 8; }
-                    for (int j = 0; j < k; ++j) visit(e[j], avail);
+                    for (int j = 0; j < k; ++j) visit(e[j]);
                 }
-                int g;
-                if (avail.empty())
+                // lowest existing colour no neighbour has, else a new one
+                uint32_t g = ncolours;
+                for (uint32_t wi = 0; wi < used.size(); ++wi)
                 {
-                    g = (int)existing.size();
-                    existing.insert((uint32_t)g);
+                    const uint64_t freebits = ~used[wi];
+                    if (freebits)
+                    {
+                        const uint32_t c = wi * 64 + (uint32_t)__builtin_ctzll(freebits);
+                        if (c < ncolours) g = c;
+                        break;
+                    }
                 }
-                else
-                    g = (int)*avail.begin();
-                groups[v] = g;
+                if (g == ncolours)
+                {
+                    ++ncolours;
+                    if (((ncolours + 63) >> 6) > used.size()) used.push_back(0ull);
+                }
+                groups[v] = (int)g;
             }
         }
     }
