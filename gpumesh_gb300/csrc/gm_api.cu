@@ -244,8 +244,8 @@ void enqueue_evaluate(gm_mesh* m, Quality* out)
 {
     uint32_t total = m->nt + m->np + m->nh;
     int nb = evaluate_blocks(total, m->sm_count);
-    if (m->parts.reserve(nb))  // a fresh scratch starts with its ticket at 0
-        GM_CUDA(cudaMemsetAsync(m->parts.p, 0, sizeof(EvalPartial), m->stream));
+    if (m->parts.reserve(nb))  // a fresh scratch starts with its ticket and bucket totals at 0
+        GM_CUDA(cudaMemsetAsync(m->parts.p, 0, kEvalScratchHead, m->stream));
     GM_CUDA(launch_evaluate(m->variant(), m->elem_set(), m->view(), m->crew, m->parts.p, nb, out, m->stream));
 }
 

@@ -391,17 +391,19 @@ __device__ __forceinline__ EQ<R> mr_hex(const Crew& c, const V3<R>* p)
 // with each of the 12 edges' squared length computed once (a corner's
 // |F|^2 is the sum of its three edges'), and the factors 1/3 of the corner
 // measure and 1/8 of the harmonic combination applied once to the sum.
+// Branch-free: every corner yields r = |F|^2 |det|^(-2/3) (3 / q for a
+// valid corner); an inverted corner's quality is q = -3 / r, so the
+// element's minimum over its inverted corners is -3 / (their smallest r),
+// and a flat corner (det = 0, r = inf) gives q = -0.
 __device__ __forceinline__ void mr_hex_corner_fast(V3<float> a, V3<float> b, V3<float> c, float f2, float sign,
-                                                   float& rsum, float& minbad, bool& all)
+                                                   float& rsum, float& minr, bool& bad)
 {
     const float det = sign * det3(a, b, c);
-    if (det > 0.f) rsum = fmaf(f2, pow_m23(det), rsum);
-    else
-    {
-        all = false;
-        const float q = sgn(det) * 3.f * pow_23(det) / f2;
-        minbad = q < minbad ? q : minbad;
-    }
+    const float r = f2 * pow_m23(det);
+    rsum += r;
+    const bool inverted = !(det > 0.f);
+    bad |= inverted;
+    minr = inverted ? fminf(minr, r) : minr;
 }
 
 __device__ __forceinline__ EQ<float> mr_hex_fast(const V3<float>* p)
@@ -412,18 +414,18 @@ __device__ __forceinline__ EQ<float> mr_hex_fast(const V3<float>* p)
     const float l01 = dot(e01, e01), l03 = dot(e03, e03), l04 = dot(e04, e04), l12 = dot(e12, e12);
     const float l15 = dot(e15, e15), l23 = dot(e23, e23), l26 = dot(e26, e26), l37 = dot(e37, e37);
     const float l45 = dot(e45, e45), l47 = dot(e47, e47), l56 = dot(e56, e56), l67 = dot(e67, e67);
-    float rsum = 0.f, minbad = 3.0e38f;
-    bool all = true;
-    mr_hex_corner_fast(e01, e04, e03, l01 + l04 + l03, -1.f, rsum, minbad, all);
-    mr_hex_corner_fast(e01, e12, e15, l01 + l12 + l15, 1.f, rsum, minbad, all);
-    mr_hex_corner_fast(e12, e26, e23, l12 + l26 + l23, -1.f, rsum, minbad, all);
-    mr_hex_corner_fast(e03, e23, e37, l03 + l23 + l37, 1.f, rsum, minbad, all);
-    mr_hex_corner_fast(e04, e45, e47, l04 + l45 + l47, 1.f, rsum, minbad, all);
-    mr_hex_corner_fast(e15, e56, e45, l15 + l56 + l45, -1.f, rsum, minbad, all);
-    mr_hex_corner_fast(e26, e56, e67, l26 + l56 + l67, 1.f, rsum, minbad, all);
-    mr_hex_corner_fast(e37, e67, e47, l37 + l67 + l47, -1.f, rsum, minbad, all);
-    if (all) return EQ<float>{rsum * (1.f / 24.f), true};
-    return EQ<float>{minbad, false};
+    float rsum = 0.f, minr = INFINITY;
+    bool bad = false;
+    mr_hex_corner_fast(e01, e04, e03, l01 + l04 + l03, -1.f, rsum, minr, bad);
+    mr_hex_corner_fast(e01, e12, e15, l01 + l12 + l15, 1.f, rsum, minr, bad);
+    mr_hex_corner_fast(e12, e26, e23, l12 + l26 + l23, -1.f, rsum, minr, bad);
+    mr_hex_corner_fast(e03, e23, e37, l03 + l23 + l37, 1.f, rsum, minr, bad);
+    mr_hex_corner_fast(e04, e45, e47, l04 + l45 + l47, 1.f, rsum, minr, bad);
+    mr_hex_corner_fast(e15, e56, e45, l15 + l56 + l45, -1.f, rsum, minr, bad);
+    mr_hex_corner_fast(e26, e56, e67, l26 + l56 + l67, 1.f, rsum, minr, bad);
+    mr_hex_corner_fast(e37, e67, e47, l37 + l67 + l47, -1.f, rsum, minr, bad);
+    if (!bad) return EQ<float>{rsum * (1.f / 24.f), true};
+    return EQ<float>{-3.f * rcp_fast(minr), false};
 }
 
 // MetricConformityEvaluator::specifiedMetric: 5-point Keast rule

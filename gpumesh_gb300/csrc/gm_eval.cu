@@ -98,18 +98,21 @@ __device__ __forceinline__ void block_reduce(double& sum, float& mn, int& bad, d
         }
 }
 
-// One launch per evaluation: every block reduces its elements to a partial;
-// the last block to finish (a ticket taken after a release fence) reduces
-// all partials in a fixed order and writes the Quality, so the result does
-// not depend on which block finishes last.  atomicInc wraps the ticket back
-// to 0, so the scratch is ready for the next launch.
+// One launch per evaluation: every block adds its bucket counts to the 20
+// totals (integer atomics: exact in any order) and stores its min / 1/q sum
+// / inverted count; the last block to finish (a ticket taken after a release
+// fence) reduces those in a fixed order and writes the Quality, so the
+// result does not depend on which block finishes last.  atomicInc wraps the
+// ticket back to 0 and the last block clears the totals, so the scratch is
+// ready for the next launch.  (A last block that also summed 20 bucket
+// columns of every block spent tens of microseconds on dependent L2 loads
+// under the tet kernel's 40-register budget.)
 struct EvalShared
 {
     int hist[20];
     float wmin[kEvalWarps];
     double wsum[kEvalWarps];
     int wbad[kEvalWarps];
-    unsigned int whist[kEvalWarps][20];
     bool last;
 };
 
@@ -120,7 +123,7 @@ __device__ __forceinline__ void eval_prologue(EvalShared& sh)
 }
 
 // the block's partial, then (last block only) the final reduction
-__device__ __noinline__ void eval_epilogue(const EvalAcc& acc, EvalShared& sh, EvalPartial* parts, Quality* out,
+__device__ __forceinline__ void eval_epilogue(const EvalAcc& acc, EvalShared& sh, EvalPartial* parts, Quality* out,
                                               uint32_t total);
 
 // connectivity of a tet (SET 4) or a hex (SET 9): 1 or 2 uint4
@@ -231,64 +234,48 @@ __global__ void __launch_bounds__(kEvalThreads, kEvalMinBlocks<VAR, SET>) evalua
     eval_epilogue(acc, sh, parts, out, total);
 }
 
-__device__ __noinline__ void eval_epilogue(const EvalAcc& acc, EvalShared& sh, EvalPartial* parts, Quality* out,
+__device__ __forceinline__ void eval_epilogue(const EvalAcc& acc, EvalShared& sh, EvalPartial* parts, Quality* out,
                                               uint32_t total)
 {
-    int* hist = sh.hist;
-    float* wmin = sh.wmin;
-    double* wsum = sh.wsum;
-    int* wbad = sh.wbad;
-    auto& whist = sh.whist;
-    bool& last = sh.last;
     double sum = acc.rs;
     float mn = acc.min_quality();
     int bad = acc.nbad;
-    block_reduce(sum, mn, bad, wsum, wmin, wbad);
+    block_reduce(sum, mn, bad, sh.wsum, sh.wmin, sh.wbad);  // its barrier also orders the shared histogram
     const int nb = gridDim.x;
     const EvalScratch S = eval_scratch(parts, nb);
-    if (threadIdx.x < 20) S.hist[threadIdx.x * nb + blockIdx.x] = hist[threadIdx.x];
+    if (threadIdx.x < 20)
+    {
+        const int c = sh.hist[threadIdx.x];
+        if (c) atomicAdd(&S.hist[threadIdx.x], (unsigned int)c);
+    }
     if (threadIdx.x == 0)
     {
         S.rsum[blockIdx.x] = sum;
         S.min[blockIdx.x] = mn;
         S.nbad[blockIdx.x] = bad;
     }
-    __threadfence();  // every writer publishes its part of the partial
+    if (threadIdx.x < 20) __threadfence();  // every writer publishes its part of the partial
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicInc(S.ticket, (unsigned int)nb - 1u) == (unsigned int)nb - 1u;
+    if (threadIdx.x == 0) sh.last = atomicInc(S.ticket, (unsigned int)nb - 1u) == (unsigned int)nb - 1u;
     __syncthreads();
-    if (!last) return;
+    if (!sh.last) return;
     __threadfence();
     // the last block: every partial, coalesced, in a fixed order
     double tsum = 0;
     float tmin = 1.0f;
     int tbad = 0;
-    unsigned int h[20];
-#pragma unroll
-    for (int b = 0; b < 20; ++b) h[b] = 0;
-    for (int i = threadIdx.x; i < nb; i += blockDim.x)
+#pragma unroll 4
+    for (int i = threadIdx.x; i < nb; i += kEvalThreads)
     {
         tsum += __ldcg(&S.rsum[i]);
         tmin = fminf(tmin, __ldcg(&S.min[i]));
         tbad += __ldcg(&S.nbad[i]);
-#pragma unroll
-        for (int b = 0; b < 20; ++b) h[b] += (unsigned int)__ldcg(&S.hist[b * nb + i]);
     }
-    __syncthreads();  // the shared reduction arrays are reused
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int b = 0; b < 20; ++b)
-    {
-        unsigned int x = h[b];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        if (lane == 0) whist[w][b] = x;
-    }
-    block_reduce(tsum, tmin, tbad, wsum, wmin, wbad);
+    block_reduce(tsum, tmin, tbad, sh.wsum, sh.wmin, sh.wbad);
     if (threadIdx.x < 20)
     {
-        unsigned long long hb = 0;
-        for (int k = 0; k < kEvalWarps; ++k) hb += whist[k][threadIdx.x];
-        out->buckets[threadIdx.x] = hb;
+        out->buckets[threadIdx.x] = __ldcg(&S.hist[threadIdx.x]);
+        S.hist[threadIdx.x] = 0u;
     }
     if (threadIdx.x == 0)
     {

@@ -30,32 +30,35 @@ struct EvalPartial
 };
 
 // Scratch of one evaluation launch of nb blocks, carved from nb EvalPartial
-// slots as structure-of-arrays so the last block reads every partial
-// coalesced: a ticket word (8 bytes), then rsum[nb], min[nb], nbad[nb] and
-// hist[20][nb] -- 8 + 96 nb bytes, within nb * sizeof(EvalPartial).
+// slots: a ticket word (8 bytes), the 20 bucket totals every block adds to
+// (80 bytes, padded to 88), then per block rsum[nb], min[nb], nbad[nb] as
+// structure-of-arrays so the last block reads them coalesced -- 96 + 16 nb
+// bytes, within nb * sizeof(EvalPartial).  The ticket and the totals are
+// zero between launches: a fresh scratch is cleared once, and the last block
+// of every launch resets them.
 struct EvalScratch
 {
     unsigned int* ticket;
+    unsigned int* hist;  // hist[b], summed over the blocks
     double* rsum;
     float* min;
     int* nbad;
-    int* hist;  // hist[b * nb + block]
 };
-static_assert(sizeof(EvalPartial) >= 104, "evaluation scratch layout");
+constexpr size_t kEvalScratchHead = 96;  // ticket + bucket totals, cleared together
+static_assert(sizeof(EvalPartial) >= kEvalScratchHead, "evaluation scratch layout");
 
 __host__ __device__ inline EvalScratch eval_scratch(EvalPartial* base, int nb)
 {
     char* p = reinterpret_cast<char*>(base);
     EvalScratch s;
     s.ticket = reinterpret_cast<unsigned int*>(p);
-    p += 8;
+    s.hist = reinterpret_cast<unsigned int*>(p + 8);
+    p += kEvalScratchHead;
     s.rsum = reinterpret_cast<double*>(p);
     p += 8 * (size_t)nb;
     s.min = reinterpret_cast<float*>(p);
     p += 4 * (size_t)nb;
     s.nbad = reinterpret_cast<int*>(p);
-    p += 4 * (size_t)nb;
-    s.hist = reinterpret_cast<int*>(p);
     return s;
 }
 
