@@ -60,9 +60,10 @@ FLOPS_PER_ELEM_EVAL = {
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
 # captures of the same kernels on the same workloads: one evaluation of the
-# 128^3 hex mesh, and the first spawn-search colour of the C2 sphere (61,699
-# vertices), scaled to a pass by vertices.
-EVAL_HEX128_TRAFFIC_BYTES = 101_564_928 + 3_570_432
+# 128^3 hex mesh and of the 128^3 x 6 tet cube, and the first spawn-search
+# colour of the C2 sphere (61,699 vertices), scaled to a pass by vertices.
+EVAL_HEX128_TRAFFIC_BYTES = 101_477_376 + 3_631_872
+EVAL_TET128_TRAFFIC_BYTES = 235_710_976 + 4_071_168
 SPAWN_C2_TRAFFIC_PER_VERTEX = (39_982_848 + 16_128) / 61_699
 
 
@@ -313,7 +314,7 @@ def eval_roofline(torch, stream, hbm_peak, kind="hex", launches=24, singles=10):
     mesh = "128^3 hexes" if kind == "hex" else "128^3 x 6 tets"
     return {"bound": "hbm", "kernel": f"evaluate_kernel (mean ratio, {mesh})", "achieved": round(achieved, 1),
             "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
-            "traffic": EVAL_HEX128_TRAFFIC_BYTES if kind == "hex" else None,
+            "traffic": EVAL_HEX128_TRAFFIC_BYTES if kind == "hex" else EVAL_TET128_TRAFFIC_BYTES,
             "algorithmic_bytes": algo, "us_per_launch": round(t * 1e6, 2),
             "timing": f"{launches} launches back to back over {R} device copies ({R * algo / 1e6:.0f} MB, "
                       f"> 2x the {l2 / 1e6:.0f} MB L2)",
