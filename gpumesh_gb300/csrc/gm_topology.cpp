@@ -33,47 +33,92 @@ const int kPriEdges[9][2] = {{0, 1}, {0, 2}, {1, 2}, {0, 3}, {1, 4}, {2, 5}, {3,
 const int kHexEdges[12][2] = {{0, 1}, {0, 3}, {1, 2}, {2, 3}, {0, 4}, {1, 5},
                               {2, 6}, {3, 7}, {4, 5}, {4, 7}, {5, 6}, {6, 7}};
 
-struct ElemRef
-{
-    uint32_t id;
-    int8_t type;
-    int8_t local;
-};
-
+// Per-vertex neighbourhoods as flat CSR arrays (Mesh::compileNeighborhoods
+// keeps a std::vector per vertex; the lists here hold the same entries in
+// the same order):
+//   elems: packed (type, local, id) refs, in element order -- tets, then
+//          prisms, then hexes, each by id
+//   verts: edge neighbours in the order the edges are first met, element by
+//          element and edge by edge (Mesh::addEdge: a neighbour is appended
+//          to both ends when the first end's list does not hold it yet)
 struct Neighbourhoods
 {
-    std::vector<std::vector<ElemRef>> elems;
-    std::vector<std::vector<uint32_t>> verts;
+    std::vector<uint32_t> e_off, e;
+    std::vector<uint32_t> v_off, v;
+    uint32_t elem_count(uint32_t x) const { return e_off[x + 1] - e_off[x]; }
 };
 
-void add_edge(Neighbourhoods& nb, uint32_t a, uint32_t b)
+template <int K>
+void count_refs(const uint32_t* conn, uint32_t count, std::vector<uint32_t>& deg)
 {
-    std::vector<uint32_t>& list = nb.verts[a];
-    for (uint32_t x : list)
-        if (x == b) return;
-    nb.verts[a].push_back(b);
-    nb.verts[b].push_back(a);
+    for (size_t i = 0; i < (size_t)count * K; ++i) ++deg[conn[i] + 1];
 }
 
+template <int K>
+void fill_refs(const uint32_t* conn, uint32_t count, int type, std::vector<uint32_t>& cur, std::vector<uint32_t>& e)
+{
+    for (uint32_t i = 0; i < count; ++i)
+        for (int k = 0; k < K; ++k)
+        {
+            const uint32_t x = conn[(size_t)K * i + k];
+            e[cur[x]++] = pack_elem_ref(type, k, i);
+        }
+}
+
+// an element's edges, appended to the bounded per-vertex lists in `slot`
 template <int K, int NE>
-void add_elements(Neighbourhoods& nb, const uint32_t* conn, uint32_t count, int type, const int (*edges)[2])
+void add_edges(const uint32_t* conn, uint32_t count, const int (*edges)[2], const std::vector<uint32_t>& base,
+               std::vector<uint32_t>& n, std::vector<uint32_t>& slot)
 {
     for (uint32_t i = 0; i < count; ++i)
     {
-        const uint32_t* e = conn + (size_t)K * i;
-        for (int k = 0; k < K; ++k) nb.elems[e[k]].push_back(ElemRef{i, (int8_t)type, (int8_t)k});
-        for (int k = 0; k < NE; ++k) add_edge(nb, e[edges[k][0]], e[edges[k][1]]);
+        const uint32_t* el = conn + (size_t)K * i;
+        for (int k = 0; k < NE; ++k)
+        {
+            const uint32_t a = el[edges[k][0]], b = el[edges[k][1]];
+            const uint32_t* la = slot.data() + base[a];
+            const uint32_t na = n[a];
+            bool seen = false;
+            for (uint32_t j = 0; j < na; ++j)
+                if (la[j] == b)
+                {
+                    seen = true;
+                    break;
+                }
+            if (seen) continue;
+            slot[base[a] + n[a]++] = b;
+            slot[base[b] + n[b]++] = a;
+        }
     }
 }
 
 Neighbourhoods build_neighbourhoods(const HostMeshView& in)
 {
+    const uint32_t nv = in.nv;
     Neighbourhoods nb;
-    nb.elems.resize(in.nv);
-    nb.verts.resize(in.nv);
-    add_elements<4, 6>(nb, in.tets, in.nt, kTypeTet, kTetEdges);
-    add_elements<6, 9>(nb, in.pris, in.np, kTypePri, kPriEdges);
-    add_elements<8, 12>(nb, in.hexs, in.nh, kTypeHex, kHexEdges);
+    nb.e_off.assign((size_t)nv + 1, 0);
+    count_refs<4>(in.tets, in.nt, nb.e_off);
+    count_refs<6>(in.pris, in.np, nb.e_off);
+    count_refs<8>(in.hexs, in.nh, nb.e_off);
+    for (uint32_t x = 0; x < nv; ++x) nb.e_off[x + 1] += nb.e_off[x];
+    nb.e.resize(nb.e_off[nv]);
+    std::vector<uint32_t> cur(nb.e_off.begin(), nb.e_off.end() - 1);
+    fill_refs<4>(in.tets, in.nt, kTypeTet, cur, nb.e);
+    fill_refs<6>(in.pris, in.np, kTypePri, cur, nb.e);
+    fill_refs<8>(in.hexs, in.nh, kTypeHex, cur, nb.e);
+
+    // every corner of a tet, prism or hex has three edges, so a vertex has at
+    // most 3 x (its element count) distinct neighbours
+    std::vector<uint32_t> base((size_t)nv + 1, 0), n(nv, 0);
+    for (uint32_t x = 0; x < nv; ++x) base[x + 1] = base[x] + 3 * nb.elem_count(x);
+    std::vector<uint32_t> slot(base[nv]);
+    add_edges<4, 6>(in.tets, in.nt, kTetEdges, base, n, slot);
+    add_edges<6, 9>(in.pris, in.np, kPriEdges, base, n, slot);
+    add_edges<8, 12>(in.hexs, in.nh, kHexEdges, base, n, slot);
+    nb.v_off.assign((size_t)nv + 1, 0);
+    for (uint32_t x = 0; x < nv; ++x) nb.v_off[x + 1] = nb.v_off[x] + n[x];
+    nb.v.resize(nb.v_off[nv]);
+    for (uint32_t x = 0; x < nv; ++x) std::copy_n(slot.begin() + base[x], n[x], nb.v.begin() + nb.v_off[x]);
     return nb;
 }
 
@@ -83,22 +128,10 @@ void build_csr(const HostMeshView& in, std::vector<uint32_t>& ve_off, std::vecto
                std::vector<uint32_t>& vv_off, std::vector<uint32_t>& vv)
 {
     Neighbourhoods nb = build_neighbourhoods(in);
-    const uint32_t nv = in.nv;
-    ve_off.assign((size_t)nv + 1, 0);
-    vv_off.assign((size_t)nv + 1, 0);
-    for (uint32_t v = 0; v < nv; ++v)
-    {
-        ve_off[v + 1] = ve_off[v] + (uint32_t)nb.elems[v].size();
-        vv_off[v + 1] = vv_off[v] + (uint32_t)nb.verts[v].size();
-    }
-    ve.resize(ve_off[nv]);
-    vv.resize(vv_off[nv]);
-    for (uint32_t v = 0; v < nv; ++v)
-    {
-        uint32_t o = ve_off[v];
-        for (const ElemRef& r : nb.elems[v]) ve[o++] = pack_elem_ref(r.type, r.local, r.id);
-        std::copy(nb.verts[v].begin(), nb.verts[v].end(), vv.begin() + vv_off[v]);
-    }
+    ve_off = std::move(nb.e_off);
+    ve = std::move(nb.e);
+    vv_off = std::move(nb.v_off);
+    vv = std::move(nb.v);
 }
 
 Topology build_topology(const HostMeshView& in, bool permute)
@@ -124,14 +157,13 @@ Topology build_topology(const HostMeshView& in, bool permute)
         else
         {
             bool sub = false;
-            for (const ElemRef& r : nb.elems[v])
+            for (uint32_t j = nb.e_off[v]; j < nb.e_off[v + 1] && !sub; ++j)
             {
-                if ((r.type == kTypeTet && bounding_tet[r.id]) || (r.type == kTypePri && bounding_pri[r.id]) ||
-                    (r.type == kTypeHex && bounding_hex[r.id]))
-                {
-                    sub = true;
-                    break;
-                }
+                const uint32_t r = nb.e[j];
+                const int type = (int)(r >> 30);
+                const uint32_t id = r & kMaxElemId;
+                sub = (type == kTypeTet && bounding_tet[id]) || (type == kTypePri && bounding_pri[id]) ||
+                      (type == kTypeHex && bounding_hex[id]);
             }
             types[v] = sub ? SUBSU : INTER;
         }
@@ -177,14 +209,17 @@ Topology build_topology(const HostMeshView& in, bool permute)
             {
                 uint32_t v = queue[qi];
                 std::fill(used.begin(), used.end(), 0ull);
-                for (const ElemRef& r : nb.elems[v])
+                for (uint32_t j = nb.e_off[v]; j < nb.e_off[v + 1]; ++j)
                 {
+                    const uint32_t r = nb.e[j];
+                    const int type = (int)(r >> 30);
+                    const uint32_t id = r & kMaxElemId;
                     const uint32_t* e;
                     int k;
-                    if (r.type == kTypeTet) { e = in.tets + 4 * (size_t)r.id; k = 4; }
-                    else if (r.type == kTypePri) { e = in.pris + 6 * (size_t)r.id; k = 6; }
-                    else { e = in.hexs + 8 * (size_t)r.id; k = 8; }
-                    for (int j = 0; j < k; ++j) visit(e[j]);
+                    if (type == kTypeTet) { e = in.tets + 4 * (size_t)id; k = 4; }
+                    else if (type == kTypePri) { e = in.pris + 6 * (size_t)id; k = 6; }
+                    else { e = in.hexs + 8 * (size_t)id; k = 8; }
+                    for (int q = 0; q < k; ++q) visit(e[q]);
                 }
                 // lowest existing colour no neighbour has, else a new one
                 uint32_t g = ncolours;
@@ -217,7 +252,7 @@ Topology build_topology(const HostMeshView& in, bool permute)
             if (types[a] == types[b])
             {
                 if (types[a] == FIXED) return false;
-                if (groups[a] == groups[b]) return nb.elems[a].size() < nb.elems[b].size();
+                if (groups[a] == groups[b]) return nb.elem_count(a) < nb.elem_count(b);
                 return groups[a] < groups[b];
             }
             return types[a] < types[b];
@@ -266,17 +301,18 @@ Topology build_topology(const HostMeshView& in, bool permute)
     t.vv_off.assign((size_t)nv + 1, 0);
     for (uint32_t p = 0; p < nv; ++p)
     {
-        t.ve_off[p + 1] = t.ve_off[p] + (uint32_t)nb.elems[order[p]].size();
-        t.vv_off[p + 1] = t.vv_off[p] + (uint32_t)nb.verts[order[p]].size();
+        const uint32_t x = (uint32_t)order[p];
+        t.ve_off[p + 1] = t.ve_off[p] + nb.elem_count(x);
+        t.vv_off[p + 1] = t.vv_off[p] + (nb.v_off[x + 1] - nb.v_off[x]);
     }
     t.ve.resize(t.ve_off[nv]);
     t.vv.resize(t.vv_off[nv]);
     for (uint32_t p = 0; p < nv; ++p)
     {
-        uint32_t o = t.ve_off[p];
-        for (const ElemRef& r : nb.elems[order[p]]) t.ve[o++] = pack_elem_ref(r.type, r.local, r.id);
-        o = t.vv_off[p];
-        for (uint32_t w : nb.verts[order[p]]) t.vv[o++] = new_of_old[w];
+        const uint32_t x = (uint32_t)order[p];
+        std::copy(nb.e.begin() + nb.e_off[x], nb.e.begin() + nb.e_off[x + 1], t.ve.begin() + t.ve_off[p]);
+        uint32_t o = t.vv_off[p];
+        for (uint32_t j = nb.v_off[x]; j < nb.v_off[x + 1]; ++j) t.vv[o++] = new_of_old[nb.v[j]];
     }
     t.new_of_old = std::move(new_of_old);
     return t;
