@@ -152,72 +152,81 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
     unsigned int n_evals = 0, n_elems = 0, n_fp64 = 0;
     while (true)
     {
-        // (1) idle groups take the next items, in group order
-        const bool idle = g.phase == kNMIdle;
-        const unsigned ball = __ballot_sync(kFullMask, idle && sub == 0);
-        if (ball && cur >= last && !exhausted)
+        // (1) idle groups take the next items, in group order (skipped while
+        // no group is idle, the common case)
+        const unsigned ball = __ballot_sync(kFullMask, g.phase == kNMIdle && sub == 0);
+        if (ball)
         {
-            uint32_t first = 0;
-            if (lane == 0) first = atomicAdd(&a.ctl->next, kClaimChunk);
-            first = __shfl_sync(kFullMask, first, 0);
-            if (first >= a.total) exhausted = true;
-            else
+            const bool idle = g.phase == kNMIdle;
+            if (cur >= last && !exhausted)
             {
-                cur = first;
-                last = min(first + kClaimChunk, a.total);
-                seg = find_segment(a.seg_start, a.nseg, first);
+                uint32_t first = 0;
+                if (lane == 0) first = atomicAdd(&a.ctl->next, kClaimChunk);
+                first = __shfl_sync(kFullMask, first, 0);
+                if (first >= a.total) exhausted = true;
+                else
+                {
+                    cur = first;
+                    last = min(first + kClaimChunk, a.total);
+                    seg = find_segment(a.seg_start, a.nseg, first);
+                }
             }
-        }
-        const uint32_t rank = __popc(ball & ((1u << leader) - 1u));
-        const uint32_t avail = cur < last ? last - cur : 0u;
-        if (idle && rank < avail)
-        {
-            const uint32_t item = cur + rank;
-            uint32_t s = seg;
-            while (item >= __ldg(&a.seg_start[s + 1])) ++s;
-            const Segment sg = a.segs[s];
-            bm = &a.meshes[sg.mesh];
-            mesh = sg.mesh;
-            need = sg.need;
-            spins = 0;
-            seen = 0;
-            g.v = bm->members[sg.member_begin + (item - __ldg(&a.seg_start[s]))];
-            g.phase = kNMWait;
-        }
-        cur += min((uint32_t)__popc(ball), avail);
-        while (cur < last && cur >= __ldg(&a.seg_start[seg + 1])) ++seg;
-        if (!__any_sync(kFullMask, g.phase != kNMIdle))
-        {
-            if (exhausted) break;
-            continue;
+            const uint32_t rank = __popc(ball & ((1u << leader) - 1u));
+            const uint32_t avail = cur < last ? last - cur : 0u;
+            if (idle && rank < avail)
+            {
+                const uint32_t item = cur + rank;
+                uint32_t s = seg;
+                while (item >= __ldg(&a.seg_start[s + 1])) ++s;
+                const Segment sg = a.segs[s];
+                bm = &a.meshes[sg.mesh];
+                mesh = sg.mesh;
+                need = sg.need;
+                spins = 0;
+                seen = 0;
+                g.v = bm->members[sg.member_begin + (item - __ldg(&a.seg_start[s]))];
+                g.phase = kNMWait;
+            }
+            cur += min((uint32_t)__popc(ball), avail);
+            while (cur < last && cur >= __ldg(&a.seg_start[seg + 1])) ++seg;
+            if (!__any_sync(kFullMask, g.phase != kNMIdle))
+            {
+                if (exhausted) break;
+                continue;
+            }
         }
         // (2) a waiting group starts once its mesh's earlier colours are done
-        // (the done count was loaded at the end of the previous step)
-        int ok = 0, give_up = 0;
-        if (g.phase == kNMWait && sub == 0)
+        // (the done count was loaded at the end of the previous step); skipped
+        // while no group waits
+        int give_up = 0;
+        if (__ballot_sync(kFullMask, g.phase == kNMWait))
         {
-            if (need == 0 || seen >= need) ok = 1;
-            else if (++spins > spin_limit || __ldcv(&a.ctl->error))
+            int ok = 0;
+            if (g.phase == kNMWait && sub == 0)
             {
-                atomicOr(&a.ctl->error, 1u);
-                give_up = 1;
+                if (need == 0 || seen >= need) ok = 1;
+                else if (++spins > spin_limit || __ldcv(&a.ctl->error))
+                {
+                    atomicOr(&a.ctl->error, 1u);
+                    give_up = 1;
+                }
             }
-        }
-        ok = __shfl_sync(kFullMask, ok, leader);
-        give_up = __shfl_sync(kFullMask, give_up, leader);
-        if (__any_sync(kFullMask, ok))
-        {
-            float ls = 0.f;
-            uint32_t nvv = 1;
-            if (ok)
+            ok = __shfl_sync(kFullMask, ok, leader);
+            give_up = __shfl_sync(kFullMask, give_up, leader);
+            if (__any_sync(kFullMask, ok))
             {
-                __threadfence();
-                sine = VAR == kVarMCDiag && sine_metric(bm->crew);
-                kc = tet_const<VAR>(bm->crew);
-                ls = nm_begin<VAR>(g, bm->view, sine, P, con, g.v, sub, nvv);
+                float ls = 0.f;
+                uint32_t nvv = 1;
+                if (ok)
+                {
+                    __threadfence();
+                    sine = VAR == kVarMCDiag && sine_metric(bm->crew);
+                    kc = tet_const<VAR>(bm->crew);
+                    ls = nm_begin<VAR>(g, bm->view, sine, P, con, g.v, sub, nvv);
+                }
+                __syncwarp();
+                nm_finish_begin(g, sp, ok, ls, nvv);
             }
-            __syncwarp();
-            nm_finish_begin(g, sp, ok, ls, nvv);
         }
         // (3) one evaluation per busy group
         const bool busy = g.phase >= kNMQ0;
