@@ -136,6 +136,8 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
     const int gi = lane / kNMGroup, sub = lane & (kNMGroup - 1), leader = gi * kNMGroup;
     WarpPatch P = nm_group_patch<VAR>(wsm, gi, a.maxe);
     float* con = nm_group_con<VAR>(wsm, gi, a.maxe);
+    float4* st = nm_group_state<VAR>(wsm, gi, a.maxe);
+    const unsigned gmask = 0xffu << leader;
     NMGroup g;
     g.phase = kNMIdle;
     g.E = 0;
@@ -239,7 +241,7 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
         if (busy)
         {
             ++g.evals;
-            if (g.phase != kNMFinal) nm_step(g, f, sp, con);
+            if (g.phase != kNMFinal) nm_step(g, f, sp, con, st, gmask, sub);
             else
             {
                 finishing = true;

@@ -13,6 +13,9 @@
 // at the next step, so the groups stay busy until the warp's work runs out.
 // Everything a step needs is in registers or shared memory: the patch, and
 // the vertex's boundary constraint copied next to it when the vertex starts.
+// The simplex, centroid, reflection and cycle counters are read only by the
+// step's state update, so they live in a per-group shared record between
+// steps instead of holding registers through the patch evaluation.
 //
 // Each vertex follows nelder_mead() (NelderMeadSmoother.cpp:100-260)
 // decision for decision: initial simplex, sort, reflection / expansion /
@@ -27,6 +30,7 @@ namespace gm {
 constexpr int kNMGroup = 8;                   // lanes per vertex
 constexpr int kNMGroups = kWarp / kNMGroup;   // vertices per warp
 constexpr int kNMConWords = 16;               // constraint record per group
+constexpr int kNMStateVecs = 7;               // search record per group, float4s
 constexpr unsigned kFullMask = 0xffffffffu;
 
 enum : int { kNMIdle = 0, kNMWait, kNMQ0, kNMInit, kNMReflect, kNMProbe, kNMFinal };
@@ -37,18 +41,53 @@ struct NMGroup
     int phase;
     int cid;
     int E;
-    int k;      // initial simplex vertex being evaluated
-    int cycle;
     int evals;
-    bool reset;
     uint32_t v;
     float ns;   // node shift
     float q0;
-    float fr;   // reflection value of the current cycle
     float ow;   // the w word of the vertex's position record, kept on commit
-    S4 s0, s1, s2, s3, vo;  // vo.p: the position at the start (the patch origin)
-    V3<float> c, xr, cand;
+    S4 vo;      // vo.p: the position at the start (the patch origin)
+    V3<float> cand;
 };
+
+// the rest of the search, in the group's shared record between steps
+struct NMState
+{
+    S4 s0, s1, s2, s3;
+    V3<float> c, xr;
+    float fr;    // reflection value of the current cycle
+    int k;       // initial simplex vertex being evaluated
+    int cycle;
+    bool reset;
+};
+
+__device__ __forceinline__ NMState nm_load(const float4* st)
+{
+    const float4 a = st[0], b = st[1], c = st[2], d = st[3], e = st[4], f = st[5], h = st[6];
+    NMState S;
+    S.s0 = S4{mk(a.x, a.y, a.z), a.w};
+    S.s1 = S4{mk(b.x, b.y, b.z), b.w};
+    S.s2 = S4{mk(c.x, c.y, c.z), c.w};
+    S.s3 = S4{mk(d.x, d.y, d.z), d.w};
+    S.c = mk(e.x, e.y, e.z);
+    S.fr = e.w;
+    S.xr = mk(f.x, f.y, f.z);
+    S.k = __float_as_int(f.w);
+    S.cycle = __float_as_int(h.x);
+    S.reset = __float_as_int(h.y) != 0;
+    return S;
+}
+
+__device__ __forceinline__ void nm_store(float4* st, const NMState& S)
+{
+    st[0] = make_float4(S.s0.p.x, S.s0.p.y, S.s0.p.z, S.s0.w);
+    st[1] = make_float4(S.s1.p.x, S.s1.p.y, S.s1.p.z, S.s1.w);
+    st[2] = make_float4(S.s2.p.x, S.s2.p.y, S.s2.p.z, S.s2.w);
+    st[3] = make_float4(S.s3.p.x, S.s3.p.y, S.s3.p.z, S.s3.w);
+    st[4] = make_float4(S.c.x, S.c.y, S.c.z, S.fr);
+    st[5] = make_float4(S.xr.x, S.xr.y, S.xr.z, __int_as_float(S.k));
+    st[6] = make_float4(__int_as_float(S.cycle), __int_as_float(S.reset ? 1 : 0), 0.f, 0.f);
+}
 
 // canonical slots per element: mean ratio reads the three frame columns,
 // metric conformity also the staged sines and cosines
@@ -59,11 +98,12 @@ __host__ __device__ constexpr int nm_slots()
 }
 
 // shared memory of one warp: the groups' canonical patches, then one
-// constraint record per group
+// constraint record per group, then one search record per group
 template <int VAR>
 __host__ __device__ constexpr size_t nm_warp_bytes(int maxe)
 {
-    return (size_t)kNMGroups * nm_slots<VAR>() * maxe * 16 + (size_t)kNMGroups * kNMConWords * 4;
+    return (size_t)kNMGroups * nm_slots<VAR>() * maxe * 16 + (size_t)kNMGroups * kNMConWords * 4 +
+           (size_t)kNMGroups * kNMStateVecs * 16;
 }
 
 template <int VAR>
@@ -84,6 +124,14 @@ template <int VAR>
 __device__ __forceinline__ float* nm_group_con(char* wsm, int gi, int maxe)
 {
     return reinterpret_cast<float*>(wsm + (size_t)kNMGroups * nm_slots<VAR>() * maxe * 16) + gi * kNMConWords;
+}
+
+template <int VAR>
+__device__ __forceinline__ float4* nm_group_state(char* wsm, int gi, int maxe)
+{
+    return reinterpret_cast<float4*>(wsm + (size_t)kNMGroups * nm_slots<VAR>() * maxe * 16 +
+                                     (size_t)kNMGroups * kNMConWords * 4) +
+           gi * kNMStateVecs;
 }
 
 // project() on a constraint record copied from a Constraint's FP32 head
@@ -135,25 +183,29 @@ __device__ __forceinline__ float nm_group_quality(const WarpPatch& P, int E, V3<
 // warp are usually in different phases, and SIMT runs each distinct path
 // once for the groups on it, so the phase-specific parts are short and the
 // common tail (insertion, convergence test, next cycle, projection of the
-// next candidate) is one block shared by every group that reaches it.
-__device__ __forceinline__ void nm_step(NMGroup& g, float f, const SmoothParams& sp, const float* con)
+// next candidate) is one block shared by every group that reaches it.  The
+// group's lanes read its shared record, update their copies alike, and lane
+// 0 writes it back once all of them have read it (gmask: the group's lanes).
+__device__ __forceinline__ void nm_step(NMGroup& g, float f, const SmoothParams& sp, const float* con, float4* st,
+                                        unsigned gmask, int sub)
 {
+    NMState S = nm_load(st);
     bool insert = false, next = false, snap_next = true;
     S4 vx{g.cand, f};
     V3<float> x = g.cand;  // the next candidate before projection
     const int phase = g.phase;
     if (phase == kNMReflect)
     {
-        g.fr = f;
-        g.xr = g.cand;
-        if (g.s3.w < f)  // expand
+        S.fr = f;
+        S.xr = g.cand;
+        if (S.s3.w < f)  // expand
         {
-            x = g.c + (g.xr - g.c) * sp.gamma;
+            x = S.c + (S.xr - S.c) * sp.gamma;
             g.phase = kNMProbe;
         }
-        else if (g.s1.w >= f)  // contract
+        else if (S.s1.w >= f)  // contract
         {
-            x = g.c + ((f > g.s0.w ? g.xr : g.s0.p) - g.c) * sp.beta;
+            x = S.c + ((f > S.s0.w ? S.xr : S.s0.p) - S.c) * sp.beta;
             g.phase = kNMProbe;
         }
         else  // accept the reflection
@@ -164,25 +216,25 @@ __device__ __forceinline__ void nm_step(NMGroup& g, float f, const SmoothParams&
     }
     else if (phase == kNMProbe)
     {
-        if (g.s3.w < g.fr && f <= g.fr) vx = S4{g.xr, g.fr};
+        if (S.s3.w < S.fr && f <= S.fr) vx = S4{S.xr, S.fr};
         insert = true;
         snap_next = false;
     }
     else if (phase == kNMInit)
     {
-        if (g.k == 0) g.s0 = vx;
-        else if (g.k == 1) g.s1 = vx;
-        else g.s2 = vx;
-        ++g.k;
-        if (g.k < 3) x = g.k == 1 ? g.s1.p : g.s2.p;
+        if (S.k == 0) S.s0 = vx;
+        else if (S.k == 1) S.s1 = vx;
+        else S.s2 = vx;
+        ++S.k;
+        if (S.k < 3) x = S.k == 1 ? S.s1.p : S.s2.p;
         else
         {
-            if (g.s0.w > g.s1.w) swp(g.s0, g.s1);
-            if (g.s1.w > g.s2.w) swp(g.s1, g.s2);
-            if (g.s2.w > g.s3.w) swp(g.s2, g.s3);
-            if (g.s0.w > g.s1.w) swp(g.s0, g.s1);
-            if (g.s1.w > g.s2.w) swp(g.s1, g.s2);
-            if (g.s0.w > g.s1.w) swp(g.s0, g.s1);
+            if (S.s0.w > S.s1.w) swp(S.s0, S.s1);
+            if (S.s1.w > S.s2.w) swp(S.s1, S.s2);
+            if (S.s2.w > S.s3.w) swp(S.s2, S.s3);
+            if (S.s0.w > S.s1.w) swp(S.s0, S.s1);
+            if (S.s1.w > S.s2.w) swp(S.s1, S.s2);
+            if (S.s0.w > S.s1.w) swp(S.s0, S.s1);
             next = true;
             snap_next = false;
         }
@@ -192,62 +244,65 @@ __device__ __forceinline__ void nm_step(NMGroup& g, float f, const SmoothParams&
         const V3<float> pos = g.vo.p;
         g.q0 = f;
         g.vo = S4{pos, f};
-        g.s0 = S4{pos + mk(g.ns, 0.f, 0.f), 0.f};
-        g.s1 = S4{pos + mk(0.f, g.ns, 0.f), 0.f};
-        g.s2 = S4{pos + mk(0.f, 0.f, g.ns), 0.f};
-        g.s3 = g.vo;
-        g.cycle = 0;
-        g.reset = false;
-        g.k = 0;
-        x = g.s0.p;
+        S.s0 = S4{pos + mk(g.ns, 0.f, 0.f), 0.f};
+        S.s1 = S4{pos + mk(0.f, g.ns, 0.f), 0.f};
+        S.s2 = S4{pos + mk(0.f, 0.f, g.ns), 0.f};
+        S.s3 = g.vo;
+        S.cycle = 0;
+        S.reset = false;
+        S.k = 0;
+        x = S.s0.p;
         g.phase = kNMInit;
     }
     if (insert)
     {
-        if (vx.w > g.s3.w) swp(g.s3, vx);
-        if (vx.w > g.s2.w) swp(g.s2, vx);
-        if (vx.w > g.s1.w) swp(g.s1, vx);
-        if (vx.w > g.s0.w) swp(g.s0, vx);
-        if ((g.s3.w - g.s1.w) < sp.convergence)
+        if (vx.w > S.s3.w) swp(S.s3, vx);
+        if (vx.w > S.s2.w) swp(S.s2, vx);
+        if (vx.w > S.s1.w) swp(S.s1, vx);
+        if (vx.w > S.s0.w) swp(S.s0, vx);
+        if ((S.s3.w - S.s1.w) < sp.convergence)
         {
-            x = g.s3.p;
+            x = S.s3.p;
             g.phase = kNMFinal;
             snap_next = true;
         }
         else
         {
-            ++g.cycle;
+            ++S.cycle;
             next = true;
         }
     }
     if (next)
     {
         snap_next = true;
-        if (g.cycle < sp.cycles)
+        if (S.cycle < sp.cycles)
         {
-            g.c = (g.s1.p + g.s2.p + g.s3.p) * (1.f / 3.f);
-            x = g.c + (g.c - g.s0.p) * sp.alpha;
+            S.c = (S.s1.p + S.s2.p + S.s3.p) * (1.f / 3.f);
+            x = S.c + (S.c - S.s0.p) * sp.alpha;
             g.phase = kNMReflect;
         }
-        else if (g.reset)
+        else if (S.reset)
         {
-            x = g.s3.p;
+            x = S.s3.p;
             g.phase = kNMFinal;
         }
         else
         {
-            g.s0 = S4{g.vo.p - mk(g.ns, 0.f, 0.f), g.vo.w};
-            g.s1 = S4{g.vo.p - mk(0.f, g.ns, 0.f), g.vo.w};
-            g.s2 = S4{g.vo.p - mk(0.f, 0.f, g.ns), g.vo.w};
-            g.s3 = g.vo;
-            g.reset = true;
-            g.cycle = 0;
-            g.k = 0;
-            x = g.s0.p;
+            S.s0 = S4{g.vo.p - mk(g.ns, 0.f, 0.f), g.vo.w};
+            S.s1 = S4{g.vo.p - mk(0.f, g.ns, 0.f), g.vo.w};
+            S.s2 = S4{g.vo.p - mk(0.f, 0.f, g.ns), g.vo.w};
+            S.s3 = g.vo;
+            S.reset = true;
+            S.cycle = 0;
+            S.k = 0;
+            x = S.s0.p;
             g.phase = kNMInit;
         }
     }
     if (snap_next) g.cand = nm_snap(g, con, x);
+    __syncwarp(gmask);
+    if (sub == 0) nm_store(st, S);
+    __syncwarp(gmask);
 }
 
 // A group takes vertex v: canonical patch and constraint record over its
@@ -335,6 +390,8 @@ __device__ void nm_lockstep_plain(const MeshView& m, const Crew& crew, const Smo
     const int gi = lane / kNMGroup, sub = lane & (kNMGroup - 1);
     WarpPatch P = nm_group_patch<VAR>(wsm, gi, maxe);
     float* con = nm_group_con<VAR>(wsm, gi, maxe);
+    float4* st = nm_group_state<VAR>(wsm, gi, maxe);
+    const unsigned gmask = 0xffu << (gi * kNMGroup);
     const TetConst kc = tet_const<VAR>(crew);
     const bool sine = VAR == kVarMCDiag && sine_metric(crew);
     NMGroup g;
@@ -368,7 +425,7 @@ __device__ void nm_lockstep_plain(const MeshView& m, const Crew& crew, const Smo
         ++g.evals;
         if (g.phase != kNMFinal)
         {
-            nm_step(g, f, sp, con);
+            nm_step(g, f, sp, con, st, gmask, sub);
             continue;
         }
         // done: commit, or defer to the FP64 acceptance kernel
