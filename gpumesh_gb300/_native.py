@@ -20,7 +20,8 @@ STATUS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupp
 SAMPLERS = {"uniform": 0, "analytic": 1, "sine": 2}
 MEASURERS = {"metric_free": 0, "metric_wise": 1}
 EVALUATORS = {"mean_ratio": 0, "metric_conformity": 1}
-SMOOTHERS = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3}
+SMOOTHERS = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3, "spring_laplace": 4,
+             "quality_laplace": 5}
 
 
 class GpuMeshError(RuntimeError):

@@ -150,6 +150,10 @@ SmoothParams parse_params(int smoother, const double* p)
     case GM_SMOOTH_GETME:
         sp.lambda = (float)(p ? p[0] : 0.78);
         break;
+    case GM_SMOOTH_SPRING_LAPLACE:
+    case GM_SMOOTH_QUALITY_LAPLACE:
+        sp.shift = (float)(p ? p[0] : 0.35);  // SLMoveCoeff / QLMoveCoeff
+        break;
     default:
         throw ApiError(GM_ERR_INVALID_ARG, "unknown smoother " + std::to_string(smoother));
     }
@@ -201,6 +205,8 @@ void relocate_group(gm_mesh* m, int smoother, const SmoothParams& sp, uint32_t b
     case GM_SMOOTH_NELDER_MEAD: GM_CUDA(launch_relocate_nm(L)); break;
     case GM_SMOOTH_GRADIENT_DESCENT: GM_CUDA(launch_relocate_gd(L)); break;
     case GM_SMOOTH_SPAWN_SEARCH: GM_CUDA(launch_relocate_spawn(L)); break;
+    case GM_SMOOTH_SPRING_LAPLACE: GM_CUDA(launch_relocate_spring(L)); break;
+    case GM_SMOOTH_QUALITY_LAPLACE: GM_CUDA(launch_relocate_qlaplace(L)); break;
     default: GM_CUDA(launch_getme_update(L, m->corners.p)); break;
     }
     GM_CUDA(launch_accept(L));

@@ -123,6 +123,15 @@ void drop_graph(gm_batch* b)
     b->graph = nullptr;
 }
 
+// the batched kernels relocate with the four smoothers of the reference's
+// CUDA path; the Laplace smoothers run on the plain path only
+void require_batch_smoother(int smoother)
+{
+    if (smoother == GM_SMOOTH_SPRING_LAPLACE || smoother == GM_SMOOTH_QUALITY_LAPLACE)
+        throw ApiError(GM_ERR_UNSUPPORTED, "the batched path relocates with Nelder-Mead, gradient descent, spawn "
+                                           "search or GETMe; use gm_smooth_pass for the Laplace smoothers");
+}
+
 void enqueue_pass(gm_batch* b, int smoother, const SmoothParams& sp)
 {
     if (smoother == GM_SMOOTH_GETME)
@@ -279,6 +288,7 @@ gm_status gm_batch_smooth_pass(gm_batch* b, int32_t smoother, const double* para
     return guarded([&] {
         require(b != nullptr, "null batch");
         SmoothParams sp = parse_smooth_params(smoother, params);
+        require_batch_smoother(smoother);
         if (smoother == GM_SMOOTH_GETME) build_tables(b, true);
         enqueue_pass(b, smoother, sp);
     });
@@ -336,6 +346,7 @@ gm_status gm_batch_capture_pass(gm_batch* b, int32_t smoother, const double* par
     return guarded([&] {
         require(b != nullptr, "null batch");
         SmoothParams sp = parse_smooth_params(smoother, params);
+        require_batch_smoother(smoother);
         if (smoother == GM_SMOOTH_GETME) build_tables(b, true);
         if (eval_slot >= 0) ensure_slots(b, (uint32_t)eval_slot);
         drop_graph(b);
@@ -415,6 +426,7 @@ gm_status gm_batch_tune(gm_batch* b, int32_t smoother, const double* params, int
     return guarded([&] {
         require(b != nullptr, "null batch");
         SmoothParams sp = parse_smooth_params(smoother, params);
+        require_batch_smoother(smoother);
         if (smoother == GM_SMOOTH_GETME) build_tables(b, true);
         for (gm_mesh* m : b->meshes)
         {

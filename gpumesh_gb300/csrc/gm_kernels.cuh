@@ -7,7 +7,7 @@
 namespace gm {
 
 constexpr int kWarp = 32;
-enum : int { kSmoothNM = 0, kSmoothGD = 1, kSmoothSpawn = 2, kSmoothGetme = 3 };
+enum : int { kSmoothNM = 0, kSmoothGD = 1, kSmoothSpawn = 2, kSmoothGetme = 3, kSmoothSpring = 4, kSmoothQLaplace = 5 };
 constexpr int kMaxCand = 64;  // spawn search evaluates 64 candidates at once
 
 // evaluation output (QualityHistogram, DataStructures/QualityHistogram.h:72-75)
@@ -823,6 +823,106 @@ __device__ V3<float> spawn_search(const MeshView& m, const Crew& crew, const Smo
         __syncwarp();
     }
     return pos;
+}
+
+// ---------------------------------------------------------------------------
+// Laplace smoothers toward AbstractMeasurer::computeVertexEquilibrium
+// ---------------------------------------------------------------------------
+// Metric-free (Measurers/MetricFreeMeasurer.cpp:107-152): pos + the sum over
+// the incident elements of (p_i - pos) for every element vertex, over the sum
+// of (vertex count - 1).  Metric-wise (MetricWiseMeasurer.cpp:190-255): every
+// element vertex with d = p_i - pos != 0 adds w = sqrt(n . M(p_i) n),
+// n = d / |d|, to the weight and w d to the displacement.  Elements over the
+// lanes, then a warp reduction.
+template <int MAXK>
+__device__ V3<float> vertex_equilibrium(const MeshView& m, const Crew& crew, uint32_t v, V3<float> pos, int lane)
+{
+    const bool wise = crew.measurer == kMeasurerMetricWise;
+    const uint32_t b = m.ve_off[v], e = m.ve_off[v + 1];
+    V3<float> disp = mk(0.f, 0.f, 0.f);
+    float weight = 0.f;
+    for (uint32_t i = b + lane; i < e; i += kWarp)
+    {
+        const uint32_t r = m.ve[i];
+        const int type = MAXK == 4 ? kTet : ref_type(r);
+        uint32_t vid[8];
+        elem_vertices(m, type, ref_id(r), vid);
+        const int n = MAXK == 4 ? 4 : type_size(type);
+        if (!wise) weight += (float)(n - 1);
+#pragma unroll
+        for (int k = 0; k < MAXK; ++k)
+        {
+            if (k >= n) break;
+            const V3<float> p = to<float>(__ldcg(&m.pos[vid[k]]));
+            const V3<float> d = p - pos;
+            if (!wise) disp = disp + d;
+            else if (d.x != 0.f || d.y != 0.f || d.z != 0.f)
+            {
+                const float w = sqrtf(quad_form(metric_at(crew, p), normalize(d)));
+                weight += w;
+                disp = disp + d * w;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        disp.x += __shfl_xor_sync(0xffffffffu, disp.x, o);
+        disp.y += __shfl_xor_sync(0xffffffffu, disp.y, o);
+        disp.z += __shfl_xor_sync(0xffffffffu, disp.z, o);
+        weight += __shfl_xor_sync(0xffffffffu, weight, o);
+    }
+    return pos + disp * (1.f / weight);
+}
+
+// SpringLaplaceSmoother::smoothVertices (Smoothers/VertexWise/SpringLaplaceSmoother.cpp:51-78):
+// mix(pos, equilibrium, moveCoeff) = pos + moveCoeff (equilibrium - pos), projected
+template <int MAXK>
+__device__ V3<float> spring_laplace(const MeshView& m, const Crew& crew, const SmoothParams& sp, uint32_t v, int cid,
+                                    V3<float> pos, int lane)
+{
+    const V3<float> c = vertex_equilibrium<MAXK>(m, crew, v, pos, lane);
+    const V3<float> out = pos + (c - pos) * sp.shift;
+    return cid != 0 ? snap(m, cid, out) : out;
+}
+
+// QualityLaplaceSmoother::smoothVertices (Smoothers/VertexWise/QualityLaplaceSmoother.cpp:55-129):
+// 8 propositions pos + shift * {-0.25, 0, 0.1, 0.2, 0.4, 0.8, 1.2, 1.6} along
+// shift = moveCoeff (equilibrium - pos), projected, evaluated at once; the
+// first best patch quality wins
+template <int VAR, int MAXK>
+__device__ V3<float> quality_laplace(const MeshView& m, const Crew& crew, const SmoothParams& sp, WarpPatch& P,
+                                     uint32_t v, int cid, V3<float> pos, int lane, int& evals)
+{
+    const V3<float> c = vertex_equilibrium<MAXK>(m, crew, v, pos, lane);
+    const V3<float> shift = (c - pos) * sp.shift;
+    V3<float> mine = pos;
+    if (lane < 8)
+    {
+        V3<float> x = pos + shift * gd_offset(lane);
+        if (cid != 0) x = snap(m, cid, x);
+        P.cand[lane] = make_float4(x.x, x.y, x.z, 0.f);
+        mine = x;
+    }
+    __syncwarp();
+    patch_multi<VAR, MAXK, float>(crew, P, 8, lane);
+    evals += 8;
+    int best = 0;
+    float bestQ = -3.0e38f;
+    for (int p = 0; p < 8; ++p)
+    {
+        const float q = P.res[p];
+        if (q > bestQ)
+        {
+            bestQ = q;
+            best = p;
+        }
+    }
+    V3<float> out;
+    out.x = __shfl_sync(0xffffffffu, mine.x, best);
+    out.y = __shfl_sync(0xffffffffu, mine.y, best);
+    out.z = __shfl_sync(0xffffffffu, mine.z, best);
+    __syncwarp();
+    return out;
 }
 
 // ---------------------------------------------------------------------------

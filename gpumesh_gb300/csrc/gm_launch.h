@@ -37,6 +37,8 @@ struct RelocLaunch
 cudaError_t launch_relocate_nm(const RelocLaunch& L);
 cudaError_t launch_relocate_gd(const RelocLaunch& L);
 cudaError_t launch_relocate_spawn(const RelocLaunch& L);
+cudaError_t launch_relocate_spring(const RelocLaunch& L);
+cudaError_t launch_relocate_qlaplace(const RelocLaunch& L);
 cudaError_t launch_getme_update(const RelocLaunch& L, const float4* corners);
 // FP64 acceptance of the vertices the preceding launch deferred
 cudaError_t launch_accept(const RelocLaunch& L);

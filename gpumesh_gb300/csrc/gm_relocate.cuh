@@ -58,6 +58,13 @@ __global__ void __launch_bounds__(128) relocate_kernel(MeshView m, Crew crew, Sm
     const int cid = m.cid[v];
     const float4 old = m.pos[v];
     const V3<float> pos = to<float>(old);
+    if constexpr (SMOOTHER == kSmoothSpring)
+    {
+        // no quality test: the reference moves the vertex unconditionally
+        const V3<float> out = spring_laplace<MAXK>(m, crew, sp, v, cid, pos, lane);
+        if (lane == 0) m.pos[v] = make_float4(out.x, out.y, out.z, old.w);
+        return;
+    }
     stage_patch_fp32<VAR, MAXK>(m, crew, v, pos, P, lane);
     int evals = 1;
     const float q0 = patch_uniform<VAR, MAXK, float>(crew, P, pos, lane);
@@ -65,6 +72,8 @@ __global__ void __launch_bounds__(128) relocate_kernel(MeshView m, Crew crew, Sm
     if (SMOOTHER == kSmoothNM) out = nelder_mead<VAR, MAXK>(m, crew, sp, P, v, cid, pos, q0, lane, evals);
     else if (SMOOTHER == kSmoothGD)
         out = gradient_descent<VAR, MAXK>(m, crew, sp, P, v, cid, pos, lane, evals);
+    else if (SMOOTHER == kSmoothQLaplace)
+        out = quality_laplace<VAR, MAXK>(m, crew, sp, P, v, cid, pos, lane, evals);
     else out = spawn_search<VAR, MAXK>(m, crew, sp, P, v, cid, pos, lane, evals);
     ++evals;
     const float q1 = patch_uniform<VAR, MAXK, float>(crew, P, out, lane);

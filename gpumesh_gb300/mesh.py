@@ -542,8 +542,17 @@ class GetmeSmoother(AbstractSmoother):
     element_wise = True
 
 
+class SpringLaplaceSmoother(AbstractSmoother):
+    kind = "spring_laplace"
+
+
+class QualityLaplaceSmoother(AbstractSmoother):
+    kind = "quality_laplace"
+
+
 SMOOTHER_CLASSES = {"nelder_mead": NelderMeadSmoother, "gradient_descent": GradientDescentSmoother,
-                    "spawn_search": SpawnSearchSmoother, "getme": GetmeSmoother}
+                    "spawn_search": SpawnSearchSmoother, "getme": GetmeSmoother,
+                    "spring_laplace": SpringLaplaceSmoother, "quality_laplace": QualityLaplaceSmoother}
 
 
 class Batch:

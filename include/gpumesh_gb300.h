@@ -66,6 +66,8 @@ typedef int gm_status;
 #define GM_SMOOTH_GRADIENT_DESCENT 1
 #define GM_SMOOTH_SPAWN_SEARCH 2
 #define GM_SMOOTH_GETME 3
+#define GM_SMOOTH_SPRING_LAPLACE 4  /* SpringLaplaceSmoother: params[0] = move coefficient (0.35) */
+#define GM_SMOOTH_QUALITY_LAPLACE 5 /* QualityLaplaceSmoother: params[0] = move coefficient (0.35) */
 
 #define GM_HIST_BUCKETS 20
 
@@ -91,6 +93,10 @@ typedef struct gm_quality
  *   spawn [move coefficient (1/20), iterations (2)]
  *          Smoothers/VertexWise/SpawnSearchSmoother.cpp:14,181
  *   GETMe [lambda (0.78)]  Smoothers/ElementWise/GetmeSmoother.cpp:22
+ *   spring Laplace  [move coefficient (0.35)]
+ *          Smoothers/VertexWise/SpringLaplaceSmoother.cpp:10
+ *   quality Laplace [move coefficient (0.35)]
+ *          Smoothers/VertexWise/QualityLaplaceSmoother.cpp:12
  * A NULL params pointer selects the defaults. */
 #define GM_PARAMS 8
 

@@ -1138,6 +1138,88 @@ static void gd_vertex(om_mesh* m, uint32_t vId, const smooth_params* sp, int64_t
     }
 }
 
+/* AbstractMeasurer::computeVertexEquilibrium.  Metric-free
+ * (Measurers/MetricFreeMeasurer.cpp:107-152): pos plus the sum over the
+ * incident elements of (p_i - pos) for every element vertex, over the sum of
+ * (vertex count - 1).  Metric-wise (Measurers/MetricWiseMeasurer.cpp:190-255,
+ * sumNode): every element vertex with d = p_i - pos != 0 adds weight
+ * w = sqrt(n . M(p_i) n), n = d / |d|, and w d. */
+static v3 vertex_equilibrium(const om_mesh* m, uint32_t v)
+{
+    const v3 pos = P(m, v);
+    double totalWeight = 0.0;
+    v3 displacement = V(0.0, 0.0, 0.0);
+    for (int64_t i = m->ne_base[v]; i < m->ne_base[v + 1]; ++i)
+    {
+        int n;
+        const uint32_t* ev = elem_verts(m, m->ne[i].type, m->ne[i].id, &n);
+        if (m->measurer == OM_MEASURER_METRIC_WISE)
+        {
+            for (int k = 0; k < n; ++k)
+            {
+                const v3 p = P(m, ev[k]);
+                const v3 d = sub(p, pos);
+                if (d.x != 0.0 || d.y != 0.0 || d.z != 0.0)
+                {
+                    const v3 nn = normalize(d);
+                    const m3 Mm = metric_at(m, p);
+                    const double weight = sqrt(dot(nn, mmulv(Mm, nn)));
+                    totalWeight += weight;
+                    displacement = add(displacement, mul(d, weight));
+                }
+            }
+        }
+        else
+        {
+            totalWeight += n - 1;
+            for (int k = 0; k < n; ++k) displacement = add(displacement, sub(P(m, ev[k]), pos));
+        }
+    }
+    return add(pos, dvs(displacement, totalWeight));
+}
+
+/* SpringLaplaceSmoother::smoothVertices (Smoothers/VertexWise/
+ * SpringLaplaceSmoother.cpp:51-78): pos = mix(pos, equilibrium, moveCoeff),
+ * mix(x, y, a) = x + a (y - x), then the boundary projection */
+static void spring_vertex(om_mesh* m, uint32_t vId, const smooth_params* sp)
+{
+    const double moveCoeff = sp->p[0];
+    const v3 pos = P(m, vId);
+    const v3 center = vertex_equilibrium(m, vId);
+    v3 out = add(pos, mul(sub(center, pos), moveCoeff));
+    if (is_constrained(m, vId)) out = snap(m, vId, out);
+    setP(m, vId, out);
+}
+
+/* QualityLaplaceSmoother::smoothVertices (Smoothers/VertexWise/
+ * QualityLaplaceSmoother.cpp:55-129): 8 propositions pos + shift * OFFSETS[p]
+ * along shift = (equilibrium - pos) * moveCoeff, projected, the first best
+ * patch quality kept */
+static void qlaplace_vertex(om_mesh* m, uint32_t vId, const smooth_params* sp, int64_t* evals)
+{
+    static const double OFFSETS[8] = {-0.25, 0.00, 0.10, 0.20, 0.40, 0.80, 1.20, 1.60};
+    const double moveCoeff = sp->p[0];
+    const v3 pos = P(m, vId);
+    const v3 center = vertex_equilibrium(m, vId);
+    const v3 shift = mul(sub(center, pos), moveCoeff);
+    v3 props[8];
+    for (int p = 0; p < 8; ++p) props[p] = add(pos, mul(shift, OFFSETS[p]));
+    if (is_constrained(m, vId))
+        for (int p = 0; p < 8; ++p) props[p] = snap(m, vId, props[p]);
+    int best = 0;
+    double bestQ = -INFINITY;
+    for (int p = 0; p < 8; ++p)
+    {
+        const double q = eval_at(m, vId, props[p], evals);
+        if (q > bestQ)
+        {
+            bestQ = q;
+            best = p;
+        }
+    }
+    setP(m, vId, props[best]);
+}
+
 /* SpawnSearchSmoother offsets (SpawnSearchSmoother.cpp:33-55) and
  * smoothVertices (SpawnSearchSmoother.cpp:161-226) */
 static v3 SPAWN_OFFSETS[64];
@@ -1390,6 +1472,8 @@ static void* pass_worker(void* arg)
             case OM_SMOOTH_GRADIENT_DESCENT: gd_vertex(c->m, v, &c->sp, &evals); break;
             case OM_SMOOTH_SPAWN_SEARCH: spawn_vertex(c->m, v, &c->sp, &evals); break;
             case OM_SMOOTH_GETME: getme_update_vertex(c->m, v, c->corner_base, c->corners, &evals); break;
+            case OM_SMOOTH_SPRING_LAPLACE: spring_vertex(c->m, v, &c->sp); break;
+            case OM_SMOOTH_QUALITY_LAPLACE: qlaplace_vertex(c->m, v, &c->sp, &evals); break;
             default: break;
             }
         }

@@ -51,6 +51,8 @@ extern "C" {
 #define OM_SMOOTH_GRADIENT_DESCENT 1
 #define OM_SMOOTH_SPAWN_SEARCH 2
 #define OM_SMOOTH_GETME 3
+#define OM_SMOOTH_SPRING_LAPLACE 4
+#define OM_SMOOTH_QUALITY_LAPLACE 5
 
 #define OM_HIST_BUCKETS 20
 
@@ -90,6 +92,7 @@ void om_evaluate(const om_mesh* m, double* out, int32_t nthreads);
  *   GD:    [node_shift_factor, security_cycles]
  *   spawn: [move_coeff, iterations]
  *   GETMe: [lambda]
+ *   spring / quality Laplace: [move_coeff]
  */
 void om_smooth_pass(om_mesh* m, int32_t smoother, const double* params,
                     int64_t ngroups, const int64_t* group_base,

@@ -19,16 +19,19 @@ LIB_PATH = os.path.join(BUILD_DIR, "libgm_oracle.so")
 SAMPLER = {"uniform": 0, "analytic": 1, "sine": 2}
 MEASURER = {"metric_free": 0, "metric_wise": 1}
 EVALUATOR = {"mean_ratio": 0, "metric_conformity": 1}
-SMOOTHER = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3}
+SMOOTHER = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3, "spring_laplace": 4,
+            "quality_laplace": 5}
 
 # Reference constants (Smoothers/VertexWise/NelderMeadSmoother.cpp:17-23,
 # GradientDescentSmoother.cpp:14-15, SpawnSearchSmoother.cpp:14 and :181,
-# GetmeSmoother.cpp:22)
+# GetmeSmoother.cpp:22, SpringLaplaceSmoother.cpp:10, QualityLaplaceSmoother.cpp:12)
 REFERENCE_PARAMS = {
     "nelder_mead": [1.0 / 24.0, 12, 1e-4, 1.0, 0.5, 2.0],
     "gradient_descent": [1.0 / 75.0, 5],
     "spawn_search": [1.0 / 20.0, 2],
     "getme": [0.78],
+    "spring_laplace": [0.35],
+    "quality_laplace": [0.35],
 }
 
 

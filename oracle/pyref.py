@@ -14,7 +14,8 @@ import numpy as np
 import refbuild
 
 BOUNDARY = {"free": 0, "box": 1, "sphere": 2}
-SMOOTHER = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3}
+SMOOTHER = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3, "spring_laplace": 4,
+            "quality_laplace": 5}
 SAMPLER = {"uniform": 0, "analytic": 1, "sine": 2}
 EVALUATOR = {"mean_ratio": 0, "metric_conformity": 1}
 

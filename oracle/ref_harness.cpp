@@ -35,7 +35,9 @@
 #include "Smoothers/ElementWise/VertexAccum.h"
 #include "Smoothers/VertexWise/GradientDescentSmoother.h"
 #include "Smoothers/VertexWise/NelderMeadSmoother.h"
+#include "Smoothers/VertexWise/QualityLaplaceSmoother.h"
 #include "Smoothers/VertexWise/SpawnSearchSmoother.h"
+#include "Smoothers/VertexWise/SpringLaplaceSmoother.h"
 
 namespace {
 
@@ -219,8 +221,9 @@ double ref_local_size(void* h, int64_t v)
     return r->crew.measurer().computeLocalElementSize(r->mesh, (uint)v);
 }
 
-// smoother: 0 NM, 1 GD, 2 spawn (reference "Thread" driver, colour-major),
-// 3 GETMe (colour-major replay of the Serial driver)
+// smoother: 0 NM, 1 GD, 2 spawn, 4 spring Laplace, 5 quality Laplace
+// (reference "Thread" driver, colour-major), 3 GETMe (colour-major replay of
+// the Serial driver)
 void ref_smooth(void* h, int smoother, int passes)
 {
     Ref* r = static_cast<Ref*>(h);
@@ -233,6 +236,8 @@ void ref_smooth(void* h, int smoother, int passes)
     std::unique_ptr<AbstractSmoother> s;
     if (smoother == 0) s.reset(new NelderMeadSmoother());
     else if (smoother == 1) s.reset(new GradientDescentSmoother());
+    else if (smoother == 4) s.reset(new SpringLaplaceSmoother());
+    else if (smoother == 5) s.reset(new QualityLaplaceSmoother());
     else s.reset(new SpawnSearchSmoother());
     Schedule schedule;
     schedule.topoOperationEnabled = false;

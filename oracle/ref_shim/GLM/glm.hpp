@@ -223,6 +223,7 @@ template <class T> tmat2<T> transpose(const tmat2<T>& m) { return tmat2<T>(m[0][
 template <class T> tmat3<T> mix(const tmat3<T>& a, const tmat3<T>& b, T t) { return a + (b - a) * t; }
 template <class T> T mix(T a, T b, T t) { return a + t * (b - a); }
 template <class T> tvec3<T> mix(const tvec3<T>& a, const tvec3<T>& b, const tvec3<T>& t) { return a + t * (b - a); }
+template <class T> tvec3<T> mix(const tvec3<T>& a, const tvec3<T>& b, T t) { return a + t * (b - a); }
 
 // rotation by `angle` radians about `axis`, composed on the right of m
 template <class T> tmat4<T> rotate(const tmat4<T>& m, T angle, const tvec3<T>& v)

@@ -29,6 +29,8 @@ void installCudaNelderMeadSmoother(float, int, float, float, float, float, float
     cuda_driver_called("installCudaNelderMeadSmoother");
 }
 void installCudaGradientDescentSmoother(int, float) { cuda_driver_called("installCudaGradientDescentSmoother"); }
+void installCudaSpringLaplaceSmoother(float) { cuda_driver_called("installCudaSpringLaplaceSmoother"); }
+void installCudaQualityLaplaceSmoother(float) { cuda_driver_called("installCudaQualityLaplaceSmoother"); }
 void installCudaSpawnSearchSmoother(float, const std::vector<glm::vec4>)
 {
     cuda_driver_called("installCudaSpawnSearchSmoother");

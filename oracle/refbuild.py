@@ -33,7 +33,8 @@ SOURCES = [
     "Boundaries/Constraints/FaceConstraint.cpp", "Boundaries/Constraints/VolumeConstraint.cpp",
     "Smoothers/AbstractSmoother.cpp", "Smoothers/VertexWise/AbstractVertexWiseSmoother.cpp",
     "Smoothers/VertexWise/NelderMeadSmoother.cpp", "Smoothers/VertexWise/GradientDescentSmoother.cpp",
-    "Smoothers/VertexWise/SpawnSearchSmoother.cpp", "Smoothers/ElementWise/AbstractElementWiseSmoother.cpp",
+    "Smoothers/VertexWise/SpawnSearchSmoother.cpp", "Smoothers/VertexWise/SpringLaplaceSmoother.cpp",
+    "Smoothers/VertexWise/QualityLaplaceSmoother.cpp", "Smoothers/ElementWise/AbstractElementWiseSmoother.cpp",
     "Smoothers/ElementWise/GetmeSmoother.cpp", "Smoothers/ElementWise/VertexAccum.cpp",
     "Topologists/AbstractTopologist.cpp", "Topologists/BatrTopologist.cpp",
 ]

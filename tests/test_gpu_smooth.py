@@ -220,3 +220,60 @@ def test_host_mirror_api_matches_the_c_abi_path():
     h2 = dev.evaluate()
     assert hist.minimumQuality() == h2.minimumQuality() and hist.harmonicMean() == h2.harmonicMean()
     assert hist.harmonicMean() > sm.passes[0].histogram.harmonicMean()
+
+
+# ---- Laplace smoothers (SpringLaplaceSmoother, QualityLaplaceSmoother) ----
+# Both move toward AbstractMeasurer::computeVertexEquilibrium: spring
+# Laplace without a quality test (no decision, so every vertex agrees with
+# the oracle to FP32 rounding), quality Laplace by the best of 8 patch
+# qualities along the same line (rare near-tie decisions may differ).
+
+@pytest.mark.parametrize("kind", ["tet", "mixed", "hex"])
+def test_spring_laplace_one_colour_matches_oracle_per_vertex(kind):
+    raw, groups = coloured(meshgen.box_mesh(8, kind, 0.25, 3))
+    for g in range(2):
+        err = one_colour(raw, groups, MR, "spring_laplace", None, g)
+        assert err.max() < 1e-5, np.sort(err)[-5:]
+
+
+@pytest.mark.parametrize("kind", ["tet", "mixed"])
+def test_quality_laplace_one_colour_matches_oracle_per_vertex(kind):
+    raw, groups = coloured(meshgen.box_mesh(8, kind, 0.25, 3))
+    for g in range(2):
+        err = one_colour(raw, groups, MR, "quality_laplace", None, g)
+        assert np.mean(err < 1e-4) >= 0.97, np.sort(err)[-10:]
+        assert np.median(err) < 1e-5
+
+
+def test_laplace_metric_wise_equilibrium_on_sphere():
+    # metric-wise measurer: each node weighted by sqrt(n . M(p_i) n) under the sine metric
+    raw, groups = coloured(meshgen.sphere_mesh(14, 0.25, 1))
+    crew = dict(sampler="sine", measurer="metric_wise", evaluator="metric_conformity", scaling=1.0 / raw.h)
+    err = one_colour(raw, groups, crew, "spring_laplace", None, 0)
+    assert err.max() < 1e-5, np.sort(err)[-5:]
+    err = one_colour(raw, groups, crew, "quality_laplace", None, 0)
+    assert np.mean(err < 1e-4) >= 0.97
+    assert np.median(err) < 1e-5
+
+
+def test_laplace_passes_quality_against_oracle():
+    raw, groups = coloured(meshgen.box_mesh(10, "tet", 0.3, 0))
+    for smoother in ("spring_laplace", "quality_laplace"):
+        gpos, opos, gq, oq, dev = run_both(raw, groups, MR, [(smoother, 3, None)])
+        assert abs(gq["min"] - oq["min"]) <= 1e-4, (smoother, gq["min"], oq["min"])
+        if np.isfinite(oq["inv_sum"]) and np.isfinite(gq["inv_sum"]):
+            assert abs(gq["mean"] - oq["mean"]) <= 1e-4, (smoother, gq["mean"], oq["mean"])
+        # box vertices stay on their faces
+        assert np.abs(np.abs(gpos[raw.cid > 0]).max(axis=1) - 1.0).max() < 1e-6
+
+
+def test_laplace_smoothers_not_on_the_batched_path():
+    from gpumesh_gb300 import mesh as M
+    from gpumesh_gb300 import _native as N
+
+    raw, groups = coloured(meshgen.box_mesh(4, "tet", 0.3, 0))
+    d = device_for(raw, groups, MR)
+    b = M.Batch([d])
+    with pytest.raises(N.GpuMeshError) as e:
+        b.smooth_pass("spring_laplace", None)
+    assert "Laplace" in str(e.value)

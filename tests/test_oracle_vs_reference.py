@@ -92,6 +92,18 @@ def test_vertex_smoothers_match_reference(case, smoother):
     assert np.array_equal(ref.pos, orc.pos)
 
 
+# the Laplace smoothers move toward AbstractMeasurer::computeVertexEquilibrium:
+# metric-free on the box cases, metric-wise (analytic and sine samplers) on
+# the others
+@pytest.mark.parametrize("case", ["tet_box", "mixed_box", "hex_box", "sphere_mc", "mixed_analytic_mr"])
+@pytest.mark.parametrize("smoother", ["spring_laplace", "quality_laplace"])
+def test_laplace_smoothers_match_reference(case, smoother):
+    raw, ref, perm, groups, pr, orc = setup(case)
+    ref.smooth(smoother, 1)
+    orc.smooth_pass(smoother, groups.group_base, groups.members, nthreads=4)
+    assert np.array_equal(ref.pos, orc.pos)
+
+
 @pytest.mark.parametrize("case", ["hex_box", "mixed_box", "tet_box"])
 def test_getme_matches_reference(case):
     raw, ref, perm, groups, pr, orc = setup(case)
