@@ -383,6 +383,19 @@ class Mesh:
     def verts(self, value):
         self.raw.pos = np.ascontiguousarray(value, np.float64)
 
+    @classmethod
+    def fromJson(cls, path: str) -> "Mesh":
+        """A mesh file in the reference tool's JSON layout (JsonDeserializer)."""
+        from .meshio import read_json
+
+        return cls(read_json(path))
+
+    def toJson(self, path: str, precision: str = "exact"):
+        """Write the mesh in the reference tool's JSON layout (JsonSerializer)."""
+        from .meshio import write_json
+
+        write_json(path, self.raw, model=self.modelName, precision=precision)
+
     def compileTopology(self):
         perm, groups = node_groups_build(self.raw, permute=True)
         self.raw = permute_mesh(self.raw, perm)

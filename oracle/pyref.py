@@ -13,7 +13,7 @@ import numpy as np
 
 import refbuild
 
-BOUNDARY = {"free": 0, "box": 1, "sphere": 2}
+BOUNDARY = {"free": 0, "box": 1, "sphere": 2, "tet": 3, "pipe": 4, "shell": 5}
 SMOOTHER = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3, "spring_laplace": 4,
             "quality_laplace": 5}
 SAMPLER = {"uniform": 0, "analytic": 1, "sine": 2}
@@ -33,6 +33,15 @@ def lib():
         L = ctypes.CDLL(path)
         vp, i64, i32, dbl = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_double
         L.ref_create.restype = vp
+        cp = ctypes.c_char_p
+        L.ref_json_write.restype = i32
+        L.ref_json_write.argtypes = [cp, cp, i32, i64, vp, vp, i64, vp, i64, vp, i64, vp]
+        L.ref_json_read.restype = vp
+        L.ref_json_read.argtypes = [cp]
+        L.ref_json_counts.argtypes = [vp, vp]
+        L.ref_json_get.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, vp, i64]
+        L.ref_json_destroy.argtypes = [vp]
+        L.ref_boundary_project.argtypes = [i32, i32, i64, vp, vp]
         L.ref_create.argtypes = [i32, i64, vp, vp, i64, vp, i64, vp, i64, vp]
         L.ref_destroy.argtypes = [vp]
         L.ref_get_perm.argtypes = [vp, vp]
@@ -126,3 +135,46 @@ class RefMesh:
     def pos(self, v):
         a = np.ascontiguousarray(v, np.float64)
         lib().ref_set_pos(self.h, _p(a))
+
+
+def json_write(path: str, raw, boundary: str, model: str = "") -> None:
+    """The reference's JsonSerializer on the mesh as given (no permutation)."""
+    p = np.ascontiguousarray(raw.pos, np.float64)
+    c = np.ascontiguousarray(raw.cid, np.int32)
+    t, r, h = (np.ascontiguousarray(a, np.uint32) for a in (raw.tets, raw.pris, raw.hexs))
+    ok = lib().ref_json_write(path.encode(), model.encode(), BOUNDARY[boundary], p.shape[0], _p(p), _p(c),
+                              t.shape[0], _p(t), r.shape[0], _p(r), h.shape[0], _p(h))
+    if not ok:
+        raise OSError(f"reference JsonSerializer could not write {path}")
+
+
+def json_read(path: str) -> dict:
+    """The reference's JsonDeserializer: positions, constraint ids,
+    connectivity, model and boundary names."""
+    L = lib()
+    h = L.ref_json_read(path.encode())
+    if not h:
+        raise OSError(f"reference JsonDeserializer could not read {path}")
+    try:
+        n = np.zeros(5, np.int64)
+        L.ref_json_counts(h, _p(n))
+        pos = np.zeros((n[0], 3), np.float64)
+        cid = np.zeros(n[1], np.int32)
+        tets = np.zeros((n[2], 4), np.uint32)
+        pris = np.zeros((n[3], 6), np.uint32)
+        hexs = np.zeros((n[4], 8), np.uint32)
+        model = ctypes.create_string_buffer(4096)
+        bound = ctypes.create_string_buffer(256)
+        L.ref_json_get(h, _p(pos), _p(cid), _p(tets), _p(pris), _p(hexs), model, 4096, bound, 256)
+        return dict(pos=pos, cid=cid, tets=tets, pris=pris, hexs=hexs, model=model.value.decode(),
+                    boundary=bound.value.decode())
+    finally:
+        L.ref_json_destroy(h)
+
+
+def boundary_project(boundary: str, cid: int, pts: np.ndarray) -> np.ndarray:
+    """The reference boundary's constraint `cid` applied to each point."""
+    p = np.ascontiguousarray(pts, np.float64)
+    out = np.zeros_like(p)
+    lib().ref_boundary_project(BOUNDARY[boundary], int(cid), p.shape[0], _p(p), _p(out))
+    return out

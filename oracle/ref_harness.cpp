@@ -12,6 +12,7 @@
 // smoothHexs / updateVertexPositions.  The sine-graded metric is added as a
 // sampler plugin through AbstractSampler's interface.
 #include <cmath>
+#include <cstdio>
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -19,7 +20,10 @@
 
 #include "Boundaries/BoundaryFree.h"
 #include "Boundaries/BoxBoundary.h"
+#include "Boundaries/PipeBoundary.h"
+#include "Boundaries/ShellBoundary.h"
 #include "Boundaries/SphereBoundary.h"
+#include "Boundaries/TetBoundary.h"
 #include "DataStructures/Mesh.h"
 #include "DataStructures/MeshCrew.h"
 #include "DataStructures/NodeGroups.h"
@@ -38,6 +42,8 @@
 #include "Smoothers/VertexWise/QualityLaplaceSmoother.h"
 #include "Smoothers/VertexWise/SpawnSearchSmoother.h"
 #include "Smoothers/VertexWise/SpringLaplaceSmoother.h"
+#include "Serialization/JsonDeserializer.h"
+#include "Serialization/JsonSerializer.h"
 
 namespace {
 
@@ -85,6 +91,49 @@ public:
     }
 };
 
+// 0 free, 1 box, 2 sphere, 3 tet, 4 pipe, 5 shell
+std::shared_ptr<AbstractBoundary> make_boundary(int b)
+{
+    switch (b)
+    {
+    case 1: return std::shared_ptr<AbstractBoundary>(new BoxBoundary());
+    case 2: return std::shared_ptr<AbstractBoundary>(new SphereBoundary());
+    case 3: return std::shared_ptr<AbstractBoundary>(new TetBoundary());
+    case 4: return std::shared_ptr<AbstractBoundary>(new PipeBoundary());
+    case 5: return std::shared_ptr<AbstractBoundary>(new ShellBoundary());
+    default: return std::shared_ptr<AbstractBoundary>(new BoundaryFree());
+    }
+}
+
+void fill_mesh(Mesh& mesh, const std::shared_ptr<AbstractBoundary>& b, int64_t nv, const double* pos,
+               const int32_t* cid, int64_t nt, const uint32_t* tets, int64_t np, const uint32_t* pris, int64_t nh,
+               const uint32_t* hexs)
+{
+    mesh.setBoundary(b);
+    for (int64_t v = 0; v < nv; ++v)
+    {
+        mesh.verts.push_back(MeshVert(glm::dvec3(pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]), (uint)v));
+        mesh.topos.push_back(MeshTopo(b->constraint(cid[v])));
+    }
+    for (int64_t i = 0; i < nt; ++i)
+        mesh.tets.push_back(MeshTet(tets[4 * i], tets[4 * i + 1], tets[4 * i + 2], tets[4 * i + 3]));
+    for (int64_t i = 0; i < np; ++i)
+    {
+        const uint32_t* e = pris + 6 * i;
+        mesh.pris.push_back(MeshPri(e[0], e[1], e[2], e[3], e[4], e[5]));
+    }
+    for (int64_t i = 0; i < nh; ++i)
+    {
+        const uint32_t* e = hexs + 8 * i;
+        mesh.hexs.push_back(MeshHex(e[0], e[1], e[2], e[3], e[4], e[5], e[6], e[7]));
+    }
+}
+
+struct RefJson
+{
+    Mesh mesh;
+};
+
 struct Ref
 {
     Mesh mesh;
@@ -98,32 +147,13 @@ struct Ref
 
 extern "C" {
 
-// boundary: 0 free, 1 box, 2 sphere; cid: constraint id per vertex
+// boundary: 0 free, 1 box, 2 sphere, 3 tet; cid: constraint id per vertex
 void* ref_create(int boundary, int64_t nv, const double* pos, const int32_t* cid, int64_t nt, const uint32_t* tets,
                  int64_t np, const uint32_t* pris, int64_t nh, const uint32_t* hexs)
 {
     Ref* r = new Ref();
-    if (boundary == 1) r->boundary.reset(new BoxBoundary());
-    else if (boundary == 2) r->boundary.reset(new SphereBoundary());
-    else r->boundary.reset(new BoundaryFree());
-    r->mesh.setBoundary(r->boundary);
-    for (int64_t v = 0; v < nv; ++v)
-    {
-        r->mesh.verts.push_back(MeshVert(glm::dvec3(pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]), (uint)v));
-        r->mesh.topos.push_back(MeshTopo(r->boundary->constraint(cid[v])));
-    }
-    for (int64_t i = 0; i < nt; ++i)
-        r->mesh.tets.push_back(MeshTet(tets[4 * i], tets[4 * i + 1], tets[4 * i + 2], tets[4 * i + 3]));
-    for (int64_t i = 0; i < np; ++i)
-    {
-        const uint32_t* e = pris + 6 * i;
-        r->mesh.pris.push_back(MeshPri(e[0], e[1], e[2], e[3], e[4], e[5]));
-    }
-    for (int64_t i = 0; i < nh; ++i)
-    {
-        const uint32_t* e = hexs + 8 * i;
-        r->mesh.hexs.push_back(MeshHex(e[0], e[1], e[2], e[3], e[4], e[5], e[6], e[7]));
-    }
+    r->boundary = make_boundary(boundary);
+    fill_mesh(r->mesh, r->boundary, nv, pos, cid, nt, tets, np, pris, nh, hexs);
     r->mesh.compileTopology(false);
     return r;
 }
@@ -259,6 +289,75 @@ void ref_set_pos(void* h, const double* in)
     Ref* r = static_cast<Ref*>(h);
     for (size_t i = 0; i < r->mesh.verts.size(); ++i)
         r->mesh.verts[i].p = glm::dvec3(in[3 * i], in[3 * i + 1], in[3 * i + 2]);
+}
+
+// ---- JSON mesh files (Serialization/JsonSerializer.cpp, JsonDeserializer.cpp) ----
+
+// JsonSerializer::serialize of a mesh given in arrays (before any topology
+// compilation); returns 1 on success
+int ref_json_write(const char* path, const char* model, int boundary, int64_t nv, const double* pos, const int32_t* cid,
+                   int64_t nt, const uint32_t* tets, int64_t np, const uint32_t* pris, int64_t nh, const uint32_t* hexs)
+{
+    Mesh mesh;
+    fill_mesh(mesh, make_boundary(boundary), nv, pos, cid, nt, tets, np, pris, nh, hexs);
+    mesh.modelName = model;
+    MeshCrew crew;
+    return JsonSerializer().serialize(path, crew, mesh) ? 1 : 0;
+}
+
+// JsonDeserializer::deserialize; null when it fails
+void* ref_json_read(const char* path)
+{
+    RefJson* r = new RefJson();
+    std::vector<MeshMetric> metrics;
+    if (!JsonDeserializer().deserialize(path, r->mesh, metrics))
+    {
+        delete r;
+        return nullptr;
+    }
+    return r;
+}
+
+// out: vertices, topos, tets, prisms, hexes
+void ref_json_counts(void* h, int64_t* out)
+{
+    const Mesh& m = static_cast<RefJson*>(h)->mesh;
+    out[0] = (int64_t)m.verts.size();
+    out[1] = (int64_t)m.topos.size();
+    out[2] = (int64_t)m.tets.size();
+    out[3] = (int64_t)m.pris.size();
+    out[4] = (int64_t)m.hexs.size();
+}
+
+void ref_json_get(void* h, double* pos, int32_t* cid, uint32_t* tets, uint32_t* pris, uint32_t* hexs, char* model,
+                  int64_t model_cap, char* bound, int64_t bound_cap)
+{
+    const Mesh& m = static_cast<RefJson*>(h)->mesh;
+    for (size_t i = 0; i < m.verts.size(); ++i)
+        for (int k = 0; k < 3; ++k) pos[3 * i + k] = m.verts[i].p[k];
+    for (size_t i = 0; i < m.topos.size(); ++i) cid[i] = m.topos[i].snapToBoundary->id();
+    for (size_t i = 0; i < m.tets.size(); ++i)
+        for (int k = 0; k < 4; ++k) tets[4 * i + k] = m.tets[i].v[k];
+    for (size_t i = 0; i < m.pris.size(); ++i)
+        for (int k = 0; k < 6; ++k) pris[6 * i + k] = m.pris[i].v[k];
+    for (size_t i = 0; i < m.hexs.size(); ++i)
+        for (int k = 0; k < 8; ++k) hexs[8 * i + k] = m.hexs[i].v[k];
+    std::snprintf(model, (size_t)model_cap, "%s", m.modelName.c_str());
+    std::snprintf(bound, (size_t)bound_cap, "%s", m.boundary().name().c_str());
+}
+
+void ref_json_destroy(void* h) { delete static_cast<RefJson*>(h); }
+
+// the boundary's constraint `id` applied to n points
+void ref_boundary_project(int boundary, int id, int64_t n, const double* in, double* out)
+{
+    std::shared_ptr<AbstractBoundary> b = make_boundary(boundary);
+    const AbstractConstraint* c = b->constraint(id);
+    for (int64_t i = 0; i < n; ++i)
+    {
+        const glm::dvec3 p = (*c)(glm::dvec3(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+        for (int k = 0; k < 3; ++k) out[3 * i + k] = p[k];
+    }
 }
 
 }  // extern "C"

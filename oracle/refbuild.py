@@ -28,6 +28,7 @@ SOURCES = [
     "Measurers/AbstractMeasurer.cpp", "Measurers/MetricFreeMeasurer.cpp", "Measurers/MetricWiseMeasurer.cpp",
     "Samplers/AbstractSampler.cpp", "Samplers/AnalyticSampler.cpp", "Samplers/UniformSampler.cpp",
     "Boundaries/AbstractBoundary.cpp", "Boundaries/BoxBoundary.cpp", "Boundaries/SphereBoundary.cpp",
+    "Boundaries/TetBoundary.cpp", "Boundaries/PipeBoundary.cpp", "Boundaries/ShellBoundary.cpp",
     "Boundaries/BoundaryFree.cpp", "Boundaries/Constraints/AbstractConstraint.cpp",
     "Boundaries/Constraints/VertexConstraint.cpp", "Boundaries/Constraints/EdgeConstraint.cpp",
     "Boundaries/Constraints/FaceConstraint.cpp", "Boundaries/Constraints/VolumeConstraint.cpp",
@@ -37,6 +38,8 @@ SOURCES = [
     "Smoothers/VertexWise/QualityLaplaceSmoother.cpp", "Smoothers/ElementWise/AbstractElementWiseSmoother.cpp",
     "Smoothers/ElementWise/GetmeSmoother.cpp", "Smoothers/ElementWise/VertexAccum.cpp",
     "Topologists/AbstractTopologist.cpp", "Topologists/BatrTopologist.cpp",
+    "Serialization/AbstractSerializer.cpp", "Serialization/AbstractDeserializer.cpp",
+    "Serialization/JsonSerializer.cpp", "Serialization/JsonDeserializer.cpp", "Serialization/JsonMeshTags.cpp",
 ]
 LOCAL = ["ref_harness.cpp", "ref_stubs.cpp"]
 FLAGS = ["-O2", "-std=c++14", "-fPIC", "-ffp-contract=off", "-w", "-DNDEBUG",

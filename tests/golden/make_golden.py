@@ -29,7 +29,7 @@ CASES = {
     "sphere_mc_8": (lambda: meshgen.sphere_mesh(8, 0.25, 1), "sphere",
                     dict(sampler="sine", evaluator="metric_conformity", scaling=4.0)),
 }
-SMOOTHERS = ["nelder_mead", "gradient_descent", "spawn_search", "getme"]
+SMOOTHERS = ["nelder_mead", "gradient_descent", "spawn_search", "getme", "spring_laplace", "quality_laplace"]
 
 
 def make(name):
@@ -53,7 +53,18 @@ def make(name):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
 
 
+# a small mesh file written by the reference's own JsonSerializer
+JSON_CASE = ("tet_box_2_ref.json", lambda: meshgen.box_mesh(2, "tet", 0.3, 0), "box", "box-tet-2")
+
+
+def make_json():
+    fname, build, boundary, model = JSON_CASE
+    pyref.json_write(os.path.join(HERE, fname), build(), boundary, model)
+
+
 if __name__ == "__main__":
     for n in CASES:
         make(n)
         print("wrote", n)
+    make_json()
+    print("wrote", JSON_CASE[0])

@@ -59,7 +59,8 @@ def test_evaluation_matches_golden(path):
 
 
 @pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p) for p in FIXTURES])
-@pytest.mark.parametrize("smoother", ["nelder_mead", "gradient_descent", "spawn_search", "getme"])
+@pytest.mark.parametrize("smoother", ["nelder_mead", "gradient_descent", "spawn_search", "getme", "spring_laplace",
+                                      "quality_laplace"])
 def test_smoothers_match_golden(path, smoother):
     d, raw = load(path)
     pr, orc = oracle(d, raw)
