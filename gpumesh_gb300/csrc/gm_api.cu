@@ -338,6 +338,41 @@ gm_status gm_node_groups_build(uint32_t nv, const int32_t* cid, uint32_t nt, con
     });
 }
 
+gm_status gm_mesh_neighbourhoods(uint32_t nv, uint32_t nt, const uint32_t* tets, uint32_t np, const uint32_t* pris,
+                                 uint32_t nh, const uint32_t* hexs, uint32_t* ve_off, uint32_t* ve, uint64_t* ve_len,
+                                 uint32_t* vv_off, uint32_t* vv, uint64_t* vv_len)
+{
+    return guarded([&] {
+        require(nv > 0 && ve_len && vv_len, "null argument");
+        require((nt == 0 || tets) && (np == 0 || pris) && (nh == 0 || hexs), "null connectivity");
+        check_conn(tets, (size_t)nt * 4, nv, "tet");
+        check_conn(pris, (size_t)np * 6, nv, "prism");
+        check_conn(hexs, (size_t)nh * 8, nv, "hex");
+        HostMeshView in;
+        in.nv = nv;
+        in.nt = nt;
+        in.np = np;
+        in.nh = nh;
+        in.tets = tets;
+        in.pris = pris;
+        in.hexs = hexs;
+        std::vector<uint32_t> eo, e, vo, v;
+        build_csr(in, eo, e, vo, v);
+        const bool fill = ve || vv;
+        if (fill)
+        {
+            require(ve && vv && ve_off && vv_off, "null output array");
+            require(*ve_len >= e.size() && *vv_len >= v.size(), "output arrays shorter than the neighbourhoods");
+            std::copy(eo.begin(), eo.end(), ve_off);
+            std::copy(e.begin(), e.end(), ve);
+            std::copy(vo.begin(), vo.end(), vv_off);
+            std::copy(v.begin(), v.end(), vv);
+        }
+        *ve_len = e.size();
+        *vv_len = v.size();
+    });
+}
+
 gm_status gm_mesh_create(gm_mesh** out)
 {
     return guarded([&] {

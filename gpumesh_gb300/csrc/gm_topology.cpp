@@ -20,6 +20,7 @@
 #include <cstdint>
 #include <cstring>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "gm_internal.h"
@@ -65,7 +66,31 @@ void fill_refs(const uint32_t* conn, uint32_t count, int type, std::vector<uint3
         }
 }
 
-// an element's edges, appended to the bounded per-vertex lists in `slot`
+// f(range, begin, end) over [0, n) in contiguous ranges, one per host thread
+// (a single range when n is small); returns the number of ranges
+template <class F>
+unsigned parallel_ranges(uint32_t n, F f)
+{
+    unsigned t = std::thread::hardware_concurrency();
+    t = std::min<unsigned>(t == 0 ? 1 : t, 16);
+    if (n < 65536 || t == 1)
+    {
+        f(0u, 0u, n);
+        return 1;
+    }
+    std::vector<std::thread> pool;
+    const uint32_t chunk = (n + t - 1) / t;
+    for (unsigned i = 0; i < t; ++i)
+    {
+        const uint32_t b = std::min<uint32_t>(n, i * chunk), e = std::min<uint32_t>(n, b + chunk);
+        pool.emplace_back(f, i, b, e);
+    }
+    for (std::thread& th : pool) th.join();
+    return t;
+}
+
+// Mesh::addEdge over every element's edges in element order, appending to
+// bounded per-vertex lists (the sequential form, for small meshes)
 template <int K, int NE>
 void add_edges(const uint32_t* conn, uint32_t count, const int (*edges)[2], const std::vector<uint32_t>& base,
                std::vector<uint32_t>& n, std::vector<uint32_t>& slot)
@@ -77,19 +102,46 @@ void add_edges(const uint32_t* conn, uint32_t count, const int (*edges)[2], cons
         {
             const uint32_t a = el[edges[k][0]], b = el[edges[k][1]];
             const uint32_t* la = slot.data() + base[a];
-            const uint32_t na = n[a];
             bool seen = false;
-            for (uint32_t j = 0; j < na; ++j)
-                if (la[j] == b)
-                {
-                    seen = true;
-                    break;
-                }
+            for (uint32_t j = 0; j < n[a] && !seen; ++j) seen = la[j] == b;
             if (seen) continue;
             slot[base[a] + n[a]++] = b;
             slot[base[b] + n[b]++] = a;
         }
     }
+}
+
+// The edge neighbours of vertex x.  Mesh::addEdge appends b to a's list and a
+// to b's when a's list does not hold b; the lists stay symmetric, so x's
+// list is the other ends of the edges at x in the order they are met:
+// x's elements in element order (its element refs), each element's edges in
+// edge-table order.  That makes every vertex independent of the others.
+uint32_t vertex_neighbours(const HostMeshView& in, const Neighbourhoods& nb, uint32_t x, uint32_t* out)
+{
+    uint32_t cnt = 0;
+    for (uint32_t j = nb.e_off[x]; j < nb.e_off[x + 1]; ++j)
+    {
+        const uint32_t r = nb.e[j];
+        const int type = (int)(r >> 30), local = (int)((r >> 27) & 7u);
+        const uint32_t id = r & kMaxElemId;
+        const uint32_t* el;
+        const int(*edges)[2];
+        int ne;
+        if (type == kTypeTet) { el = in.tets + 4 * (size_t)id; edges = kTetEdges; ne = 6; }
+        else if (type == kTypePri) { el = in.pris + 6 * (size_t)id; edges = kPriEdges; ne = 9; }
+        else { el = in.hexs + 8 * (size_t)id; edges = kHexEdges; ne = 12; }
+        for (int k = 0; k < ne; ++k)
+        {
+            uint32_t w;
+            if (edges[k][0] == local) w = el[edges[k][1]];
+            else if (edges[k][1] == local) w = el[edges[k][0]];
+            else continue;
+            bool seen = false;
+            for (uint32_t q = 0; q < cnt && !seen; ++q) seen = out[q] == w;
+            if (!seen) out[cnt++] = w;
+        }
+    }
+    return cnt;
 }
 
 Neighbourhoods build_neighbourhoods(const HostMeshView& in)
@@ -109,16 +161,43 @@ Neighbourhoods build_neighbourhoods(const HostMeshView& in)
 
     // every corner of a tet, prism or hex has three edges, so a vertex has at
     // most 3 x (its element count) distinct neighbours
-    std::vector<uint32_t> base((size_t)nv + 1, 0), n(nv, 0);
-    for (uint32_t x = 0; x < nv; ++x) base[x + 1] = base[x] + 3 * nb.elem_count(x);
-    std::vector<uint32_t> slot(base[nv]);
-    add_edges<4, 6>(in.tets, in.nt, kTetEdges, base, n, slot);
-    add_edges<6, 9>(in.pris, in.np, kPriEdges, base, n, slot);
-    add_edges<8, 12>(in.hexs, in.nh, kHexEdges, base, n, slot);
+    if (nv < 65536)
+    {
+        std::vector<uint32_t> base((size_t)nv + 1, 0), n(nv, 0);
+        for (uint32_t x = 0; x < nv; ++x) base[x + 1] = base[x] + 3 * nb.elem_count(x);
+        std::vector<uint32_t> slot(base[nv]);
+        add_edges<4, 6>(in.tets, in.nt, kTetEdges, base, n, slot);
+        add_edges<6, 9>(in.pris, in.np, kPriEdges, base, n, slot);
+        add_edges<8, 12>(in.hexs, in.nh, kHexEdges, base, n, slot);
+        nb.v_off.assign((size_t)nv + 1, 0);
+        for (uint32_t x = 0; x < nv; ++x) nb.v_off[x + 1] = nb.v_off[x] + n[x];
+        nb.v.resize(nb.v_off[nv]);
+        for (uint32_t x = 0; x < nv; ++x) std::copy_n(slot.begin() + base[x], n[x], nb.v.begin() + nb.v_off[x]);
+        return nb;
+    }
+    // large meshes: vertex by vertex on the host's threads, each range of
+    // vertices filling its own list, concatenated in order
+    uint32_t most = 0;
+    for (uint32_t x = 0; x < nv; ++x) most = std::max(most, nb.elem_count(x));
+    std::vector<uint32_t> n(nv, 0);
+    std::vector<std::vector<uint32_t>> lists(16);
+    std::vector<uint32_t> first(17, 0);
+    const unsigned ranges = parallel_ranges(nv, [&](unsigned r, uint32_t b, uint32_t e) {
+        std::vector<uint32_t>& out = lists[r];
+        std::vector<uint32_t> tmp(3 * (size_t)most + 1);
+        out.reserve((size_t)(e - b) * 16);
+        first[r] = b;
+        for (uint32_t x = b; x < e; ++x)
+        {
+            n[x] = vertex_neighbours(in, nb, x, tmp.data());
+            out.insert(out.end(), tmp.begin(), tmp.begin() + n[x]);
+        }
+    });
     nb.v_off.assign((size_t)nv + 1, 0);
     for (uint32_t x = 0; x < nv; ++x) nb.v_off[x + 1] = nb.v_off[x] + n[x];
     nb.v.resize(nb.v_off[nv]);
-    for (uint32_t x = 0; x < nv; ++x) std::copy_n(slot.begin() + base[x], n[x], nb.v.begin() + nb.v_off[x]);
+    for (unsigned r = 0; r < ranges; ++r)
+        std::copy(lists[r].begin(), lists[r].end(), nb.v.begin() + nb.v_off[first[r]]);
     return nb;
 }
 
@@ -307,13 +386,15 @@ Topology build_topology(const HostMeshView& in, bool permute)
     }
     t.ve.resize(t.ve_off[nv]);
     t.vv.resize(t.vv_off[nv]);
-    for (uint32_t p = 0; p < nv; ++p)
-    {
-        const uint32_t x = (uint32_t)order[p];
-        std::copy(nb.e.begin() + nb.e_off[x], nb.e.begin() + nb.e_off[x + 1], t.ve.begin() + t.ve_off[p]);
-        uint32_t o = t.vv_off[p];
-        for (uint32_t j = nb.v_off[x]; j < nb.v_off[x + 1]; ++j) t.vv[o++] = new_of_old[nb.v[j]];
-    }
+    parallel_ranges(nv, [&](unsigned, uint32_t b, uint32_t e) {
+        for (uint32_t p = b; p < e; ++p)
+        {
+            const uint32_t x = (uint32_t)order[p];
+            std::copy(nb.e.begin() + nb.e_off[x], nb.e.begin() + nb.e_off[x + 1], t.ve.begin() + t.ve_off[p]);
+            uint32_t o = t.vv_off[p];
+            for (uint32_t j = nb.v_off[x]; j < nb.v_off[x + 1]; ++j) t.vv[o++] = new_of_old[nb.v[j]];
+        }
+    });
     t.new_of_old = std::move(new_of_old);
     return t;
 }

@@ -219,6 +219,21 @@ def node_groups_build(raw: RawMesh, permute: bool = True):
     return perm, NodeGroups(gb[:g + 1].copy(), members[:gb[g]].copy(), ranges[:6 * g].copy())
 
 
+def neighbourhoods(raw: RawMesh):
+    """(ve_off, ve, vv_off, vv): the vertex neighbourhoods the library builds
+    for an upload (Mesh::compileNeighborhoods order, input indices)."""
+    L = N.lib()
+    t, r, h = (np.ascontiguousarray(a, np.uint32) for a in (raw.tets, raw.pris, raw.hexs))
+    el, vl = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    args = (raw.nv, t.shape[0], N.ptr(t), r.shape[0], N.ptr(r), h.shape[0], N.ptr(h))
+    N.check(L.gm_mesh_neighbourhoods(*args, None, None, ctypes.byref(el), None, None, ctypes.byref(vl)))
+    eo, vo = np.zeros(raw.nv + 1, np.uint32), np.zeros(raw.nv + 1, np.uint32)
+    e, v = np.zeros(el.value, np.uint32), np.zeros(vl.value, np.uint32)
+    N.check(L.gm_mesh_neighbourhoods(*args, N.ptr(eo), N.ptr(e), ctypes.byref(el), N.ptr(vo), N.ptr(v),
+                                     ctypes.byref(vl)))
+    return eo, e, vo, v
+
+
 def permute_mesh(raw: RawMesh, perm: np.ndarray) -> RawMesh:
     """Apply a vertex permutation (new index -> old index) like NodeGroups::clusterNodes."""
     new_of_old = np.empty_like(perm)

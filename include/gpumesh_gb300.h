@@ -122,6 +122,17 @@ gm_status gm_node_groups_build(uint32_t nv, const int32_t* cid, uint32_t nt, con
                                uint32_t np, const uint32_t* pris, uint32_t nh, const uint32_t* hexs,
                                int32_t permute, uint32_t* perm, uint32_t* group_base, uint32_t* members,
                                uint32_t* ranges, uint32_t* ngroups);
+/* The vertex neighbourhoods Mesh::compileNeighborhoods builds
+ * (DataStructures/Mesh.cpp:365-460), as the library builds them for an
+ * upload, in input indices:
+ *   ve_off[nv+1], ve[]  incident elements, packed (type << 30 | local << 27
+ *                       | id), tets then prisms then hexes, each by id
+ *   vv_off[nv+1], vv[]  edge neighbours in Mesh::addEdge order
+ * Call with ve == vv == NULL to get *ve_len and *vv_len, then with arrays of
+ * those lengths. */
+gm_status gm_mesh_neighbourhoods(uint32_t nv, uint32_t nt, const uint32_t* tets, uint32_t np, const uint32_t* pris,
+                                 uint32_t nh, const uint32_t* hexs, uint32_t* ve_off, uint32_t* ve, uint64_t* ve_len,
+                                 uint32_t* vv_off, uint32_t* vv, uint64_t* vv_len);
 
 /* ---- device mesh ---------------------------------------------------------- */
 gm_status gm_mesh_create(gm_mesh** out);

@@ -57,3 +57,64 @@ def test_build_is_deterministic():
     a = M.node_groups_build(raw)
     b = M.node_groups_build(raw)
     assert (a[0] == b[0]).all() and (a[1].members == b[1].members).all()
+
+
+# Mesh::compileNeighborhoods / Mesh::addEdge (DataStructures/Mesh.cpp:365-460)
+# restated with numpy: every element's edges in element order (tets, prisms,
+# hexes) and edge-table order; a vertex's neighbours in the order their edge
+# is first met; its elements in element order.
+_EDGES = {4: ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)),
+          6: ((0, 1), (0, 2), (1, 2), (0, 3), (1, 4), (2, 5), (3, 4), (3, 5), (4, 5)),
+          8: ((0, 1), (0, 3), (1, 2), (2, 3), (0, 4), (1, 5), (2, 6), (3, 7), (4, 5), (4, 7), (5, 6), (6, 7))}
+
+
+def _reference_neighbourhoods(raw):
+    nv = raw.nv
+    a, b, refs_v, refs = [], [], [], []
+    for type_code, conn in ((0, raw.tets), (2, raw.pris), (3, raw.hexs)):
+        k = conn.shape[1]
+        if not conn.shape[0]:
+            continue
+        ids = np.arange(conn.shape[0], dtype=np.uint64)
+        for local in range(k):
+            refs_v.append(conn[:, local].astype(np.int64))
+            refs.append((np.uint64(type_code) << np.uint64(30)) | (np.uint64(local) << np.uint64(27)) | ids)
+        # element-major edge events
+        ea = np.stack([conn[:, e0] for e0, _ in _EDGES[k]], axis=1).reshape(-1)
+        eb = np.stack([conn[:, e1] for _, e1 in _EDGES[k]], axis=1).reshape(-1)
+        a.append(ea.astype(np.int64))
+        b.append(eb.astype(np.int64))
+    # element refs: by vertex, then element order (tets < prisms < hexes, then id)
+    rv = np.concatenate(refs_v)
+    rr = np.concatenate(refs).astype(np.uint64)
+    tcode = rr >> np.uint64(30)
+    eid = rr & np.uint64((1 << 27) - 1)
+    order = np.lexsort((eid, tcode, rv))
+    ve_off = np.concatenate([[0], np.cumsum(np.bincount(rv, minlength=nv))]).astype(np.uint32)
+    ve = rr[order].astype(np.uint32)
+    # edge neighbours: both directions, first occurrence of each pair, by vertex then first occurrence
+    a, b = np.concatenate(a), np.concatenate(b)
+    seq = np.arange(a.shape[0], dtype=np.int64)
+    src = np.concatenate([a, b])
+    dst = np.concatenate([b, a])
+    sq = np.concatenate([seq, seq])
+    key = src * nv + dst
+    o = np.lexsort((sq, key))
+    key, sq, src, dst = key[o], sq[o], src[o], dst[o]
+    first = np.ones(key.shape[0], bool)
+    first[1:] = key[1:] != key[:-1]
+    src, dst, sq = src[first], dst[first], sq[first]
+    o = np.lexsort((sq, src))
+    vv_off = np.concatenate([[0], np.cumsum(np.bincount(src, minlength=nv))]).astype(np.uint32)
+    return ve_off, ve, vv_off, dst[o].astype(np.uint32)
+
+
+@pytest.mark.parametrize("build", [lambda: meshgen.box_mesh(5, "mixed", 0.2, 1),      # sequential path
+                                   lambda: meshgen.box_mesh(44, "tet", 0.2, 1),       # threaded path (91k vertices)
+                                   lambda: meshgen.box_mesh(42, "mixed", 0.2, 1)])
+def test_neighbourhoods_follow_the_reference_order(build):
+    raw = build()
+    got = M.neighbourhoods(raw)
+    want = _reference_neighbourhoods(raw)
+    for g, w, name in zip(got, want, ("ve_off", "ve", "vv_off", "vv")):
+        assert np.array_equal(g, w), name
