@@ -594,7 +594,7 @@ gm_status gm_mesh_set_constraints(gm_mesh* m, uint32_t n, const int32_t* kind, c
             Constraint& c = table[i];
             std::memset(&c, 0, sizeof(c));
             c.kind = kind[i];
-            require(c.kind >= GM_CON_VOLUME && c.kind <= GM_CON_POINT, "unknown constraint kind");
+            require(c.kind >= GM_CON_VOLUME && c.kind <= GM_CON_PIPE_CIRCLE, "unknown constraint kind");
             const double* p = params + 6 * (size_t)i;
             double a[3] = {p[0], p[1], p[2]}, b[3] = {p[3], p[4], p[5]}, u[3] = {0, 0, 0}, len = 0;
             if (c.kind == GM_CON_PLANE)

@@ -10,7 +10,8 @@
 //                    Measurers/MetricWiseMeasurer.cpp:64-188
 //   samplers         Samplers/UniformSampler.cpp:45, AbstractSampler.cpp:190-208
 //   projections      Boundaries/Constraints/{Face,Edge,Vertex,Volume}Constraint.cpp,
-//                    Boundaries/SphereBoundary.cpp:42-45
+//                    Boundaries/SphereBoundary.cpp:42-45, ShellBoundary.cpp:41-49,
+//                    PipeBoundary.cpp:42-116
 // Positive element qualities are carried as reciprocals (1/q), which is all
 // a harmonic mean needs, so the common path has no division.
 #pragma once
@@ -27,7 +28,17 @@ constexpr int kHex = 3;
 enum : int { kSamplerUniform = 0, kSamplerAnalytic = 1, kSamplerSine = 2 };
 enum : int { kMeasurerMetricFree = 0, kMeasurerMetricWise = 1 };
 enum : int { kEvalMeanRatio = 0, kEvalMetricConformity = 1 };
-enum : int { kConVolume = 0, kConPlane = 1, kConSegment = 2, kConSphere = 3, kConPoint = 4 };
+enum : int
+{
+    kConVolume = 0,
+    kConPlane = 1,
+    kConSegment = 2,
+    kConSphere = 3,
+    kConPoint = 4,
+    kConShellInner = 5,   // ShellBoundary::InFace: the radius-0.5 sphere
+    kConPipeCylinder = 6, // PipeBoundary::CylinderFace: the U-bend pipe wall
+    kConPipeCircle = 7    // PipeBoundary::Y*CircleEdge: a pipe-end circle, centre in a
+};
 
 // smoothing-wide parameters, passed by value to every kernel
 struct Crew
@@ -101,6 +112,33 @@ template <> __device__ __forceinline__ float sqrt_<float>(float x) { return sqrt
 template <> __device__ __forceinline__ double sqrt_<double>(double x) { return sqrt(x); }
 template <class R> __device__ __forceinline__ V3<R> normalize(V3<R> a) { return a * rsqrt_<R>(dot(a, a)); }
 template <class R> __device__ __forceinline__ R length(V3<R> a) { return sqrt_<R>(dot(a, a)); }
+
+// the U-bend pipe (Boundaries/PipeBoundary.cpp:3-6, 42-56, 95-116): radius 0.3,
+// end faces normal to -x
+template <class R>
+__device__ __forceinline__ V3<R> pipe_cylinder(V3<R> p)
+{
+    V3<R> center;
+    if (p.x < R(0.5)) center = V3<R>{p.x, p.y < R(0) ? R(-0.5) : R(0.5), R(0)};  // straights
+    else  // arc
+    {
+        center = p - V3<R>{R(0.5), R(0), p.z};
+        center = normalize(center) * R(0.5);
+        center = V3<R>{R(0.5), R(0), R(0)} + center;
+    }
+    const V3<R> dist = p - center;
+    return center + normalize(dist) * R(0.3);
+}
+
+template <class R>
+__device__ __forceinline__ V3<R> pipe_circle(V3<R> c, V3<R> p)
+{
+    const V3<R> n{R(-1), R(0), R(0)};
+    const V3<R> dist = p - c;
+    const R offset = dot(dist, n);
+    const V3<R> ext = dist - n * offset;
+    return c + normalize(ext) * R(0.3);
+}
 
 // Single-instruction FP32 approximations (PTX ISA: ex2 / lg2 / rcp / sqrt
 // .approx.ftz.f32, relative error of order 2^-22).  Subnormal inputs flush
@@ -781,6 +819,12 @@ __device__ __forceinline__ V3<R> project(const Constraint* con, int ncon, int id
         return normalize(p);
     case kConPoint:
         return dbl ? mk<R>((R)k.ad[0], (R)k.ad[1], (R)k.ad[2]) : mk<R>((R)k.a[0], (R)k.a[1], (R)k.a[2]);
+    case kConShellInner:
+        return normalize(p) * R(0.5);
+    case kConPipeCylinder:
+        return pipe_cylinder(p);
+    case kConPipeCircle:
+        return pipe_circle(dbl ? mk<R>((R)k.ad[0], (R)k.ad[1], (R)k.ad[2]) : mk<R>((R)k.a[0], (R)k.a[1], (R)k.a[2]), p);
     default:
         return p;
     }

@@ -158,6 +158,9 @@ __device__ __forceinline__ V3<float> project_rec(const float* r, V3<float> p)
     }
     case kConSphere: return normalize(p);
     case kConPoint: return a;
+    case kConShellInner: return normalize(p) * 0.5f;
+    case kConPipeCylinder: return pipe_cylinder(p);
+    case kConPipeCircle: return pipe_circle(a, p);
     default: return p;
     }
 }

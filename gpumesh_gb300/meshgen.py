@@ -26,6 +26,9 @@ CON_PLANE = 1
 CON_SEGMENT = 2
 CON_SPHERE = 3
 CON_POINT = 4
+CON_SHELL_INNER = 5   # ShellBoundary::InFace (radius 0.5 sphere)
+CON_PIPE_CYLINDER = 6  # PipeBoundary::CylinderFace
+CON_PIPE_CIRCLE = 7    # PipeBoundary::YNeg/YPosCircleEdge (params: circle centre)
 
 _GOLDEN = np.uint64(0x9E3779B97F4A7C15)
 

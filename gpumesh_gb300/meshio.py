@@ -15,8 +15,9 @@ and reads it back tag by tag (JsonDeserializer.cpp:23-131): a missing
 "topos" leaves every vertex free, an unknown tag is an error, and the
 boundary name selects one of the reference's boundaries (AbstractDeserializer
 .cpp:10-29; an unknown name selects "Free").  `read_json` returns a RawMesh
-whose constraint table is that boundary's (Box, Sphere, Tet and Free: the
-planes, segments and unit sphere the relocation kernels project onto);
+whose constraint table is that boundary's (Free, Box, Sphere, Tet, Shell and
+Pipe: the planes, segments, spheres and pipe surfaces the relocation kernels
+project onto);
 `write_json` writes the same layout, with the reference's 6 significant
 digits (`ostream <<` defaults) or with every double written exactly.
 """
@@ -29,8 +30,8 @@ import os
 
 import numpy as np
 
-from .meshgen import (CON_PLANE, CON_SEGMENT, CON_SPHERE, CON_VOLUME, RawMesh, box_constraints,
-                      sphere_constraints)
+from .meshgen import (CON_PIPE_CIRCLE, CON_PIPE_CYLINDER, CON_PLANE, CON_SEGMENT, CON_SHELL_INNER, CON_SPHERE,
+                      CON_VOLUME, RawMesh, box_constraints, sphere_constraints)
 
 TAGS = ("Model", "Boundary", "verts", "topos", "tets", "pris", "hexs")
 
@@ -82,16 +83,33 @@ def free_constraints():
     return np.array([CON_VOLUME], np.int32), np.zeros((1, 6), np.float64)
 
 
+def shell_constraints():
+    """ShellBoundary (Boundaries/ShellBoundary.cpp:3-56): outer face 1 the
+    unit sphere, inner face 2 the radius-0.5 sphere."""
+    kind = np.array([CON_VOLUME, CON_SPHERE, CON_SHELL_INNER], np.int32)
+    return kind, np.zeros((3, 6), np.float64)
+
+
+def pipe_constraints():
+    """PipeBoundary (Boundaries/PipeBoundary.cpp:3-116): the U-bend wall 1,
+    the two end disks 2 and 3 (planes through (-1, -+0.5, 0) with normal
+    (-1, 0, 0)), their rim circles 4 and 5."""
+    kind = np.array([CON_VOLUME, CON_PIPE_CYLINDER, CON_PLANE, CON_PLANE, CON_PIPE_CIRCLE, CON_PIPE_CIRCLE],
+                    np.int32)
+    par = np.zeros((6, 6), np.float64)
+    par[2] = (-1.0, -0.5, 0.0, -1.0, 0.0, 0.0)
+    par[3] = (-1.0, 0.5, 0.0, -1.0, 0.0, 0.0)
+    par[4, :3] = (-1.0, -0.5, 0.0)
+    par[5, :3] = (-1.0, 0.5, 0.0)
+    return kind, par
+
+
 BOUNDARIES = {"Free": free_constraints, "Box": box_constraints, "Sphere": sphere_constraints,
-              "Tet": tet_constraints}
-UNSUPPORTED = {"Pipe": "cylinder and disk faces", "Shell": "the radius-0.5 inner sphere"}
+              "Tet": tet_constraints, "Shell": shell_constraints, "Pipe": pipe_constraints}
 
 
 def boundary_table(name: str):
     """(kind, params) of a reference boundary by name ("Free" for an unknown name)."""
-    if name in UNSUPPORTED:
-        raise NotImplementedError(f"boundary {name!r}: the relocation kernels do not project onto "
-                                  f"{UNSUPPORTED[name]}")
     return BOUNDARIES.get(name, free_constraints)()
 
 

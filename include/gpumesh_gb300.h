@@ -61,6 +61,9 @@ typedef int gm_status;
 #define GM_CON_SEGMENT 2
 #define GM_CON_SPHERE 3
 #define GM_CON_POINT 4
+#define GM_CON_SHELL_INNER 5   /* ShellBoundary::InFace (radius 0.5 sphere) */
+#define GM_CON_PIPE_CYLINDER 6 /* PipeBoundary::CylinderFace */
+#define GM_CON_PIPE_CIRCLE 7   /* PipeBoundary::YNeg/YPosCircleEdge; params: circle centre */
 /* smoothers */
 #define GM_SMOOTH_NELDER_MEAD 0
 #define GM_SMOOTH_GRADIENT_DESCENT 1

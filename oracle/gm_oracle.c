@@ -438,6 +438,38 @@ static v3 project_id(const om_mesh* m, int32_t id, v3 pos)
         return normalize(pos);
     case OM_CON_POINT:
         return V(pp[0], pp[1], pp[2]);
+    case OM_CON_SHELL_INNER:
+        /* ShellBoundary::InFace::operator() (ShellBoundary.cpp:41-44) */
+        return mul(normalize(pos), 0.5);
+    case OM_CON_PIPE_CYLINDER:
+    {
+        /* PipeBoundary::CylinderFace::operator() (PipeBoundary.cpp:43-56),
+         * PIPE_RADIUS 0.3 (:3) */
+        v3 center;
+        if (pos.x < 0.5)
+            center = V(pos.x, (pos.y < 0.0 ? -0.5 : 0.5), 0.0);
+        else
+        {
+            center = sub(pos, V(0.5, 0.0, pos.z));
+            center = mul(normalize(center), 0.5);
+            center = add(V(0.5, 0, 0), center);
+        }
+        v3 dist = sub(pos, center);
+        v3 extProj = mul(normalize(dist), 0.3);
+        return add(center, extProj);
+    }
+    case OM_CON_PIPE_CIRCLE:
+    {
+        /* PipeBoundary::YNeg/YPosCircleEdge::operator() (PipeBoundary.cpp:
+         * 100-105, 111-116): the circle of radius 0.3 about the end-face
+         * centre, in the face of normal EXT_FACE_NORMAL = (-1, 0, 0) */
+        v3 c = V(pp[0], pp[1], pp[2]);
+        v3 n = V(-1, 0, 0);
+        v3 dist = sub(pos, c);
+        double offset = dot(dist, n);
+        v3 extProj = sub(dist, mul(n, offset));
+        return add(c, mul(normalize(extProj), 0.3));
+    }
     default:
         return pos;
     }

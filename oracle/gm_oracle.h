@@ -45,6 +45,9 @@ extern "C" {
 #define OM_CON_SEGMENT 2 /* SegmentConstraint, EdgeConstraint.cpp:185 */
 #define OM_CON_SPHERE 3  /* SphereBoundary::Face, SphereBoundary.cpp:42 */
 #define OM_CON_POINT 4   /* VertexConstraint, VertexConstraint.cpp:60 */
+#define OM_CON_SHELL_INNER 5   /* ShellBoundary::InFace, ShellBoundary.cpp:41-44 */
+#define OM_CON_PIPE_CYLINDER 6 /* PipeBoundary::CylinderFace, PipeBoundary.cpp:42-56 */
+#define OM_CON_PIPE_CIRCLE 7   /* PipeBoundary::Y*CircleEdge, PipeBoundary.cpp:95-116 */
 
 /* smoothers */
 #define OM_SMOOTH_NELDER_MEAD 0

@@ -321,3 +321,25 @@ def test_c2_schedule_quality_matches_oracle():
     (omin, omean), (smin, smean) = oracle_ensemble(raw, groups, crew, w.schedule)
     assert abs(g["min"] - omin) <= max(1e-4, 2 * smin), (g["min"], omin, smin)
     assert abs(g["mean"] - omean) <= max(1e-4, 2 * smean), (g["mean"], omean, smean)
+
+
+@pytest.mark.parametrize("boundary", ["Pipe", "Shell", "Tet"])
+def test_boundary_kinds_project_on_the_gpu(boundary):
+    """Every constraint kind of the reference's boundaries (plane, segment,
+    unit and radius-0.5 spheres, the pipe wall and rim circles) projected in
+    the relocation kernels: a box mesh whose boundary vertices carry the
+    boundary's ids in turn, one spring-Laplace colour (no decision, so every
+    vertex must agree with the FP64 oracle to FP32 rounding)."""
+    from gpumesh_gb300 import meshio
+
+    raw = meshgen.box_mesh(7, "tet", 0.25, 3)
+    kind, par = meshio.boundary_table(boundary)
+    ids = np.array([i for i in range(kind.shape[0]) if kind[i] != meshgen.CON_VOLUME], np.int32)
+    b = np.nonzero(raw.cid > 0)[0]
+    raw.cid = raw.cid.copy()
+    raw.cid[b] = ids[np.arange(b.size) % ids.size]
+    raw.con_kind, raw.con_param = kind, par
+    raw, groups = coloured(raw)
+    for g in range(groups.count()):
+        err = one_colour(raw, groups, MR, "spring_laplace", None, g)
+        assert err.max() < 1e-5, (g, np.sort(err)[-5:])

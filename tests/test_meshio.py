@@ -1,7 +1,8 @@
 """JSON mesh files (gpumesh_gb300.meshio) against the reference's own
 JsonSerializer / JsonDeserializer and boundaries: a committed file written by
 the reference, byte-identical output in the reference's precision, exact
-round trips, and the Tet boundary's constraint table."""
+round trips, and every boundary's constraint table (Box, Sphere, Tet, Shell,
+Pipe) projecting as the reference's constraint objects do."""
 
 import os
 
@@ -61,8 +62,8 @@ def test_rejects_unknown_tags_and_bad_ids(tmp_path):
     p.write_text('{"verts": [[0,0,0],[1,0,0],[0,1,0]], "tets": [[0,1,2,3]]}')
     with pytest.raises(ValueError, match="outside"):
         meshio.read_json(str(p))
-    p.write_text('{"Boundary": "Pipe", "verts": [[0,0,0]]}')
-    with pytest.raises(NotImplementedError):
+    p.write_text('{"Boundary": "Box", "verts": [[0,0,0]], "topos": [19]}')
+    with pytest.raises(ValueError, match="not a Box constraint"):
         meshio.read_json(str(p))
 
 
@@ -99,17 +100,17 @@ def test_reader_agrees_with_the_reference_reader(tmp_path):
 
 
 @need_ref
-def test_tet_boundary_table_projects_like_the_reference():
-    kind, par = meshio.tet_constraints()
+@pytest.mark.parametrize("boundary", ["Tet", "Shell", "Pipe", "Box", "Sphere"])
+def test_boundary_tables_project_like_the_reference(boundary):
+    kind, par = meshio.boundary_table(boundary)
     ids = [i for i in range(kind.shape[0]) if kind[i] != meshgen.CON_VOLUME]
     # an oracle mesh with one vertex per constraint id, projecting through it
     n = kind.shape[0]
-    pos = np.zeros((n, 3))
-    orc = pyoracle.OracleMesh(pos, np.zeros((0, 4), np.uint32), np.zeros((0, 6), np.uint32),
+    orc = pyoracle.OracleMesh(np.zeros((n, 3)), np.zeros((0, 4), np.uint32), np.zeros((0, 6), np.uint32),
                               np.zeros((0, 8), np.uint32), np.arange(n, dtype=np.int32), kind, par)
     rng = np.random.default_rng(7)
     pts = rng.uniform(-1.5, 1.5, (64, 3))
     for i in ids:
-        theirs = pyref.boundary_project("tet", i, pts)
+        theirs = pyref.boundary_project(boundary.lower(), i, pts)
         mine = np.array([orc.project(i, p) for p in pts])
-        assert np.array_equal(mine, theirs), i
+        assert np.array_equal(mine, theirs), (boundary, i)
