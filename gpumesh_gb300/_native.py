@@ -57,6 +57,7 @@ def lib():
     L.gm_version.restype = ctypes.c_char_p
     sigs = {
         "gm_node_groups_build": [u32, vp, u32, vp, u32, vp, u32, vp, i32, vp, vp, vp, vp, vp],
+        "gm_node_groups_build_device": [u32, vp, u32, vp, u32, vp, u32, vp, i32, vp, vp, vp, vp, vp],
         "gm_mesh_neighbourhoods": [u32, u32, vp, u32, vp, u32, vp, vp, vp, vp, vp, vp, vp],
         "gm_mesh_create": [ctypes.POINTER(vp)],
         "gm_mesh_destroy": [vp],

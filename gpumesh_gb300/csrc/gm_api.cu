@@ -311,12 +311,15 @@ const char* gm_status_string(gm_status s)
 
 const char* gm_version(void) { return "gpumesh_gb300 sm_103a " __DATE__; }
 
-gm_status gm_node_groups_build(uint32_t nv, const int32_t* cid, uint32_t nt, const uint32_t* tets, uint32_t np,
-                               const uint32_t* pris, uint32_t nh, const uint32_t* hexs, int32_t permute, uint32_t* perm,
-                               uint32_t* group_base, uint32_t* members, uint32_t* ranges, uint32_t* ngroups)
+namespace {
+
+gm_status node_groups(uint32_t nv, const int32_t* cid, uint32_t nt, const uint32_t* tets, uint32_t np,
+                      const uint32_t* pris, uint32_t nh, const uint32_t* hexs, int32_t permute, uint32_t* perm,
+                      uint32_t* group_base, uint32_t* members, uint32_t* ranges, uint32_t* ngroups, bool device)
 {
     return guarded([&] {
         require(nv > 0 && cid && perm && group_base && members && ngroups, "null argument");
+        require((nt == 0 || tets) && (np == 0 || pris) && (nh == 0 || hexs), "null connectivity");
         check_conn(tets, (size_t)nt * 4, nv, "tet");
         check_conn(pris, (size_t)np * 6, nv, "prism");
         check_conn(hexs, (size_t)nh * 8, nv, "hex");
@@ -329,13 +332,37 @@ gm_status gm_node_groups_build(uint32_t nv, const int32_t* cid, uint32_t nt, con
         in.tets = tets;
         in.pris = pris;
         in.hexs = hexs;
-        Topology t = build_topology(in, permute != 0);
+        ColourSource source;
+        if (device)
+            source = [&](const std::vector<uint32_t>& e_off, const std::vector<uint32_t>& e, std::vector<int>& c) {
+                device_colours(in, e_off, e, c);
+            };
+        Topology t = build_topology(in, permute != 0, source);
         std::copy(t.perm.begin(), t.perm.end(), perm);
         std::copy(t.group_base.begin(), t.group_base.end(), group_base);
         std::copy(t.members.begin(), t.members.end(), members);
         if (ranges) std::copy(t.ranges.begin(), t.ranges.end(), ranges);
         *ngroups = (uint32_t)(t.group_base.size() - 1);
     });
+}
+
+}  // namespace
+
+gm_status gm_node_groups_build(uint32_t nv, const int32_t* cid, uint32_t nt, const uint32_t* tets, uint32_t np,
+                               const uint32_t* pris, uint32_t nh, const uint32_t* hexs, int32_t permute, uint32_t* perm,
+                               uint32_t* group_base, uint32_t* members, uint32_t* ranges, uint32_t* ngroups)
+{
+    return node_groups(nv, cid, nt, tets, np, pris, nh, hexs, permute, perm, group_base, members, ranges, ngroups,
+                       false);
+}
+
+gm_status gm_node_groups_build_device(uint32_t nv, const int32_t* cid, uint32_t nt, const uint32_t* tets, uint32_t np,
+                                      const uint32_t* pris, uint32_t nh, const uint32_t* hexs, int32_t permute,
+                                      uint32_t* perm, uint32_t* group_base, uint32_t* members, uint32_t* ranges,
+                                      uint32_t* ngroups)
+{
+    return node_groups(nv, cid, nt, tets, np, pris, nh, hexs, permute, perm, group_base, members, ranges, ngroups,
+                       true);
 }
 
 gm_status gm_mesh_neighbourhoods(uint32_t nv, uint32_t nt, const uint32_t* tets, uint32_t np, const uint32_t* pris,

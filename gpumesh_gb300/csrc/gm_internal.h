@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -46,7 +47,17 @@ struct Topology
     std::vector<uint32_t> vv_off, vv;  // vertex -> neighbour vertices (new ids)
 };
 
-Topology build_topology(const HostMeshView& in, bool permute);
+// Fills colour[v] (>= 0) for every vertex that is not fixed, from the
+// vertex -> element refs of the mesh (e_off, e: the neighbourhood CSR).
+using ColourSource = std::function<void(const std::vector<uint32_t>& e_off, const std::vector<uint32_t>& e,
+                                        std::vector<int>& colour)>;
+
+// the device order mode's colours (gm_colour.cu)
+void device_colours(const HostMeshView& in, const std::vector<uint32_t>& e_off, const std::vector<uint32_t>& e,
+                    std::vector<int>& colour);
+
+// colour_source empty: NodeGroups::determineGroups' greedy colouring
+Topology build_topology(const HostMeshView& in, bool permute, ColourSource colour_source = nullptr);
 void build_csr(const HostMeshView& in, std::vector<uint32_t>& ve_off, std::vector<uint32_t>& ve,
                std::vector<uint32_t>& vv_off, std::vector<uint32_t>& vv);
 

@@ -20,6 +20,7 @@
 #include <cstdint>
 #include <cstring>
 #include <numeric>
+#include <stdexcept>
 #include <thread>
 #include <vector>
 
@@ -213,7 +214,7 @@ void build_csr(const HostMeshView& in, std::vector<uint32_t>& ve_off, std::vecto
     vv = std::move(nb.v);
 }
 
-Topology build_topology(const HostMeshView& in, bool permute)
+Topology build_topology(const HostMeshView& in, bool permute, ColourSource colour_source)
 {
     const uint32_t nv = in.nv;
     Neighbourhoods nb = build_neighbourhoods(in);
@@ -248,14 +249,22 @@ Topology build_topology(const HostMeshView& in, bool permute)
         }
     }
 
-    // ---- greedy breadth-first colouring ----
-    // The reference copies the set of existing colours for every vertex and
-    // erases its neighbours' colours; the first remaining colour (or a new
-    // one) is taken.  A bitmask of the neighbours' colours gives the same
-    // first-fit choice without the set copies.
+    // ---- colours: the reference's greedy breadth-first colouring, or one
+    //      given by the caller (the device colouring order mode) ----
     const int NO_GROUP = -2, UNSET = -1;
     std::vector<int> groups(nv, NO_GROUP);
+    if (colour_source)
     {
+        colour_source(nb.e_off, nb.e, groups);
+        for (uint32_t v = 0; v < nv; ++v)
+            if (types[v] != FIXED && groups[v] < 0) throw std::runtime_error("a movable vertex has no colour");
+    }
+    else
+    {
+        // The reference copies the set of existing colours for every vertex
+        // and erases its neighbours' colours; the first remaining colour (or
+        // a new one) is taken.  A bitmask of the neighbours' colours gives
+        // the same first-fit choice without the set copies.
         size_t seek = 0;
         uint32_t ncolours = 0;
         std::vector<uint64_t> used;  // colours taken by the current vertex's neighbours

@@ -203,8 +203,11 @@ class NodeGroups:
         return np.concatenate(parts) if parts else np.zeros(0, np.uint32)
 
 
-def node_groups_build(raw: RawMesh, permute: bool = True):
-    """NodeGroups::build on the host (native): returns (perm, NodeGroups)."""
+def node_groups_build(raw: RawMesh, permute: bool = True, order: str = "reference"):
+    """NodeGroups::build on the host (native): returns (perm, NodeGroups).
+    order "reference": the reference's greedy breadth-first colouring (the
+    same groups as the reference); "device": colours from Jones-Plassmann
+    rounds on the GPU (a different relocation order)."""
     nv = raw.nv
     perm = np.zeros(nv, np.uint32)
     gb = np.zeros(nv + 1, np.uint32)
@@ -212,9 +215,10 @@ def node_groups_build(raw: RawMesh, permute: bool = True):
     ranges = np.zeros(6 * nv, np.uint32)
     ng = ctypes.c_uint32(0)
     L = N.lib()
-    N.check(L.gm_node_groups_build(nv, N.ptr(raw.cid), raw.tets.shape[0], N.ptr(raw.tets), raw.pris.shape[0],
-                                   N.ptr(raw.pris), raw.hexs.shape[0], N.ptr(raw.hexs), int(permute), N.ptr(perm),
-                                   N.ptr(gb), N.ptr(members), N.ptr(ranges), ctypes.byref(ng)))
+    fn = {"reference": L.gm_node_groups_build, "device": L.gm_node_groups_build_device}[order]
+    N.check(fn(nv, N.ptr(raw.cid), raw.tets.shape[0], N.ptr(raw.tets), raw.pris.shape[0], N.ptr(raw.pris),
+               raw.hexs.shape[0], N.ptr(raw.hexs), int(permute), N.ptr(perm), N.ptr(gb), N.ptr(members),
+               N.ptr(ranges), ctypes.byref(ng)))
     g = ng.value
     return perm, NodeGroups(gb[:g + 1].copy(), members[:gb[g]].copy(), ranges[:6 * g].copy())
 

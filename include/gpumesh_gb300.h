@@ -125,6 +125,18 @@ gm_status gm_node_groups_build(uint32_t nv, const int32_t* cid, uint32_t nt, con
                                uint32_t np, const uint32_t* pris, uint32_t nh, const uint32_t* hexs,
                                int32_t permute, uint32_t* perm, uint32_t* group_base, uint32_t* members,
                                uint32_t* ranges, uint32_t* ngroups);
+/* The same outputs in the device order mode: the colours come from
+ * Jones-Plassmann rounds on the GPU (two vertices conflict when they share
+ * an element; each round colours the uncoloured vertices whose hashed index
+ * beats every uncoloured conflicting vertex, with the lowest colour their
+ * coloured neighbours leave free; deterministic), not from the reference's
+ * greedy breadth-first colouring, so the relocation order differs from the
+ * reference's.  Classes, sort and groups as gm_node_groups_build.  Fixed
+ * vertices take colour 0 and are in no group. */
+gm_status gm_node_groups_build_device(uint32_t nv, const int32_t* cid, uint32_t nt, const uint32_t* tets, uint32_t np,
+                                      const uint32_t* pris, uint32_t nh, const uint32_t* hexs, int32_t permute,
+                                      uint32_t* perm, uint32_t* group_base, uint32_t* members, uint32_t* ranges,
+                                      uint32_t* ngroups);
 /* The vertex neighbourhoods Mesh::compileNeighborhoods builds
  * (DataStructures/Mesh.cpp:365-460), as the library builds them for an
  * upload, in input indices:
