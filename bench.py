@@ -22,6 +22,7 @@ path has no exchange step); value is the sum over ranks.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import re
@@ -440,8 +441,8 @@ def bench_gpu(args, rank, world, local):
         per.setdefault(sm, []).append(e0.elapsed_time(e1) * 1e-3)
     dom = max(per, key=lambda k: sum(per[k]))
     fpe = flops_per_elem(w, raw)
-    fp32 = __import__("ctypes").c_double(0)
-    N.check(N.lib().gm_probe_fp32_tflops(__import__("ctypes").byref(fp32)))
+    fp32 = ctypes.c_double(0)
+    N.check(N.lib().gm_probe_fp32_tflops(ctypes.byref(fp32)))
     # element evaluations of the dominant smoother's passes: measured by a
     # dedicated counted pass of that smoother from the same input
     dev.restore_positions()
@@ -485,7 +486,7 @@ def bench_gpu(args, rank, world, local):
             e2e_times.append(t1 - t0)
     e2e_total = max_over_ranks(sum(e2e_times), world)
     e2e = {"value": reloc * args.steps * world / e2e_total, "unit": UNIT, "h2d_bytes_per_step": raw.nv * 16,
-           "d2h_bytes_per_step": raw.nv * 16 + n * __import__("ctypes").sizeof(N.Quality)}
+           "d2h_bytes_per_step": raw.nv * 16 + n * ctypes.sizeof(N.Quality)}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,

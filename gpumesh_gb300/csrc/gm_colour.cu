@@ -119,29 +119,10 @@ void device_colours(const HostMeshView& in, const std::vector<uint32_t>& e_off, 
                     std::vector<int>& colour)
 {
     const uint32_t nv = in.nv;
-    struct Buffers
-    {
-        DBuf<uint32_t> off, e, tets, pris, hexs;
-        DBuf<int32_t> cid;
-        DBuf<int> a, b;
-        DBuf<unsigned int> ctr;
-        ~Buffers()
-        {
-            off.release();
-            e.release();
-            tets.release();
-            pris.release();
-            hexs.release();
-            cid.release();
-            a.release();
-            b.release();
-            ctr.release();
-        }
-    } B;
-    DBuf<uint32_t>&d_off = B.off, &d_e = B.e, &d_tets = B.tets, &d_pris = B.pris, &d_hexs = B.hexs;
-    DBuf<int32_t>& d_cid = B.cid;
-    DBuf<int>&a = B.a, &b = B.b;
-    DBuf<unsigned int>& ctr = B.ctr;
+    DBuf<uint32_t> d_off, d_e, d_tets, d_pris, d_hexs;
+    DBuf<int32_t> d_cid;
+    DBuf<int> a, b;
+    DBuf<unsigned int> ctr;
     cudaStream_t s = nullptr;
     upload(d_off, e_off.data(), e_off.size(), s);
     upload(d_e, e.data(), e.size(), s);
@@ -172,8 +153,7 @@ void device_colours(const HostMeshView& in, const std::vector<uint32_t>& e_off, 
         GM_CUDA(cudaGetLastError());
         GM_CUDA(cudaMemcpy(h, ctr.p, sizeof(h), cudaMemcpyDeviceToHost));
         if (h[1]) throw ApiError(GM_ERR_UNSUPPORTED, "device colouring needs more than 128 colours");
-        std::swap(a.p, b.p);
-        std::swap(a.cap, b.cap);
+        std::swap(a, b);
     }
     colour.resize(nv);
     GM_CUDA(cudaMemcpy(colour.data(), a.p, nv * sizeof(int), cudaMemcpyDeviceToHost));

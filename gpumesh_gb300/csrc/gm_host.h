@@ -61,12 +61,34 @@ gm_status guarded(F&& f)
     }
 }
 
-// growable device buffer
+// growable device buffer, owning its allocation (freed on destruction;
+// moved, never copied)
 template <class T>
 struct DBuf
 {
     T* p = nullptr;
     size_t cap = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), cap(o.cap)
+    {
+        o.p = nullptr;
+        o.cap = 0;
+    }
+    DBuf& operator=(DBuf&& o) noexcept
+    {
+        if (this != &o)
+        {
+            release();
+            p = o.p;
+            cap = o.cap;
+            o.p = nullptr;
+            o.cap = 0;
+        }
+        return *this;
+    }
+    ~DBuf() { release(); }
     // true when the buffer was (re)allocated
     bool reserve(size_t n)
     {
