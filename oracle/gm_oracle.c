@@ -164,6 +164,18 @@ struct om_mesh
     double scaling, scaling2, scaling3, aspect_ratio;
     m3 rot, rotinv;
 
+    /* LocalSampler's background mesh (Samplers/LocalSampler.cpp:352-429):
+     * the mesh at crew set-up split into tets, their face neighbours, the
+     * analytic metric at every vertex, and the sampler caches -- per vertex
+     * the last background tet holding it, per element its first background
+     * tet (Tetrahedralizer.h:39-200) */
+    int64_t nbg;
+    uint32_t* bg; /* 8 per background tet: v[4], n[4] (0xffffffff: no neighbour) */
+    double* bg_pos;
+    m3* bg_metric;
+    uint32_t* vcache;
+    uint32_t* ecache; /* tets, then prisms, then hexes */
+
     int64_t patch_evals;
 };
 
@@ -323,6 +335,11 @@ om_mesh* om_create(int64_t nv, const double* pos, int64_t nt, const uint32_t* te
 void om_destroy(om_mesh* m)
 {
     if (!m) return;
+    free(m->bg);
+    free(m->bg_pos);
+    free(m->bg_metric);
+    free(m->vcache);
+    free(m->ecache);
     free(m->pos);
     free(m->tets);
     free(m->pris);
@@ -374,6 +391,200 @@ void om_set_constraints(om_mesh* m, int32_t n, const int32_t* kind, const double
     }
 }
 
+/* ---- LocalSampler background mesh ---- */
+
+#define BG_NONE 0xffffffffu
+
+/* MeshTet::tris (DataStructures/Mesh.cpp:30-35): the face opposite each vertex */
+static const int TET_TRIS[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};
+
+static m3 analytic_metric(const om_mesh* m, v3 p);
+
+/* the vertex rotations of tetrahedrize (DataStructures/Tetrahedralizer.h:9-34):
+ * each prism / hex is turned so that its smallest vertex id comes first */
+static const unsigned PRI_ROT[6][6] = {{0, 1, 2, 3, 4, 5}, {1, 2, 0, 4, 5, 3}, {2, 0, 1, 5, 3, 4},
+                                       {3, 5, 4, 0, 2, 1}, {4, 3, 5, 1, 0, 2}, {5, 4, 3, 2, 1, 0}};
+static const unsigned HEX_ROT[8][8] = {{0, 1, 2, 3, 4, 5, 6, 7}, {1, 0, 4, 5, 2, 3, 7, 6}, {2, 1, 5, 6, 3, 0, 4, 7},
+                                       {3, 0, 1, 2, 7, 4, 5, 6}, {4, 0, 3, 7, 5, 1, 2, 6}, {5, 1, 0, 4, 6, 2, 3, 7},
+                                       {6, 2, 1, 5, 7, 3, 0, 4}, {7, 3, 2, 6, 4, 0, 1, 5}};
+static const unsigned HEX_LOOP[8] = {0, 120, 240, 0, 0, 240, 120, 0};
+
+static inline unsigned umin(unsigned a, unsigned b) { return b < a ? b : a; }
+
+static void bg_push(om_mesh* m, unsigned a, unsigned b, unsigned c, unsigned d)
+{
+    uint32_t* t = m->bg + 8 * (size_t)m->nbg++;
+    t[0] = a;
+    t[1] = b;
+    t[2] = c;
+    t[3] = d;
+    t[4] = t[5] = t[6] = t[7] = BG_NONE;
+}
+
+/* tetrahedrize (Tetrahedralizer.h:37-200): tets as they are; a prism into 3
+ * tets and a hex into 5 or 6, the diagonals chosen from the vertex ids so that
+ * neighbouring elements split their shared faces alike; every element's cache
+ * is its first background tet */
+static void tetrahedrize(om_mesh* m)
+{
+    m->nbg = 0;
+    for (int64_t i = 0; i < m->nt; ++i)
+    {
+        const uint32_t* e = m->tets + 4 * i;
+        m->ecache[i] = (uint32_t)m->nbg;
+        bg_push(m, e[0], e[1], e[2], e[3]);
+    }
+    for (int64_t i = 0; i < m->np; ++i)
+    {
+        const uint32_t* pv = m->pris + 6 * i;
+        m->ecache[m->nt + i] = (uint32_t)m->nbg;
+        unsigned s = 0;
+        for (unsigned k = 1; k < 6; ++k)
+            if (pv[k] < pv[s]) s = k;
+        unsigned v[6];
+        for (int k = 0; k < 6; ++k) v[k] = pv[PRI_ROT[s][k]];
+        if (umin(v[1], v[5]) < umin(v[2], v[4]))
+        {
+            bg_push(m, v[0], v[1], v[2], v[5]);
+            bg_push(m, v[0], v[1], v[5], v[4]);
+            bg_push(m, v[0], v[4], v[5], v[3]);
+        }
+        else
+        {
+            bg_push(m, v[0], v[1], v[2], v[4]);
+            bg_push(m, v[0], v[4], v[2], v[5]);
+            bg_push(m, v[0], v[4], v[5], v[3]);
+        }
+    }
+    for (int64_t i = 0; i < m->nh; ++i)
+    {
+        const uint32_t* hv = m->hexs + 8 * i;
+        m->ecache[m->nt + m->np + i] = (uint32_t)m->nbg;
+        unsigned s = 0;
+        for (unsigned k = 1; k < 8; ++k)
+            if (hv[k] < hv[s]) s = k;
+        unsigned v[8];
+        for (int k = 0; k < 8; ++k) v[k] = hv[HEX_ROT[s][k]];
+        unsigned diag = 0;
+        if (umin(v[1], v[6]) < umin(v[2], v[5])) diag |= 4u;
+        if (umin(v[3], v[6]) < umin(v[2], v[7])) diag |= 2u;
+        if (umin(v[4], v[6]) < umin(v[5], v[7])) diag |= 1u;
+        unsigned tmp;
+        if (HEX_LOOP[diag] == 120)
+        {
+            tmp = v[1]; v[1] = v[4]; v[4] = v[3]; v[3] = tmp;
+            tmp = v[5]; v[5] = v[7]; v[7] = v[2]; v[2] = tmp;
+        }
+        else if (HEX_LOOP[diag] == 240)
+        {
+            tmp = v[1]; v[1] = v[3]; v[3] = v[4]; v[4] = tmp;
+            tmp = v[5]; v[5] = v[2]; v[2] = v[7]; v[7] = tmp;
+        }
+        switch ((diag & 1u) + ((diag & 2u) >> 1) + ((diag & 4u) >> 2))
+        {
+        case 0:
+            bg_push(m, v[0], v[1], v[2], v[5]);
+            bg_push(m, v[0], v[2], v[7], v[5]);
+            bg_push(m, v[0], v[2], v[3], v[7]);
+            bg_push(m, v[0], v[5], v[7], v[4]);
+            bg_push(m, v[2], v[7], v[5], v[6]);
+            break;
+        case 1:
+            bg_push(m, v[0], v[5], v[7], v[4]);
+            bg_push(m, v[0], v[1], v[7], v[5]);
+            bg_push(m, v[1], v[6], v[7], v[5]);
+            bg_push(m, v[0], v[7], v[2], v[3]);
+            bg_push(m, v[0], v[7], v[1], v[2]);
+            bg_push(m, v[1], v[7], v[6], v[2]);
+            break;
+        case 2:
+            bg_push(m, v[0], v[4], v[5], v[6]);
+            bg_push(m, v[0], v[3], v[7], v[6]);
+            bg_push(m, v[0], v[7], v[4], v[6]);
+            bg_push(m, v[0], v[1], v[2], v[5]);
+            bg_push(m, v[0], v[3], v[6], v[2]);
+            bg_push(m, v[0], v[6], v[5], v[2]);
+            break;
+        default:
+            bg_push(m, v[0], v[2], v[3], v[6]);
+            bg_push(m, v[0], v[3], v[7], v[6]);
+            bg_push(m, v[0], v[7], v[4], v[6]);
+            bg_push(m, v[0], v[5], v[6], v[4]);
+            bg_push(m, v[1], v[5], v[6], v[0]);
+            bg_push(m, v[1], v[6], v[2], v[0]);
+            break;
+        }
+    }
+}
+
+typedef struct
+{
+    uint32_t key[3];
+    uint32_t tet, side;
+} face_rec;
+
+static int face_cmp(const void* pa, const void* pb)
+{
+    const face_rec* a = (const face_rec*)pa;
+    const face_rec* b = (const face_rec*)pb;
+    for (int k = 0; k < 3; ++k)
+        if (a->key[k] != b->key[k]) return a->key[k] < b->key[k] ? -1 : 1;
+    if (a->tet != b->tet) return a->tet < b->tet ? -1 : 1;
+    return a->side < b->side ? -1 : (a->side > b->side);
+}
+
+/* LocalSampler::buildBackgroundMesh (Samplers/LocalSampler.cpp:352-429) at
+ * the current positions: the background tets, the analytic metric at every
+ * vertex (LocalSampler::updateAnalyticalMetric, :186-203), the two tets of
+ * every shared face linked as neighbours (the XOR set of TriSet pairs a face's
+ * first and second owner; sorting the faces pairs them alike), and every
+ * vertex's cache the last tet holding it */
+static void build_background(om_mesh* m)
+{
+    free(m->bg);
+    free(m->bg_pos);
+    free(m->bg_metric);
+    free(m->vcache);
+    free(m->ecache);
+    const int64_t maxbg = m->nt + 3 * m->np + 6 * m->nh;
+    m->bg = (uint32_t*)malloc(sizeof(uint32_t) * 8 * (size_t)(maxbg + 1));
+    m->ecache = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)(m->nt + m->np + m->nh + 1));
+    m->vcache = (uint32_t*)calloc((size_t)m->nv + 1, sizeof(uint32_t));
+    m->bg_pos = (double*)malloc(sizeof(double) * 3 * (size_t)(m->nv + 1));
+    m->bg_metric = (m3*)malloc(sizeof(m3) * (size_t)(m->nv + 1));
+    memcpy(m->bg_pos, m->pos, sizeof(double) * 3 * (size_t)m->nv);
+    for (int64_t v = 0; v < m->nv; ++v) m->bg_metric[v] = analytic_metric(m, P(m, (uint32_t)v));
+    tetrahedrize(m);
+    face_rec* f = (face_rec*)malloc(sizeof(face_rec) * 4 * (size_t)(m->nbg + 1));
+    for (int64_t t = 0; t < m->nbg; ++t)
+        for (int s = 0; s < 4; ++s)
+        {
+            face_rec* r = f + 4 * t + s;
+            uint32_t a = m->bg[8 * t + TET_TRIS[s][0]], b = m->bg[8 * t + TET_TRIS[s][1]], c = m->bg[8 * t + TET_TRIS[s][2]];
+            uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
+            if (c < lo) { r->key[0] = c; r->key[1] = lo; r->key[2] = hi; }
+            else if (c < hi) { r->key[0] = lo; r->key[1] = c; r->key[2] = hi; }
+            else { r->key[0] = lo; r->key[1] = hi; r->key[2] = c; }
+            r->tet = (uint32_t)t;
+            r->side = (uint32_t)s;
+        }
+    qsort(f, (size_t)(4 * m->nbg), sizeof(face_rec), face_cmp);
+    for (int64_t i = 0; i + 1 < 4 * m->nbg;)
+    {
+        if (memcmp(f[i].key, f[i + 1].key, sizeof(f[i].key)) == 0)
+        {
+            m->bg[8 * (size_t)f[i].tet + 4 + f[i].side] = f[i + 1].tet;
+            m->bg[8 * (size_t)f[i + 1].tet + 4 + f[i + 1].side] = f[i].tet;
+            i += 2;
+        }
+        else
+            ++i;
+    }
+    free(f);
+    for (int64_t t = 0; t < m->nbg; ++t)
+        for (int k = 0; k < 4; ++k) m->vcache[m->bg[8 * t + k]] = (uint32_t)t;
+}
+
 void om_set_crew(om_mesh* m, int32_t sampler, int32_t measurer, int32_t evaluator,
                  double scaling, double aspect_ratio)
 {
@@ -390,6 +601,7 @@ void om_set_crew(om_mesh* m, int32_t sampler, int32_t measurer, int32_t evaluato
     m->rot = mrotate(id, 3.14159265358979323846 / 4.0, V(0, 0, 1));
     m->rot = mrotate(m->rot, 3.14159265358979323846 / 4.0, V(0, -1, 0));
     m->rotinv = mtranspose(m->rot);
+    if (sampler == OM_SAMPLER_LOCAL) build_background(m);
 }
 
 void om_get_pos(const om_mesh* m, double* out) { memcpy(out, m->pos, sizeof(double) * 3 * (size_t)m->nv); }
@@ -497,24 +709,140 @@ void om_project(const om_mesh* m, int64_t v, const double* in, double* out)
 /* samplers                                                                  */
 /* ------------------------------------------------------------------------ */
 
+/* AbstractSampler::vertMetric(position) (AbstractSampler.cpp:190-208) */
+static m3 analytic_metric(const om_mesh* m, v3 p)
+{
+    double x = mmulv(m->rot, p).x * (2.5 * 3.14159265358979323846);
+    double a = m->aspect_ratio;
+    double c = (1.0 - cos(x)) / 2.0;
+    double sizeX = m->scaling * pow(a, pow(c, a));
+    double Mx = sizeX * sizeX;
+    double My = m->scaling2;
+    double Mz = My;
+    m3 Mm = mdiag(Mx, My, Mz);
+    return mmul(mmul(m->rotinv, Mm), m->rot);
+}
+
+/* The sampler cache of the element or vertex being measured: LocalSampler::
+ * metricAt starts its walk at the background tet it names.  The measures set
+ * it per element (its first background tet) and per sampled vertex (the
+ * vertex's cache); thread-local, since passes run on several threads. */
+static __thread uint32_t tl_cache;
+
+/* tetParams (DataStructures/Tetrahedralizer.h:211-234): barycentric
+ * coordinates of p in background tet t; inside within -1e-4 */
+static int bg_params(const om_mesh* m, const uint32_t* t, v3 p, double coor[4])
+{
+    v3 vp0 = V(m->bg_pos[3 * t[0]], m->bg_pos[3 * t[0] + 1], m->bg_pos[3 * t[0] + 2]);
+    v3 vp1 = V(m->bg_pos[3 * t[1]], m->bg_pos[3 * t[1] + 1], m->bg_pos[3 * t[1] + 2]);
+    v3 vp2 = V(m->bg_pos[3 * t[2]], m->bg_pos[3 * t[2] + 1], m->bg_pos[3 * t[2] + 2]);
+    v3 vp3 = V(m->bg_pos[3 * t[3]], m->bg_pos[3 * t[3] + 1], m->bg_pos[3 * t[3] + 2]);
+    m3 T = M(sub(vp0, vp3), sub(vp1, vp3), sub(vp2, vp3));
+    v3 y = mmulv(minverse(T), sub(p, vp3));
+    coor[0] = y.x;
+    coor[1] = y.y;
+    coor[2] = y.z;
+    coor[3] = 1.0 - (y.x + y.y + y.z);
+    const double EPSILON_IN = -1e-4;
+    return coor[0] >= EPSILON_IN && coor[1] >= EPSILON_IN && coor[2] >= EPSILON_IN && coor[3] >= EPSILON_IN;
+}
+
+/* triIntersect (Tetrahedralizer.h:236-271): the ray orig + s dir crosses the
+ * triangle (v1, v2, v3) from its front */
+static int tri_intersect(v3 v1, v3 v2, v3 v3_, v3 orig, v3 dir)
+{
+    const double EPSILON = 1e-12;
+    v3 e1 = sub(v2, v1);
+    v3 e2 = sub(v3_, v1);
+    v3 pvec = cross(dir, e2);
+    double det = dot(pvec, e1);
+    if (det < EPSILON) return 0;
+    v3 tvec = sub(orig, v1);
+    double u = dot(tvec, pvec);
+    if (u < 0.0 || u > det) return 0;
+    v3 qvec = cross(tvec, e1);
+    double v = dot(dir, qvec);
+    if (v < 0.0 || v + u > det) return 0;
+    return 1;
+}
+
+/* LocalSampler::metricAt (Samplers/LocalSampler.cpp:212-311): walk the
+ * background mesh from tet `cache` (through the face a ray from the current
+ * tet's centroid, or from one of four weighted interior points, leaves), then
+ * interpolate the vertex metrics barycentrically; a point outside the mesh
+ * takes the clamped coordinates of the last tet */
+static m3 local_metric(const om_mesh* m, v3 position, uint32_t cache)
+{
+    const uint32_t* tet = m->bg + 8 * (size_t)cache;
+    double coor[4];
+    int isUnreachable = 0;
+    while (!isUnreachable && !bg_params(m, tet, position, coor))
+    {
+        v3 vp[4];
+        for (int k = 0; k < 4; ++k)
+            vp[k] = V(m->bg_pos[3 * tet[k]], m->bg_pos[3 * tet[k] + 1], m->bg_pos[3 * tet[k] + 2]);
+        v3 orig = mul(add(add(add(vp[0], vp[1]), vp[2]), vp[3]), 0.25);
+        v3 dir = normalize(sub(orig, position));
+        int t = 4;
+        int trialCount = -1;
+        while (t == 4 && !isUnreachable)
+        {
+            for (t = 0; t < 4; ++t)
+            {
+                if (tri_intersect(vp[TET_TRIS[t][0]], vp[TET_TRIS[t][1]], vp[TET_TRIS[t][2]], orig, dir))
+                {
+                    if (tet[4 + t] != BG_NONE) tet = m->bg + 8 * (size_t)tet[4 + t];
+                    else isUnreachable = 1;
+                    break;
+                }
+            }
+            if (t == 4)
+            {
+                ++trialCount;
+                if (trialCount < 4)
+                {
+                    const double INV_MASS = 1.0 / 10.0;
+                    const double WEIGHTS[] = {1.0, 2.0, 3.0, 4.0};
+                    v3 s = add(add(add(mul(vp[0], WEIGHTS[(trialCount + 0) % 4]), mul(vp[1], WEIGHTS[(trialCount + 1) % 4])),
+                                   mul(vp[2], WEIGHTS[(trialCount + 2) % 4])),
+                               mul(vp[3], WEIGHTS[(trialCount + 3) % 4]));
+                    orig = mul(s, INV_MASS);
+                    dir = normalize(sub(orig, position));
+                }
+                else
+                {
+                    isUnreachable = 1;
+                    break;
+                }
+            }
+        }
+    }
+    if (isUnreachable)
+    {
+        double sum = 0.0;
+        for (int k = 0; k < 4; ++k)
+        {
+            if (coor[k] < 0.0) coor[k] = 0.0;
+            else sum += coor[k];
+        }
+        for (int k = 0; k < 4; ++k) coor[k] /= sum;
+    }
+    m3 r = mscale(m->bg_metric[tet[0]], coor[0]);
+    r = madd(r, mscale(m->bg_metric[tet[1]], coor[1]));
+    r = madd(r, mscale(m->bg_metric[tet[2]], coor[2]));
+    r = madd(r, mscale(m->bg_metric[tet[3]], coor[3]));
+    return r;
+}
+
 static m3 metric_at(const om_mesh* m, v3 p)
 {
     switch (m->sampler)
     {
     case OM_SAMPLER_ANALYTIC:
-    {
-        /* AbstractSampler::vertMetric(position) (AbstractSampler.cpp:190-208),
-         * returned by AnalyticSampler::metricAt (AnalyticSampler.cpp:45-49) */
-        double x = mmulv(m->rot, p).x * (2.5 * 3.14159265358979323846);
-        double a = m->aspect_ratio;
-        double c = (1.0 - cos(x)) / 2.0;
-        double sizeX = m->scaling * pow(a, pow(c, a));
-        double Mx = sizeX * sizeX;
-        double My = m->scaling2;
-        double Mz = My;
-        m3 Mm = mdiag(Mx, My, Mz);
-        return mmul(mmul(m->rotinv, Mm), m->rot);
-    }
+        /* AnalyticSampler::metricAt (AnalyticSampler.cpp:45-49) */
+        return analytic_metric(m, p);
+    case OM_SAMPLER_LOCAL:
+        return local_metric(m, p, tl_cache);
     case OM_SAMPLER_SINE:
     {
         /* sine-graded anisotropic metric s^2 * diag(1 + 9 sin^2(4 pi x), 1, 1):
@@ -875,8 +1203,18 @@ static inline const uint32_t* elem_verts(const om_mesh* m, int type, int64_t idx
     return m->hexs + 8 * idx;
 }
 
+/* the element's sampler cache (its first background tet) for the measures
+ * that follow; only the local sampler reads it */
+static inline void use_elem_cache(const om_mesh* m, int type, int64_t idx)
+{
+    if (!m->ecache) return;
+    int64_t off = type == OM_TET ? 0 : type == OM_PRI ? m->nt : m->nt + m->np;
+    tl_cache = m->ecache[off + idx];
+}
+
 static double element_quality(const om_mesh* m, int type, int64_t idx)
 {
+    use_elem_cache(m, type, idx);
     int n;
     const uint32_t* e = elem_verts(m, type, idx, &n);
     v3 vp[8];
@@ -1194,6 +1532,7 @@ static v3 vertex_equilibrium(const om_mesh* m, uint32_t v)
                 if (d.x != 0.0 || d.y != 0.0 || d.z != 0.0)
                 {
                     const v3 nn = normalize(d);
+                    if (m->vcache) tl_cache = m->vcache[ev[k]]; /* sampler.metricAt(v.p, v.c) */
                     const m3 Mm = metric_at(m, p);
                     const double weight = sqrt(dot(nn, mmulv(Mm, nn)));
                     totalWeight += weight;
@@ -1310,6 +1649,7 @@ typedef struct
 /* GetmeSmoother::smoothTets (Smoothers/ElementWise/GetmeSmoother.cpp:55-125) */
 static void getme_tet(const om_mesh* m, int64_t eId, double lambda, corner_out* out)
 {
+    use_elem_cache(m, OM_TET, eId);
     const uint32_t* vi = m->tets + 4 * eId;
     v3 vp[4], vpp[4];
     for (int k = 0; k < 4; ++k) vp[k] = P(m, vi[k]);
@@ -1337,6 +1677,7 @@ static void getme_tet(const om_mesh* m, int64_t eId, double lambda, corner_out* 
 /* GetmeSmoother::smoothPris (GetmeSmoother.cpp:127-233) */
 static void getme_pri(const om_mesh* m, int64_t eId, double lambda, corner_out* out)
 {
+    use_elem_cache(m, OM_PRI, eId);
     const uint32_t* vi = m->pris + 6 * eId;
     v3 vp[6], vpp[6];
     for (int k = 0; k < 6; ++k) vp[k] = P(m, vi[k]);
@@ -1377,6 +1718,7 @@ static void getme_pri(const om_mesh* m, int64_t eId, double lambda, corner_out* 
 /* GetmeSmoother::smoothHexs (GetmeSmoother.cpp:235-374) */
 static void getme_hex(const om_mesh* m, int64_t eId, double lambda, corner_out* out)
 {
+    use_elem_cache(m, OM_HEX, eId);
     const uint32_t* vi = m->hexs + 8 * eId;
     v3 vp[8], vpp[8];
     for (int k = 0; k < 8; ++k) vp[k] = P(m, vi[k]);

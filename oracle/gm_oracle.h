@@ -32,6 +32,7 @@ extern "C" {
 #define OM_SAMPLER_UNIFORM 0
 #define OM_SAMPLER_ANALYTIC 1
 #define OM_SAMPLER_SINE 2
+#define OM_SAMPLER_LOCAL 3 /* LocalSampler: the analytic metric on a background copy of the mesh */
 
 #define OM_MEASURER_METRIC_FREE 0
 #define OM_MEASURER_METRIC_WISE 1

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libgm_oracle.so")
 
-SAMPLER = {"uniform": 0, "analytic": 1, "sine": 2}
+SAMPLER = {"uniform": 0, "analytic": 1, "sine": 2, "local": 3}
 MEASURER = {"metric_free": 0, "metric_wise": 1}
 EVALUATOR = {"mean_ratio": 0, "metric_conformity": 1}
 SMOOTHER = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3, "spring_laplace": 4,

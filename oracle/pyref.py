@@ -16,7 +16,7 @@ import refbuild
 BOUNDARY = {"free": 0, "box": 1, "sphere": 2, "tet": 3, "pipe": 4, "shell": 5}
 SMOOTHER = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3, "spring_laplace": 4,
             "quality_laplace": 5}
-SAMPLER = {"uniform": 0, "analytic": 1, "sine": 2}
+SAMPLER = {"uniform": 0, "analytic": 1, "sine": 2, "local": 3}
 EVALUATOR = {"mean_ratio": 0, "metric_conformity": 1}
 
 _lib = None

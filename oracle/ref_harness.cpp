@@ -34,6 +34,7 @@
 #include "Evaluators/MetricConformityEvaluator.h"
 #include "Measurers/AbstractMeasurer.h"
 #include "Samplers/AnalyticSampler.h"
+#include "Samplers/LocalSampler.h"
 #include "Samplers/UniformSampler.h"
 #include "Smoothers/ElementWise/GetmeSmoother.h"
 #include "Smoothers/ElementWise/VertexAccum.h"
@@ -196,15 +197,19 @@ void ref_get_tets(void* h, uint32_t* out)
         for (int k = 0; k < 4; ++k) out[4 * i + k] = r->mesh.tets[i].v[k];
 }
 
-// sampler: 0 uniform, 1 analytic, 2 sine; evaluator: 0 mean ratio, 1 metric conformity
+// sampler: 0 uniform, 1 analytic, 2 sine, 3 local; evaluator: 0 mean ratio, 1 metric conformity
 void ref_set_crew(void* h, int sampler, int evaluator, double scaling, double aspect)
 {
     Ref* r = static_cast<Ref*>(h);
     if (sampler == 1) r->sampler.reset(new AnalyticSampler());
     else if (sampler == 2) r->sampler.reset(new SineSampler());
+    else if (sampler == 3) r->sampler.reset(new LocalSampler());
     else r->sampler.reset(new UniformSampler());
     r->sampler->setScaling(scaling);
     r->sampler->setAspectRatio(aspect);
+    // GpuMeshCharacter::updateSampling: the local sampler's background mesh
+    // and vertex metrics from the mesh as it is now
+    if (sampler == 3) r->sampler->updateAnalyticalMetric(r->mesh);
     if (evaluator == 1) r->evaluator.reset(new MetricConformityEvaluator());
     else r->evaluator.reset(new MeanRatioEvaluator());
     r->crew.setSampler(r->mesh, r->sampler);

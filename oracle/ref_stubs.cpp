@@ -7,6 +7,7 @@
 
 #include <GLM/glm.hpp>
 
+#include "DataStructures/GpuMesh.h"
 #include "DataStructures/Mesh.h"
 #include "DataStructures/NodeGroups.h"
 
@@ -23,6 +24,11 @@ void installCudaMetricFreeMeasurer() { cuda_driver_called("installCudaMetricFree
 void installCudaMetricWiseMeasurer() { cuda_driver_called("installCudaMetricWiseMeasurer"); }
 void installCudaAnalyticSampler() { cuda_driver_called("installCudaAnalyticSampler"); }
 void installCudaUniformSampler() { cuda_driver_called("installCudaUniformSampler"); }
+void installCudaLocalSampler() { cuda_driver_called("installCudaLocalSampler"); }
+void updateCudaLocalTets(const std::vector<GpuLocalTet>&) { cuda_driver_called("updateCudaLocalTets"); }
+void updateCudaLocalCache(const std::vector<GLuint>&) { cuda_driver_called("updateCudaLocalCache"); }
+void updateCudaRefVerts(const std::vector<GpuVert>&) { cuda_driver_called("updateCudaRefVerts"); }
+void updateCudaRefMetrics(const std::vector<GpuMetric>&) { cuda_driver_called("updateCudaRefMetrics"); }
 void installCudaGetmeSmoother() { cuda_driver_called("installCudaGetmeSmoother"); }
 void installCudaNelderMeadSmoother(float, int, float, float, float, float, float)
 {

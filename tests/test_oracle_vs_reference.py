@@ -30,9 +30,18 @@ CASES = {
                        dict(sampler="uniform", evaluator="metric_conformity", scaling=2.0)),
 }
 
+# LocalSampler: the analytic metric interpolated on a background copy of the
+# mesh, located by walking from the element's or vertex's cached tet
+LOCAL_CASES = {
+    "tet_local_mc": (lambda: meshgen.box_mesh(4, "tet", 0.25, 6), "box",
+                     dict(sampler="local", evaluator="metric_conformity", scaling=2.0, aspect_ratio=3.0)),
+    "mixed_local_mr": (lambda: meshgen.box_mesh(4, "mixed", 0.1, 7), "box",
+                       dict(sampler="local", evaluator="mean_ratio", scaling=2.0, aspect_ratio=3.0)),
+}
+
 
 def setup(case):
-    build, boundary, crew = CASES[case]
+    build, boundary, crew = {**CASES, **LOCAL_CASES}[case]
     raw = build()
     ref = pyref.RefMesh(raw, boundary)
     ref.set_crew(**crew)
@@ -110,4 +119,34 @@ def test_getme_matches_reference(case):
     for _ in range(2):
         ref.smooth("getme", 1)
         orc.smooth_pass("getme", groups.group_base, groups.members, nthreads=3)
+    assert np.array_equal(ref.pos, orc.pos)
+
+
+@pytest.mark.parametrize("case", list(LOCAL_CASES))
+def test_local_sampler_evaluation_matches_reference(case):
+    raw, ref, perm, groups, pr, orc = setup(case)
+    for t, arr in ((0, pr.tets), (2, pr.pris), (3, pr.hexs)):
+        for i in range(arr.shape[0]):
+            assert ref.element_quality(t, i) == orc.element_quality(t, i), (t, i)
+    for v in range(pr.nv):
+        assert ref.patch_quality(v) == orc.patch_quality(v), v
+    r, o = ref.evaluate(thread=True), orc.evaluate(nthreads=3)
+    assert r["min"] == o["min"] and r["count"] == o["count"]
+
+
+@pytest.mark.parametrize("case", list(LOCAL_CASES))
+@pytest.mark.parametrize("smoother", ["nelder_mead", "gradient_descent", "spawn_search", "spring_laplace",
+                                      "quality_laplace"])
+def test_local_sampler_smoothing_matches_reference(case, smoother):
+    raw, ref, perm, groups, pr, orc = setup(case)
+    ref.smooth(smoother, 1)
+    orc.smooth_pass(smoother, groups.group_base, groups.members, nthreads=4)
+    assert np.array_equal(ref.pos, orc.pos)
+
+
+@pytest.mark.parametrize("case", ["mixed_local_mr"])
+def test_local_sampler_getme_matches_reference(case):
+    raw, ref, perm, groups, pr, orc = setup(case)
+    ref.smooth("getme", 1)
+    orc.smooth_pass("getme", groups.group_base, groups.members, nthreads=3)
     assert np.array_equal(ref.pos, orc.pos)
