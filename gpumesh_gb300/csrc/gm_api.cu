@@ -26,10 +26,10 @@ namespace {
 
 void set_crew(gm_mesh* m, int sampler, int measurer, int evaluator, double scaling, double aspect)
 {
-    require(sampler >= 0 && sampler <= 2, "unknown sampler");
+    require(sampler >= 0 && sampler <= GM_SAMPLER_LOCAL, "unknown sampler");
     require(measurer >= 0 && measurer <= 1, "unknown measurer");
     require(evaluator >= 0 && evaluator <= 1, "unknown evaluator");
-    Crew& c = m->crew;
+    Crew c = m->crew;
     c.sampler = sampler;
     c.measurer = measurer;
     c.evaluator = evaluator;
@@ -64,6 +64,30 @@ void set_crew(gm_mesh* m, int sampler, int measurer, int evaluator, double scali
     rot(A, pi / 4.0, 0, -1, 0, c.rot);
     for (int j = 0; j < 3; ++j)
         for (int r = 0; r < 3; ++r) c.rotinv[j * 3 + r] = c.rot[r * 3 + j];
+    c.local = nullptr;
+    if (sampler == GM_SAMPLER_LOCAL)
+    {
+        // GpuMeshCharacter::updateSampling rebuilds the background when the
+        // scaling or the aspect ratio changes (GpuMeshCharacter.cpp:1115-1129)
+        const auto& L = m->local;
+        if (!L || (L->from_mesh && (L->scaling != scaling || L->aspect != aspect)))
+            m->local = local_background_from_mesh(m, c);
+        c.local = m->local->field.p;
+    }
+    m->crew = c;  // only once everything above succeeded
+}
+
+// a new topology: the local sampler's background follows it while the local
+// sampler is installed, and is dropped otherwise (rebuilt when installed)
+void topology_changed(gm_mesh* m)
+{
+    if (m->crew.sampler == GM_SAMPLER_LOCAL)
+    {
+        m->local = local_background_from_mesh(m, m->crew);
+        m->crew.local = m->local->field.p;
+    }
+    else
+        m->local.reset();
 }
 
 void update_patch_shape(gm_mesh* m, const uint32_t* ve_off_host)
@@ -502,6 +526,7 @@ gm_status gm_mesh_upload(gm_mesh* m, uint32_t nv, const double* xyz, const int32
         upload(m->hexs, reinterpret_cast<const uint4*>(hexs), (size_t)nh * 2, m->stream);
         upload_csr(m, ve_off, ve, vv_off, vv);
         GM_CUDA(cudaStreamSynchronize(m->stream));
+        topology_changed(m);
     });
 }
 
@@ -667,6 +692,27 @@ gm_status gm_mesh_set_crew(gm_mesh* m, int32_t sampler, int32_t measurer, int32_
     });
 }
 
+gm_status gm_mesh_build_local_background(gm_mesh* m)
+{
+    return guarded([&] {
+        require(m != nullptr, "null mesh");
+        drop_job(m);
+        m->local = local_background_from_mesh(m, m->crew);
+        if (m->crew.sampler == GM_SAMPLER_LOCAL) m->crew.local = m->local->field.p;
+    });
+}
+
+gm_status gm_mesh_set_local_background(gm_mesh* m, uint32_t ntets, const uint32_t* tets8, uint32_t nverts,
+                                       const double* xyz, const double* metrics6)
+{
+    return guarded([&] {
+        require(m != nullptr, "null mesh");
+        drop_job(m);
+        m->local = local_background_given(m, ntets, tets8, nverts, xyz, metrics6);
+        if (m->crew.sampler == GM_SAMPLER_LOCAL) m->crew.local = m->local->field.p;
+    });
+}
+
 gm_status gm_mesh_clone(gm_mesh* dst, const gm_mesh* src)
 {
     return guarded([&] {
@@ -701,6 +747,7 @@ gm_status gm_mesh_clone(gm_mesh* dst, const gm_mesh* src)
         dst->n_members = src->n_members;
         dst->group_base = src->group_base;
         dst->crew = src->crew;
+        dst->local = src->local;  // shared, so dst->crew.local stays valid
         dst->ks = src->ks;
         dst->maxe = src->maxe;
         dst->warps_per_block = src->warps_per_block;
@@ -718,6 +765,7 @@ gm_status gm_mesh_device_bytes(const gm_mesh* m, uint64_t* bytes)
         b += m->con.cap * sizeof(Constraint) + m->parts.cap * sizeof(EvalPartial) + m->corners.cap * sizeof(float4);
         b += m->saved.cap * sizeof(float4) + m->def_v.cap * 4 + (m->def_old.cap + m->def_new.cap) * sizeof(float4);
         b += m->quality.cap * sizeof(Quality);
+        if (m->local) b += m->local->bytes();
         *bytes = b;
     });
 }

@@ -25,7 +25,7 @@ constexpr int kTet = 0;
 constexpr int kPri = 2;
 constexpr int kHex = 3;
 
-enum : int { kSamplerUniform = 0, kSamplerAnalytic = 1, kSamplerSine = 2 };
+enum : int { kSamplerUniform = 0, kSamplerAnalytic = 1, kSamplerSine = 2, kSamplerLocal = 3 };
 enum : int { kMeasurerMetricFree = 0, kMeasurerMetricWise = 1 };
 enum : int { kEvalMeanRatio = 0, kEvalMetricConformity = 1 };
 enum : int
@@ -40,12 +40,38 @@ enum : int
     kConPipeCircle = 7    // PipeBoundary::Y*CircleEdge: a pipe-end circle, centre in a
 };
 
+// LocalSampler's background mesh in device memory (Samplers/LocalSampler.cpp:
+// 352-429): the mesh as it was when the crew was set, split into tets, their
+// face neighbours, the analytic metric at its vertices, and a uniform grid
+// whose every cell names a tet near it, where a walk starts.
+struct LocalField
+{
+    uint32_t nbg;
+    const uint4* tv;      // background tet vertices
+    const uint4* tn;      // neighbour across the face opposite vertex k (0xffffffff: none)
+    const float4* pf;     // background vertex positions
+    const double* pd;     // the same in FP64, 3 per vertex
+    const float* mf;      // vertex metrics xx yy zz xy xz yz
+    const double* md;
+    const uint32_t* cell;    // grid cell -> start tet
+    const uint32_t* ecache;  // element (tets, prisms, hexes) -> its first background tet; null: none
+    uint32_t nt, np, ne;     // tets, prisms and elements the caches were built for
+    int g[3];
+    double lo[3], inv_h[3];
+};
+
+// the element a metric is sampled for, as a walk start hint:
+// type << 27 | element id (kNoHint: none)
+constexpr uint32_t kNoHint = 0xffffffffu;
+__device__ __forceinline__ uint32_t elem_hint(int type, uint32_t id) { return ((uint32_t)type << 27) | id; }
+
 // smoothing-wide parameters, passed by value to every kernel
 struct Crew
 {
     int sampler, measurer, evaluator, pad;
     double scaling, scaling2, scaling3, aspect;
     double rot[9], rotinv[9];  // column-major, AbstractSampler::_rotMat / _rotInv
+    const LocalField* local;   // kSamplerLocal only
 };
 
 // one boundary constraint (index = constraint id)
@@ -220,8 +246,178 @@ __device__ __noinline__ Sym3<R> analytic_metric(const Crew& c, V3<R> p)
     return M;
 }
 
+// LocalSampler::metricAt (Samplers/LocalSampler.cpp:212-311) on the device:
+// the walk starts at the grid cell's tet instead of a per-element cache (the
+// reference starts at the element's first background tet); each step leaves
+// the current tet through the face that a ray from its centroid (or from one
+// of four weighted interior points) crosses, at most kLocalWalk steps; then
+// the vertex metrics are interpolated barycentrically, with the coordinates
+// clamped when the point lies outside the background mesh.  A point within
+// the reference's -1e-4 tolerance of a face may settle in either tet, so the
+// metric agrees with the CPU walk's to that tolerance, not bit for bit.
+constexpr int kLocalWalk = 512;
+// MeshTet::tris (DataStructures/Mesh.cpp:30-35): the face opposite vertex f,
+// three 2-bit vertex indices
+__device__ __forceinline__ int tet_face(int f) { return f == 0 ? 0x39 : f == 1 ? 0x2c : f == 2 ? 0x34 : 0x18; }
+
 template <class R>
-__device__ __forceinline__ Sym3<R> metric_at(const Crew& c, V3<R> p)
+__device__ __forceinline__ V3<R> local_pos(const LocalField& L, uint32_t v)
+{
+    if constexpr (sizeof(R) == 8)
+        return V3<R>{(R)L.pd[3 * (size_t)v], (R)L.pd[3 * (size_t)v + 1], (R)L.pd[3 * (size_t)v + 2]};
+    else
+    {
+        const float4 q = __ldg(&L.pf[v]);
+        return V3<R>{(R)q.x, (R)q.y, (R)q.z};
+    }
+}
+
+template <class R>
+__device__ __forceinline__ bool local_params(const V3<R>* vp, V3<R> p, R coor[4])
+{
+    // y = T^-1 (p - v3), T = [v0 - v3, v1 - v3, v2 - v3]
+    const V3<R> c0 = vp[0] - vp[3], c1 = vp[1] - vp[3], c2 = vp[2] - vp[3], d = p - vp[3];
+    const R det = det3(c0, c1, c2);
+    const R id = R(1) / det;
+    coor[0] = det3(d, c1, c2) * id;
+    coor[1] = det3(c0, d, c2) * id;
+    coor[2] = det3(c0, c1, d) * id;
+    coor[3] = R(1) - (coor[0] + coor[1] + coor[2]);
+    const R eps = R(-1e-4);
+    return coor[0] >= eps && coor[1] >= eps && coor[2] >= eps && coor[3] >= eps;
+}
+
+template <class R>
+__device__ __forceinline__ bool local_tri_intersect(V3<R> v1, V3<R> v2, V3<R> v3, V3<R> orig, V3<R> dir)
+{
+    const V3<R> e1 = v2 - v1, e2 = v3 - v1;
+    const V3<R> pvec = cross(dir, e2);
+    const R det = dot(pvec, e1);
+    if (det < R(1e-12)) return false;
+    const V3<R> tvec = orig - v1;
+    const R u = dot(tvec, pvec);
+    if (u < R(0) || u > det) return false;
+    const V3<R> qvec = cross(tvec, e1);
+    const R v = dot(dir, qvec);
+    return !(v < R(0) || v + u > det);
+}
+
+// start of the walk: the element's first background tet, as the reference's
+// measures set the sampler cache per element (so that a point outside the
+// background clamps in the same tet), else the grid cell's tet
+__device__ __forceinline__ uint32_t local_start_elem(const LocalField& L, uint32_t hint)
+{
+    if (hint == kNoHint || !L.ecache) return kNoHint;
+    const uint32_t type = hint >> 27, id = hint & ((1u << 27) - 1);
+    const uint32_t e = id + (type == (uint32_t)kTet ? 0u : type == (uint32_t)kPri ? L.nt : L.nt + L.np);
+    return e < L.ne ? __ldg(&L.ecache[e]) : kNoHint;  // a mesh since re-uploaded: no cache
+}
+
+template <class R>
+__device__ __noinline__ Sym3<R> local_metric(const LocalField& L, V3<R> p, uint32_t hint)
+{
+    uint32_t t = local_start_elem(L, hint);
+    if (t == kNoHint)
+    {
+        int ci[3];
+        const R pc[3] = {p.x, p.y, p.z};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            const R f = (pc[k] - (R)L.lo[k]) * (R)L.inv_h[k];
+            int i = f > R(0) ? (int)f : 0;
+            ci[k] = i < L.g[k] ? i : L.g[k] - 1;
+        }
+        t = L.cell[((size_t)ci[2] * L.g[1] + ci[1]) * L.g[0] + ci[0]];
+    }
+    uint4 tv = __ldg(&L.tv[t]);
+    V3<R> vp[4] = {local_pos<R>(L, tv.x), local_pos<R>(L, tv.y), local_pos<R>(L, tv.z), local_pos<R>(L, tv.w)};
+    R coor[4];
+    bool unreachable = false;
+    int steps = 0;
+    while (!local_params(vp, p, coor))
+    {
+        if (++steps > kLocalWalk)
+        {
+            unreachable = true;
+            break;
+        }
+        V3<R> orig = (vp[0] + vp[1] + vp[2] + vp[3]) * R(0.25);
+        V3<R> dir = normalize(orig - p);
+        int exit_face = -1;
+        for (int trial = -1; trial < 4 && exit_face < 0; ++trial)
+        {
+            if (trial >= 0)
+            {
+                const R w[4] = {R(1), R(2), R(3), R(4)};
+                orig = (vp[0] * w[(trial + 0) % 4] + vp[1] * w[(trial + 1) % 4] + vp[2] * w[(trial + 2) % 4] +
+                        vp[3] * w[(trial + 3) % 4]) * R(0.1);
+                dir = normalize(orig - p);
+            }
+#pragma unroll
+            for (int f = 0; f < 4; ++f)
+            {
+                const int q = tet_face(f);
+                if (local_tri_intersect(vp[q & 3], vp[(q >> 2) & 3], vp[q >> 4], orig, dir))
+                {
+                    exit_face = f;
+                    break;
+                }
+            }
+        }
+        if (exit_face < 0)
+        {
+            unreachable = true;
+            break;
+        }
+        const uint4 tn = __ldg(&L.tn[t]);
+        const uint32_t nb = exit_face == 0 ? tn.x : exit_face == 1 ? tn.y : exit_face == 2 ? tn.z : tn.w;
+        if (nb == 0xffffffffu)
+        {
+            unreachable = true;
+            break;
+        }
+        t = nb;
+        tv = __ldg(&L.tv[t]);
+        vp[0] = local_pos<R>(L, tv.x);
+        vp[1] = local_pos<R>(L, tv.y);
+        vp[2] = local_pos<R>(L, tv.z);
+        vp[3] = local_pos<R>(L, tv.w);
+    }
+    if (unreachable)
+    {
+        R sum = R(0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            if (coor[k] < R(0)) coor[k] = R(0);
+            else sum += coor[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) coor[k] /= sum;
+    }
+    const uint32_t vv[4] = {tv.x, tv.y, tv.z, tv.w};
+    Sym3<R> M{R(0), R(0), R(0), R(0), R(0), R(0)};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        R m6[6];
+        if constexpr (sizeof(R) == 8)
+            for (int j = 0; j < 6; ++j) m6[j] = (R)L.md[6 * (size_t)vv[k] + j];
+        else
+            for (int j = 0; j < 6; ++j) m6[j] = (R)__ldg(&L.mf[6 * (size_t)vv[k] + j]);
+        M.xx += coor[k] * m6[0];
+        M.yy += coor[k] * m6[1];
+        M.zz += coor[k] * m6[2];
+        M.xy += coor[k] * m6[3];
+        M.xz += coor[k] * m6[4];
+        M.yz += coor[k] * m6[5];
+    }
+    return M;
+}
+
+template <class R>
+__device__ __forceinline__ Sym3<R> metric_at(const Crew& c, V3<R> p, uint32_t hint = kNoHint)
 {
     if (c.sampler == kSamplerSine)
     {
@@ -231,6 +427,7 @@ __device__ __forceinline__ Sym3<R> metric_at(const Crew& c, V3<R> p)
         return {s2 * (R(1) + R(9) * s * s), s2, s2, R(0), R(0), R(0)};
     }
     if (c.sampler == kSamplerAnalytic) return analytic_metric(c, p);
+    if (c.sampler == kSamplerLocal) return local_metric(*c.local, p, hint);
     R s2 = (R)c.scaling2;
     return {s2, s2, s2, R(0), R(0), R(0)};
 }
@@ -468,14 +665,15 @@ __device__ __forceinline__ EQ<float> mr_hex_fast(const V3<float>* p)
 
 // MetricConformityEvaluator::specifiedMetric: 5-point Keast rule
 template <class R>
-__device__ __forceinline__ Sym3<R> specified_metric(const Crew& c, V3<R> v0, V3<R> v1, V3<R> v2, V3<R> v3)
+__device__ __forceinline__ Sym3<R> specified_metric(const Crew& c, V3<R> v0, V3<R> v1, V3<R> v2, V3<R> v3,
+                                                    uint32_t hint)
 {
     const R H = R(0.5), Q = R((1.0 - 0.5) / 3.0);
-    Sym3<R> m0 = metric_at(c, (v0 + v1 + v2 + v3) * R(0.25));
-    Sym3<R> m1 = metric_at(c, v0 * H + v1 * Q + v2 * Q + v3 * Q);
-    Sym3<R> m2 = metric_at(c, v0 * Q + v1 * H + v2 * Q + v3 * Q);
-    Sym3<R> m3 = metric_at(c, v0 * Q + v1 * Q + v2 * H + v3 * Q);
-    Sym3<R> m4 = metric_at(c, v0 * Q + v1 * Q + v2 * Q + v3 * H);
+    Sym3<R> m0 = metric_at(c, (v0 + v1 + v2 + v3) * R(0.25), hint);
+    Sym3<R> m1 = metric_at(c, v0 * H + v1 * Q + v2 * Q + v3 * Q, hint);
+    Sym3<R> m2 = metric_at(c, v0 * Q + v1 * H + v2 * Q + v3 * Q, hint);
+    Sym3<R> m3 = metric_at(c, v0 * Q + v1 * Q + v2 * H + v3 * Q, hint);
+    Sym3<R> m4 = metric_at(c, v0 * Q + v1 * Q + v2 * Q + v3 * H, hint);
     const R a = R(-0.8), b = R(0.45);
     Sym3<R> r;
     r.xx = m0.xx * a + (m1.xx + m2.xx + m3.xx + m4.xx) * b;
@@ -692,11 +890,11 @@ __device__ __noinline__ EQ<R> mc_hex_diag(const Crew& c, const V3<R>* p)
 }
 
 template <class R>
-__device__ __forceinline__ EQ<R> mc_tet(const Crew& c, const V3<R>* p)
+__device__ __forceinline__ EQ<R> mc_tet(const Crew& c, const V3<R>* p, uint32_t hint)
 {
     V3<R> c0, c1, c2;
     tet_frame(p[3] - p[0], p[3] - p[1], p[3] - p[2], c0, c1, c2);
-    Sym3<R> Ms = specified_metric(c, p[0], p[1], p[2], p[3]);
+    Sym3<R> Ms = specified_metric(c, p[0], p[1], p[2], p[3], hint);
     R rq = 0, q = 0;
     bool pos;
     mc_corner(c0, c1, c2, Ms, rq, q, pos);
@@ -704,7 +902,7 @@ __device__ __forceinline__ EQ<R> mc_tet(const Crew& c, const V3<R>* p)
 }
 
 template <class R>
-__device__ __noinline__ EQ<R> mc_pri(const Crew& c, const V3<R>* p)
+__device__ __noinline__ EQ<R> mc_pri(const Crew& c, const V3<R>* p, uint32_t hint)
 {
     V3<R> e03 = p[3] - p[0], e14 = p[4] - p[1], e25 = p[5] - p[2];
     V3<R> e01 = p[1] - p[0], e12 = p[2] - p[1], e20 = p[0] - p[2];
@@ -713,17 +911,17 @@ __device__ __noinline__ EQ<R> mc_pri(const Crew& c, const V3<R>* p)
     V3<R> a, b, d;
     R rq = 0, q = 0;
     bool pos;
-    pri_frame(-e01, e20, e03, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[3]), rq, q, pos); acc.add(rq, q, pos);
-    pri_frame(-e12, e01, e14, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[4]), rq, q, pos); acc.add(rq, q, pos);
-    pri_frame(-e20, e12, e25, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[5]), rq, q, pos); acc.add(rq, q, pos);
-    pri_frame(-e34, e53, e03, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[3], p[4], p[5]), rq, q, pos); acc.add(rq, q, pos);
-    pri_frame(-e45, e34, e14, a, b, d); mc_corner(a, b, d, specified_metric(c, p[1], p[3], p[4], p[5]), rq, q, pos); acc.add(rq, q, pos);
-    pri_frame(-e53, e45, e25, a, b, d); mc_corner(a, b, d, specified_metric(c, p[2], p[3], p[4], p[5]), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e01, e20, e03, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[3], hint), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e12, e01, e14, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[4], hint), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e20, e12, e25, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[1], p[2], p[5], hint), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e34, e53, e03, a, b, d); mc_corner(a, b, d, specified_metric(c, p[0], p[3], p[4], p[5], hint), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e45, e34, e14, a, b, d); mc_corner(a, b, d, specified_metric(c, p[1], p[3], p[4], p[5], hint), rq, q, pos); acc.add(rq, q, pos);
+    pri_frame(-e53, e45, e25, a, b, d); mc_corner(a, b, d, specified_metric(c, p[2], p[3], p[4], p[5], hint), rq, q, pos); acc.add(rq, q, pos);
     return acc.result(6);
 }
 
 template <class R>
-__device__ __noinline__ EQ<R> mc_hex(const Crew& c, const V3<R>* p)
+__device__ __noinline__ EQ<R> mc_hex(const Crew& c, const V3<R>* p, uint32_t hint)
 {
     V3<R> e01 = p[1] - p[0], e03 = p[3] - p[0], e04 = p[4] - p[0], e12 = p[2] - p[1];
     V3<R> e15 = p[5] - p[1], e23 = p[3] - p[2], e26 = p[6] - p[2], e37 = p[7] - p[3];
@@ -731,20 +929,21 @@ __device__ __noinline__ EQ<R> mc_hex(const Crew& c, const V3<R>* p)
     CornerAcc<R> acc;
     R rq = 0, q = 0;
     bool pos;
-    mc_corner(e01, e04, -e03, specified_metric(c, p[0], p[1], p[3], p[4]), rq, q, pos); acc.add(rq, q, pos);
-    mc_corner(e01, e12, e15, specified_metric(c, p[0], p[1], p[2], p[5]), rq, q, pos); acc.add(rq, q, pos);
-    mc_corner(e12, e26, -e23, specified_metric(c, p[1], p[2], p[3], p[6]), rq, q, pos); acc.add(rq, q, pos);
-    mc_corner(e03, e23, e37, specified_metric(c, p[0], p[2], p[3], p[7]), rq, q, pos); acc.add(rq, q, pos);
-    mc_corner(e04, e45, e47, specified_metric(c, p[0], p[4], p[5], p[7]), rq, q, pos); acc.add(rq, q, pos);
-    mc_corner(e15, -e56, e45, specified_metric(c, p[1], p[4], p[5], p[6]), rq, q, pos); acc.add(rq, q, pos);
-    mc_corner(e26, e56, e67, specified_metric(c, p[2], p[5], p[6], p[7]), rq, q, pos); acc.add(rq, q, pos);
-    mc_corner(e37, e67, -e47, specified_metric(c, p[3], p[4], p[6], p[7]), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e01, e04, -e03, specified_metric(c, p[0], p[1], p[3], p[4], hint), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e01, e12, e15, specified_metric(c, p[0], p[1], p[2], p[5], hint), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e12, e26, -e23, specified_metric(c, p[1], p[2], p[3], p[6], hint), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e03, e23, e37, specified_metric(c, p[0], p[2], p[3], p[7], hint), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e04, e45, e47, specified_metric(c, p[0], p[4], p[5], p[7], hint), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e15, -e56, e45, specified_metric(c, p[1], p[4], p[5], p[6], hint), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e26, e56, e67, specified_metric(c, p[2], p[5], p[6], p[7], hint), rq, q, pos); acc.add(rq, q, pos);
+    mc_corner(e37, e67, -e47, specified_metric(c, p[3], p[4], p[6], p[7], hint), rq, q, pos); acc.add(rq, q, pos);
     return acc.result(8);
 }
 
 // quality of an element of the given type; MAXK = 4 means tets only
+// hint: the element (elem_hint) when known, for the local sampler's walk
 template <int VAR, int MAXK, class R>
-__device__ __forceinline__ EQ<R> elem_quality(const Crew& c, int type, const V3<R>* p)
+__device__ __forceinline__ EQ<R> elem_quality(const Crew& c, int type, const V3<R>* p, uint32_t hint = kNoHint)
 {
     if (VarTraits<VAR>::diag_metric)
     {
@@ -754,9 +953,9 @@ __device__ __forceinline__ EQ<R> elem_quality(const Crew& c, int type, const V3<
     }
     if (!VarTraits<VAR>::mean_ratio)
     {
-        if (MAXK == 4 || type == kTet) return mc_tet(c, p);
-        if (type == kPri) return mc_pri(c, p);
-        return mc_hex(c, p);
+        if (MAXK == 4 || type == kTet) return mc_tet(c, p, hint);
+        if (type == kPri) return mc_pri(c, p, hint);
+        return mc_hex(c, p, hint);
     }
     if (MAXK == 4 || type == kTet) return mr_tet<VAR, R>(c, p);
     if (type == kPri) return mr_pri<VAR, R>(c, p);

@@ -64,8 +64,8 @@ __device__ __forceinline__ int eval_element(const MeshView& m, const Crew& crew,
     }
     EQ<float> q;
     if constexpr (SET == 9 && VAR == kVarMRFree) q = mr_hex_fast(p);
-    else if constexpr (SET == 9) q = elem_quality<VAR, MAXK, float>(crew, kHex, p);
-    else q = elem_quality<VAR, MAXK, float>(crew, type, p);
+    else if constexpr (SET == 9) q = elem_quality<VAR, MAXK, float>(crew, kHex, p, elem_hint(kHex, id));
+    else q = elem_quality<VAR, MAXK, float>(crew, type, p, elem_hint(type, id));
     return acc.add(q);
 }
 
@@ -131,12 +131,14 @@ template <int SET>
 struct Conn
 {
     uint4 a, b;
+    uint32_t i;  // element index (the local sampler's walk hint)
 };
 
 template <int SET>
 __device__ __forceinline__ Conn<SET> load_conn(const MeshView& m, uint32_t i)
 {
     Conn<SET> c;
+    c.i = i;
     if (SET == 9)
     {
         c.a = __ldg(&m.hexs[2 * (size_t)i]);
@@ -169,8 +171,8 @@ __device__ __forceinline__ int eval_conn(const MeshView& m, const Crew& crew, co
     }
     EQ<float> q;
     if constexpr (SET == 9 && VAR == kVarMRFree) q = mr_hex_fast(p);
-    else if constexpr (SET == 9) q = elem_quality<VAR, MAXK, float>(crew, kHex, p);
-    else q = elem_quality<VAR, MAXK, float>(crew, kTet, p);
+    else if constexpr (SET == 9) q = elem_quality<VAR, MAXK, float>(crew, kHex, p, elem_hint(kHex, c.i));
+    else q = elem_quality<VAR, MAXK, float>(crew, kTet, p, elem_hint(kTet, c.i));
     return acc.add(q);
 }
 

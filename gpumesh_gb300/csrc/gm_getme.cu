@@ -22,7 +22,7 @@ __device__ __forceinline__ void getme_one(const MeshView& m, const Crew& crew, f
     V3<float> vp[N], vpp[N];
 #pragma unroll
     for (int k = 0; k < N; ++k) vp[k] = to<float>(m.pos[vi[k]]);
-    float w = getme_transform<VAR, float, N>(m, crew, lambda, type, vi, vp, vpp);
+    float w = getme_transform<VAR, float, N>(m, crew, lambda, type, vi, vp, vpp, elem_hint(type, id));
 #pragma unroll
     for (int k = 0; k < N; ++k) out[(size_t)id * N + k] = make_float4(vpp[k].x, vpp[k].y, vpp[k].z, w);
 }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -119,6 +120,27 @@ void upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s)
 // the smoother parameter block of the C ABI (GM_PARAMS doubles), with defaults
 SmoothParams parse_smooth_params(int smoother, const double* params);
 
+// LocalSampler's background mesh in device memory, with the LocalField that
+// points into it (the crew's `local`); shared by a mesh and its clones
+struct LocalBackground
+{
+    DBuf<uint4> tv, tn;
+    DBuf<float4> pf;
+    DBuf<double> pd, md;
+    DBuf<float> mf;
+    DBuf<uint32_t> cell, ecache;
+    DBuf<LocalField> field;
+    uint32_t nbg = 0, nref = 0;
+    bool from_mesh = false;  // built from the mesh (analytic vertex metrics) rather than given
+    double scaling = 0.0, aspect = 0.0;
+    size_t bytes() const
+    {
+        return tv.cap * 32 + pf.cap * 16 + pd.cap * 8 + md.cap * 8 + mf.cap * 4 + (cell.cap + ecache.cap) * 4 +
+               sizeof(LocalField);
+    }
+};
+
+
 }  // namespace gm
 
 using namespace gm;
@@ -163,6 +185,8 @@ struct gm_mesh
     DBuf<int> job_counter;    // passes done
     DBuf<Quality> job_fresh;  // evaluation of the pass just run
     uint32_t job_max_passes = 0;
+    // LocalSampler background (crew.local points into it)
+    std::shared_ptr<LocalBackground> local;
 
     MeshView view() const
     {
@@ -188,8 +212,8 @@ struct gm_mesh
     // evaluator x measurer variant of the vertex kernels
     int variant() const
     {
-        if (crew.evaluator == GM_EVALUATOR_METRIC_CONFORMITY)
-            return crew.sampler == GM_SAMPLER_ANALYTIC ? kVarMC : kVarMCDiag;
+        if (crew.evaluator == GM_EVALUATOR_METRIC_CONFORMITY)  // general metric, or a diagonal one
+            return (crew.sampler == GM_SAMPLER_ANALYTIC || crew.sampler == GM_SAMPLER_LOCAL) ? kVarMC : kVarMCDiag;
         return crew.measurer == GM_MEASURER_METRIC_WISE ? kVarMRWise : kVarMRFree;
     }
     // variant of the GETMe element pass, whose volumes also follow the measurer
@@ -203,4 +227,12 @@ struct gm_mesh
     // element set of the evaluation kernel: 4 tets only, 8 mixed, 9 hexes only
     int elem_set() const { return (nt == 0 && np == 0 && nh) ? 9 : maxk(); }
 };
+
+namespace gm {
+// LocalSampler backgrounds (gm_local.cu): from the resident mesh with the
+// analytic metric of `crew` at its vertices, or given by the caller
+std::shared_ptr<LocalBackground> local_background_from_mesh(gm_mesh* m, const Crew& crew);
+std::shared_ptr<LocalBackground> local_background_given(gm_mesh* m, uint32_t ntets, const uint32_t* tets8,
+                                                        uint32_t nverts, const double* xyz, const double* metrics6);
+}  // namespace gm
 

@@ -194,7 +194,7 @@ __device__ __forceinline__ void stage_patch(const MeshView& m, uint32_t v, WarpP
 #pragma unroll
         for (int k = 0; k < 8; ++k)
             if (k < n) P.sp[k * P.maxe + i] = __ldcg(&m.pos[vid[k]]);
-        P.meta[i] = type | (loc << 2);
+        P.meta[i] = (int)((uint32_t)type | ((uint32_t)loc << 2) | (ref_id(r) << 5));
     }
     __syncwarp();
 }
@@ -434,9 +434,9 @@ __device__ __forceinline__ void stage_patch_fp32(const MeshView& m, const Crew& 
 template <int VAR, int MAXK, class R>
 __device__ __forceinline__ EQ<R> staged_quality(const Crew& crew, const WarpPatch& P, int e, V3<R> c)
 {
-    int meta = P.meta[e];
-    int type = MAXK == 4 ? kTet : (meta & 3);
-    int loc = meta >> 2;
+    const uint32_t meta = (uint32_t)P.meta[e];
+    int type = MAXK == 4 ? kTet : (int)(meta & 3u);
+    int loc = (int)((meta >> 2) & 7u);
     V3<R> p[MAXK];
     int n = MAXK == 4 ? 4 : type_size(type);
 #pragma unroll
@@ -445,7 +445,7 @@ __device__ __forceinline__ EQ<R> staged_quality(const Crew& crew, const WarpPatc
         if (k < n) p[k] = (k == loc) ? c : to<R>(P.sp[k * P.maxe + e]);
         else p[k] = c;
     }
-    return elem_quality<VAR, MAXK, R>(crew, type, p);
+    return elem_quality<VAR, MAXK, R>(crew, type, p, elem_hint(type, meta >> 5));
 }
 
 // patch quality semantics of AbstractEvaluator::accumulatePatchQuality /
@@ -584,7 +584,7 @@ __device__ double patch_quality_global(const MeshView& m, const Crew& crew, uint
             if (k < n) p[k] = (k == loc) ? c : to<double>(__ldcg(&m.pos[vid[k]]));
             else p[k] = c;
         }
-        acc_add(a, elem_quality<VAR, MAXK, double>(crew, type, p));
+        acc_add(a, elem_quality<VAR, MAXK, double>(crew, type, p, elem_hint(type, ref_id(r))));
     }
     acc_reduce(a, kWarp);
     return acc_final(a, E);
@@ -975,9 +975,9 @@ __device__ __forceinline__ R hex_volume(const Crew& c, const V3<R>* vp)
 }
 
 template <int VAR, class R>
-__device__ __forceinline__ R quality_value(const Crew& c, int type, const V3<R>* p)
+__device__ __forceinline__ R quality_value(const Crew& c, int type, const V3<R>* p, uint32_t hint)
 {
-    EQ<R> q = elem_quality<VAR, 8, R>(c, type, p);
+    EQ<R> q = elem_quality<VAR, 8, R>(c, type, p, hint);
     return q.pos ? R(1) / q.v : q.v;
 }
 
@@ -985,7 +985,7 @@ __device__ __forceinline__ R quality_value(const Crew& c, int type, const V3<R>*
 // position (their VertexConstraint), constrained corners are projected
 template <int VAR, class R, int N>
 __device__ __forceinline__ R getme_transform(const MeshView& m, const Crew& c, R lambda, int type, const uint32_t* vi,
-                                             const V3<R>* vp, V3<R>* vpp)
+                                             const V3<R>* vp, V3<R>* vpp, uint32_t hint)
 {
     V3<R> nrm[N];
     if (N == 4)
@@ -1049,8 +1049,8 @@ __device__ __forceinline__ R getme_transform(const MeshView& m, const Crew& c, R
         if (id < 0) vpp[k] = vp[k];
         else if (id > 0) vpp[k] = snap(m, id, vpp[k]);
     }
-    R q = quality_value<VAR, R>(c, type, vp);
-    R qp = quality_value<VAR, R>(c, type, vpp);
+    R q = quality_value<VAR, R>(c, type, vp, hint);
+    R qp = quality_value<VAR, R>(c, type, vpp, hint);
     return qp / (R(1) + q);
 }
 

@@ -146,6 +146,21 @@ class AnalyticSampler(AbstractSampler):
     metric_wise = True
 
 
+class LocalSampler(AbstractSampler):
+    """Samplers/LocalSampler.cpp: the analytic metric stored at the vertices
+    of a background tet mesh (the mesh when the sampling was last updated,
+    split into tets) and interpolated barycentrically in the tet holding the
+    point.  updateAnalyticalMetric (:193-203) rebuilds the background from
+    the mesh's current positions."""
+    kind = "local"
+    metric_wise = True
+
+    def updateAnalyticalMetric(self, mesh):
+        dev = mesh.device()
+        dev.set_crew(self.kind, "metric_wise", "mean_ratio", self.scaling(), self.aspectRatio())
+        dev.build_local_background()
+
+
 class SineSampler(AbstractSampler):
     """Sine-graded anisotropic metric scaling^2 * diag(1 + 9 sin^2(4 pi x), 1, 1)."""
     kind = "sine"
@@ -282,6 +297,22 @@ class DeviceMesh:
     def set_crew(self, sampler: str, measurer: str, evaluator: str, scaling=1.0, aspect_ratio=1.0):
         N.check(N.lib().gm_mesh_set_crew(self.h, N.SAMPLERS[sampler], N.MEASURERS[measurer],
                                          N.EVALUATORS[evaluator], float(scaling), float(aspect_ratio)))
+
+    def build_local_background(self):
+        """The local sampler's background from the resident mesh (the crew's
+        scaling and aspect ratio)."""
+        N.check(N.lib().gm_mesh_build_local_background(self.h))
+
+    def set_local_background(self, tets8: np.ndarray, verts: np.ndarray, metrics6: np.ndarray):
+        """A background given as the reference's GpuLocalTet records (4
+        vertices, 4 face neighbours), vertex positions and symmetric vertex
+        metrics (xx yy zz xy xz yz)."""
+        t = np.ascontiguousarray(tets8, np.uint32).reshape(-1, 8)
+        p = np.ascontiguousarray(verts, np.float64).reshape(-1, 3)
+        m = np.ascontiguousarray(metrics6, np.float64).reshape(-1, 6)
+        if m.shape[0] != p.shape[0]:
+            raise ValueError("one metric per background vertex")
+        N.check(N.lib().gm_mesh_set_local_background(self.h, t.shape[0], N.ptr(t), p.shape[0], N.ptr(p), N.ptr(m)))
 
     def set_stream(self, stream: int):
         N.check(N.lib().gm_mesh_set_stream(self.h, ctypes.c_void_p(stream)))

@@ -44,11 +44,14 @@ typedef int gm_status;
 #define GM_HEX 3
 
 /* samplers: UniformSampler (Samplers/UniformSampler.cpp:45), AnalyticSampler
- * (Samplers/AbstractSampler.cpp:190-208) and the sine-graded anisotropic
- * metric s^2 diag(1 + 9 sin^2(4 pi x), 1, 1) */
+ * (Samplers/AbstractSampler.cpp:190-208), the sine-graded anisotropic
+ * metric s^2 diag(1 + 9 sin^2(4 pi x), 1, 1) and LocalSampler
+ * (Samplers/LocalSampler.cpp:212-311: the metric interpolated in a
+ * background tet mesh) */
 #define GM_SAMPLER_UNIFORM 0
 #define GM_SAMPLER_ANALYTIC 1
 #define GM_SAMPLER_SINE 2
+#define GM_SAMPLER_LOCAL 3
 /* measurers: MetricFreeMeasurer, MetricWiseMeasurer (Measurers/) */
 #define GM_MEASURER_METRIC_FREE 0
 #define GM_MEASURER_METRIC_WISE 1
@@ -205,6 +208,27 @@ gm_status gm_mesh_set_constraints(gm_mesh* mesh, uint32_t n, const int32_t* kind
  * sampler's fixed one and is rebuilt here. */
 gm_status gm_mesh_set_crew(gm_mesh* mesh, int32_t sampler, int32_t measurer, int32_t evaluator, double scaling,
                            double aspect_ratio);
+/* GM_SAMPLER_LOCAL samples a background tet mesh kept with the mesh.
+ * gm_mesh_build_local_background builds it from the resident mesh as
+ * LocalSampler::updateAnalyticalMetric does (Samplers/LocalSampler.cpp:
+ * 193-203, 352-429): prisms and hexes split into tets as Tetrahedralizer.h
+ * splits them, face neighbours, the analytic metric (the crew's scaling and
+ * aspect ratio) at every vertex.  gm_mesh_set_crew with GM_SAMPLER_LOCAL
+ * builds it when the mesh has none, or has one built with another scaling or
+ * aspect ratio; a topology upload rebuilds it while the local sampler is
+ * installed.  Vertex moves leave it as it is, as in the reference. */
+gm_status gm_mesh_build_local_background(gm_mesh* mesh);
+/* Replaces updateCudaLocalTets / updateCudaRefVerts / updateCudaRefMetrics
+ * (resources/cuda/Sampling/Local.cu:143-230; LocalSampler::updateCudaData,
+ * Samplers/LocalSampler.cpp:126-158): a background given by the caller.
+ * tets8: per tet its 4 vertices, then the neighbour across the face opposite
+ * each vertex (0xffffffff: none), as GpuLocalTet (DataStructures/GpuMesh.h:
+ * 166-180); xyz: 3 doubles per vertex; metrics6: xx yy zz xy xz yz per
+ * vertex (GpuMetric is a mat4; the shim passes its symmetric 3x3 part).
+ * The per-vertex walk caches (updateCudaLocalCache) are not needed: walks
+ * start from a uniform grid over the background. */
+gm_status gm_mesh_set_local_background(gm_mesh* mesh, uint32_t ntets, const uint32_t* tets8, uint32_t nverts,
+                                       const double* xyz, const double* metrics6);
 
 /* Copy a resident mesh (topology, groups, constraints, crew, positions)
  * device to device into `dst`: a new job on an existing topology needs only

@@ -1,0 +1,157 @@
+"""The local sampler (LocalSampler: the analytic metric stored at the vertices
+of a background tet mesh, interpolated in the tet holding the point) on the
+GPU against the FP64 oracle's LocalSampler.
+
+The device walk starts from a uniform grid cell, the oracle's from the
+element's (or vertex's) cached background tet; both end in a tet holding the
+point, where the interpolated metric is the same up to rounding (a point on a
+shared face gets the same metric from either side).  Tolerances are those of
+the analytic metric's tests: FP32 element qualities, FP64 sums."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from gpumesh_gb300 import _native as N
+from gpumesh_gb300 import meshgen
+from gpumesh_gb300 import mesh as M
+
+from helpers import coloured, device_for, edge_lengths, oracle_for
+from test_gpu_evaluate import compare
+
+pytestmark = pytest.mark.gpu
+
+MRW = dict(sampler="local", measurer="metric_wise", evaluator="mean_ratio", scaling=2.0, aspect_ratio=3.0)
+MC = dict(sampler="local", measurer="metric_wise", evaluator="metric_conformity", scaling=2.0, aspect_ratio=3.0)
+
+
+@pytest.mark.parametrize("kind", ["tet", "mixed", "hex"])
+@pytest.mark.parametrize("crew", ["mrw", "mc"])
+def test_evaluation_matches_oracle(kind, crew):
+    raw = meshgen.box_mesh(6, kind, 0.15, 2, gaussian=True)
+    compare(raw, MRW if crew == "mrw" else MC, rel=1e-4)
+
+
+def _moved_inside(raw, frac, seed):
+    """Interior vertices moved by up to frac of the local size; the boundary
+    stays, so every element stays inside the background mesh."""
+    rng = np.random.default_rng(seed)
+    h = edge_lengths(raw)
+    d = rng.uniform(-1.0, 1.0, raw.pos.shape) * (frac * h)[:, None]
+    d[raw.cid != 0] = 0.0
+    return raw.pos + d
+
+
+@pytest.mark.parametrize("kind", ["tet", "mixed"])
+def test_background_stays_when_vertices_move(kind):
+    # the background is the mesh when the crew was installed; moving the
+    # vertices afterwards samples it at the new positions on both sides
+    raw = meshgen.box_mesh(6, kind, 0.1, 3)
+    moved = _moved_inside(raw, 0.15, 11)
+    dev = device_for(raw, None, MC)
+    dev.upload_positions(moved)
+    g = dev.evaluate()
+    orc = oracle_for(raw, MC)
+    orc.pos = moved.astype(np.float32).astype(np.float64)
+    o = orc.evaluate()
+    assert g.sampleCount() == o["count"] and o["min"] > 0.0
+    assert abs(g.minimumQuality() - o["min"]) <= 1e-4 * max(1.0, abs(o["min"])) + 1e-6
+    assert abs(g.harmonicMean() - o["mean"]) <= 1e-4
+    # and differs from sampling a background rebuilt at the moved positions
+    dev.build_local_background()
+    assert abs(dev.evaluate().harmonicMean() - g.harmonicMean()) > 1e-6
+
+
+def test_scaling_change_rebuilds_and_vertex_moves_do_not():
+    raw = meshgen.box_mesh(5, "mixed", 0.15, 4, gaussian=True)
+    dev = device_for(raw, None, MC)
+    a = dev.evaluate().harmonicMean()
+    dev.upload_positions(_moved_inside(raw, 0.2, 3))
+    dev.set_crew("local", "metric_wise", "metric_conformity", 2.0, 3.0)  # same sampling: background kept
+    dev.upload_positions(raw.pos)
+    assert dev.evaluate().harmonicMean() == a
+    dev.set_crew("local", "metric_wise", "metric_conformity", 3.0, 3.0)  # new scaling: rebuilt
+    o = oracle_for(raw, dict(MC, scaling=3.0)).evaluate()
+    assert abs(dev.evaluate().harmonicMean() - o["mean"]) <= 1e-4
+
+
+def _tet_neighbours(tets):
+    faces = ((1, 2, 3), (0, 3, 2), (0, 1, 3), (0, 2, 1))
+    owner = {}
+    nb = np.full((tets.shape[0], 4), 0xFFFFFFFF, np.uint64)
+    for t in range(tets.shape[0]):
+        for s, f in enumerate(faces):
+            key = tuple(sorted(int(tets[t, k]) for k in f))
+            if key in owner:
+                u, r = owner.pop(key)
+                nb[t, s], nb[u, r] = u, t
+            else:
+                owner[key] = (t, s)
+    return nb.astype(np.uint32)
+
+
+def test_given_background_matches_the_built_one():
+    # the reference's CUDA driver receives the background from the host
+    # (GpuLocalTet records, reference vertices and metrics): a tet mesh given
+    # as its own background samples as the one built from it
+    raw = meshgen.box_mesh(5, "tet", 0.2, 5)
+    built = device_for(raw, None, MC).evaluate()
+    ana = oracle_for(raw, dict(MC, sampler="analytic"))
+    m6 = np.array([[m[0, 0], m[1, 1], m[2, 2], m[0, 1], m[0, 2], m[1, 2]] for m in map(ana.metric_at, raw.pos)])
+    pos32 = raw.pos.astype(np.float32).astype(np.float64)
+    tets8 = np.concatenate([raw.tets.astype(np.uint32), _tet_neighbours(raw.tets)], axis=1)
+    dev = M.DeviceMesh(raw, None)
+    dev.set_local_background(tets8, pos32, m6)
+    dev.set_crew("local", "metric_wise", "metric_conformity", 2.0, 3.0)
+    given = dev.evaluate()
+    assert abs(given.harmonicMean() - built.harmonicMean()) <= 1e-6
+    assert abs(given.minimumQuality() - built.minimumQuality()) <= 1e-6
+
+
+def test_bad_backgrounds_are_rejected():
+    raw = meshgen.box_mesh(3, "tet", 0.2, 5)
+    dev = M.DeviceMesh(raw, None)
+    t = np.array([[0, 1, 2, 9, 0xFFFFFFFF, 0xFFFFFFFF, 0xFFFFFFFF, 0xFFFFFFFF]], np.uint32)
+    p = np.zeros((4, 3))
+    m = np.tile([1.0, 1.0, 1.0, 0.0, 0.0, 0.0], (4, 1))
+    with pytest.raises(N.GpuMeshError, match="invalid argument"):
+        dev.set_local_background(t, p, m)
+    t[0, 3], t[0, 5] = 3, 7
+    with pytest.raises(N.GpuMeshError, match="neighbour"):
+        dev.set_local_background(t, p, m)
+    # a mesh with nothing uploaded has no background to build
+    L = N.lib()
+    h = ctypes.c_void_p()
+    N.check(L.gm_mesh_create(ctypes.byref(h)))
+    try:
+        assert L.gm_mesh_set_crew(h, N.SAMPLERS["local"], 1, 1, 1.0, 1.0) == 6  # invalid state
+        assert L.gm_mesh_build_local_background(h) == 6
+    finally:
+        L.gm_mesh_destroy(h)
+
+
+def test_clone_shares_the_background():
+    raw = meshgen.box_mesh(5, "mixed", 0.15, 4, gaussian=True)
+    src = device_for(raw, None, MC)
+    want = src.evaluate().harmonicMean()
+    dst = M.DeviceMesh(None, clone_of=src)
+    src.close()
+    assert dst.evaluate().harmonicMean() == want
+
+
+@pytest.mark.parametrize("smoother", ["nelder_mead", "spring_laplace"])
+def test_one_colour_relocation_matches_oracle(smoother):
+    raw, groups = coloured(meshgen.box_mesh(7, "mixed", 0.2, 3))
+    dev = device_for(raw, groups, MC)
+    b, e = int(groups.group_base[0]), int(groups.group_base[1])
+    dev.smooth_group(smoother, b, e - b, None)
+    orc = oracle_for(raw, MC)
+    orc.pos = raw.pos.astype(np.float32).astype(np.float64)
+    orc.smooth_pass(smoother, np.array([0, e - b], np.int64), groups.members[b:e])
+    err = (np.linalg.norm(dev.fetch_positions() - orc.pos, axis=1) / edge_lengths(raw))[groups.members[b:e]]
+    if smoother == "spring_laplace":
+        assert err.max() < 1e-5, np.sort(err)[-5:]
+    else:
+        assert np.mean(err < 1e-4) >= 0.97, np.sort(err)[-10:]
+        assert np.median(err) < 1e-5
