@@ -176,6 +176,16 @@ struct om_mesh
     uint32_t* vcache;
     uint32_t* ecache; /* tets, then prisms, then hexes */
 
+    /* KdTreeSampler (Samplers/KdTreeSampler.cpp): nodes in the pre-order of
+     * buildGpuBuffers (:374-397); TextureSampler (TextureSampler.cpp): the
+     * metric grid of buildGrid (:275-448) */
+    int32_t depth;
+    int64_t nkd, kd_cap;
+    struct om_kd* kd;
+    int tex_size[3];
+    double tex_min[3], tex_ext[3];
+    m3* tex;
+
     int64_t patch_evals;
 };
 
@@ -328,6 +338,7 @@ om_mesh* om_create(int64_t nv, const double* pos, int64_t nt, const uint32_t* te
     m->cid = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nv + 1));
     memcpy(m->cid, cid, sizeof(int32_t) * (size_t)nv);
     build_topology(m);
+    m->depth = -1;
     om_set_crew(m, OM_SAMPLER_UNIFORM, OM_MEASURER_METRIC_FREE, OM_EVALUATOR_MEAN_RATIO, 1.0, 1.0);
     return m;
 }
@@ -340,6 +351,8 @@ void om_destroy(om_mesh* m)
     free(m->bg_metric);
     free(m->vcache);
     free(m->ecache);
+    free(m->kd);
+    free(m->tex);
     free(m->pos);
     free(m->tets);
     free(m->pris);
@@ -585,6 +598,258 @@ static void build_background(om_mesh* m)
         for (int k = 0; k < 4; ++k) m->vcache[m->bg[8 * t + k]] = (uint32_t)t;
 }
 
+/* ------------------------------------------------------------------------ */
+/* kd-tree and texture samplers                                              */
+/* ------------------------------------------------------------------------ */
+
+static m3 local_metric(const om_mesh* m, v3 position, uint32_t cache);
+
+/* the reference sorts vertex ids by one coordinate with std::sort; the same
+ * call (same comparisons, same order among equal coordinates) is made from
+ * the C++ helper oracle/om_sort.cpp */
+void om_argsort_axis(const double* pos, int64_t n, int axis, uint32_t* out);
+
+struct om_kd
+{
+    int64_t left, right;
+    double sep[4]; /* axis, then the separator value; a leaf keeps zeros */
+    m3 metric;
+};
+
+static int64_t kd_push(om_mesh* m)
+{
+    if (m->nkd == m->kd_cap)
+    {
+        m->kd_cap = m->kd_cap ? 2 * m->kd_cap : 64;
+        m->kd = (struct om_kd*)realloc(m->kd, sizeof(struct om_kd) * (size_t)m->kd_cap);
+    }
+    struct om_kd* k = m->kd + m->nkd;
+    memset(k, 0, sizeof(*k));
+    k->left = k->right = -1;
+    return m->nkd++;
+}
+
+static double coord(const om_mesh* m, uint32_t v, int axis) { return m->pos[3 * (size_t)v + axis]; }
+
+/* KdTreeSampler::build (KdTreeSampler.cpp:268-372): split at the median of
+ * the widest extent (x, then y, then z on ties), vertices on the separator
+ * going to both sides; a leaf (height 0 or at most 3 vertices) holds the
+ * local metric at its vertices' mean, its walk started at the first vertex's
+ * cache */
+static int64_t kd_build(om_mesh* m, int height, uint32_t* xs, uint32_t* ys, uint32_t* zs, int64_t n)
+{
+    const int64_t id = kd_push(m);
+    if (height > 0 && n > 3)
+    {
+        const double ex = coord(m, xs[n - 1], 0) - coord(m, xs[0], 0);
+        const double ey = coord(m, ys[n - 1], 1) - coord(m, ys[0], 1);
+        const double ez = coord(m, zs[n - 1], 2) - coord(m, zs[0], 2);
+        v3 axis = V(1, 0, 0);
+        const int64_t r = n / 2, l = r - 1;
+        uint32_t sl = xs[l], sr = xs[r];
+        if (ey >= ex && ey >= ez)
+        {
+            axis = V(0, 1, 0);
+            sl = ys[l];
+            sr = ys[r];
+        }
+        else if (ez >= ex && ez >= ey)
+        {
+            axis = V(0, 0, 1);
+            sl = zs[l];
+            sr = zs[r];
+        }
+        v3 sp;
+        if (n % 2 == 0)
+        {
+            v3 a = P(m, sl), b = P(m, sr);
+            sp = V((a.x + b.x) / 2.0, (a.y + b.y) / 2.0, (a.z + b.z) / 2.0);
+        }
+        else
+            sp = P(m, sr);
+        const double sv = dot(axis, sp);
+        m->kd[id].sep[0] = axis.x;
+        m->kd[id].sep[1] = axis.y;
+        m->kd[id].sep[2] = axis.z;
+        m->kd[id].sep[3] = sv;
+        uint32_t* lists[6];
+        int64_t cnt[6] = {0, 0, 0, 0, 0, 0};
+        for (int q = 0; q < 6; ++q) lists[q] = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)(n + 1));
+        uint32_t* src[3] = {xs, ys, zs};
+        for (int64_t v = 0; v < n; ++v)
+            for (int q = 0; q < 3; ++q)
+            {
+                const double d = dot(P(m, src[q][v]), axis) - sv;
+                if (d <= 0.0) lists[2 * q][cnt[2 * q]++] = src[q][v];
+                if (d >= 0.0) lists[2 * q + 1][cnt[2 * q + 1]++] = src[q][v];
+            }
+        const int64_t left = kd_build(m, height - 1, lists[0], lists[2], lists[4], cnt[0]);
+        m->kd[id].left = left;
+        const int64_t right = kd_build(m, height - 1, lists[1], lists[3], lists[5], cnt[1]);
+        m->kd[id].right = right;
+        for (int q = 0; q < 6; ++q) free(lists[q]);
+    }
+    else
+    {
+        v3 mean = V(0, 0, 0);
+        for (int64_t v = 0; v < n; ++v) mean = add(mean, P(m, xs[v]));
+        const double dn = (double)n;
+        mean = V(mean.x / dn, mean.y / dn, mean.z / dn);
+        m->kd[id].metric = local_metric(m, mean, m->vcache[xs[0]]);
+    }
+    return id;
+}
+
+/* KdTreeSampler::updateAnalyticalMetric (KdTreeSampler.cpp:116-180) */
+static void build_kdtree(om_mesh* m)
+{
+    m->nkd = 0;
+    int height = m->depth;
+    if (height < 0) height = (int)log2(ceil((double)m->nv / 3.0));
+    uint32_t* s[3];
+    for (int a = 0; a < 3; ++a)
+    {
+        s[a] = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)(m->nv + 1));
+        om_argsort_axis(m->pos, m->nv, a, s[a]);
+    }
+    kd_build(m, height, s[0], s[1], s[2], m->nv);
+    for (int a = 0; a < 3; ++a) free(s[a]);
+}
+
+/* KdTreeSampler::metricAt (KdTreeSampler.cpp:218-247) */
+static m3 kd_metric(const om_mesh* m, v3 p)
+{
+    int64_t node = -1, child = 0;
+    while (child != -1)
+    {
+        node = child;
+        const struct om_kd* k = m->kd + node;
+        child = dot(p, V(k->sep[0], k->sep[1], k->sep[2])) - k->sep[3] < 0.0 ? k->left : k->right;
+    }
+    return m->kd[node].metric;
+}
+
+/* TextureSampler::cellId (TextureSampler.cpp:513-524) */
+static void tex_cell(const om_mesh* m, const double* pos, int* id)
+{
+    for (int k = 0; k < 3; ++k)
+    {
+        const double r = (pos[k] - m->tex_min[k]) / m->tex_ext[k];
+        int c = (int)(r * (double)m->tex_size[k]);
+        id[k] = c < 0 ? 0 : c > m->tex_size[k] - 1 ? m->tex_size[k] - 1 : c;
+    }
+}
+
+static size_t tex_index(const om_mesh* m, int i, int j, int k)
+{
+    return ((size_t)k * m->tex_size[1] + j) * m->tex_size[0] + i;
+}
+
+/* TextureSampler::buildGrid (TextureSampler.cpp:275-448): a grid of about
+ * one cell per vertex over the bounding box; each background tet, in order,
+ * fills the unset cells of its cell box grown by one with the local metric
+ * at the cell centres, its walk started at that tet.  Cells no tet box
+ * reaches keep the default metric (identity). */
+static void build_texture(om_mesh* m)
+{
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t v = 0; v < m->nv; ++v)
+        for (int k = 0; k < 3; ++k)
+        {
+            const double x = m->pos[3 * v + k];
+            lo[k] = x < lo[k] ? x : lo[k];
+            hi[k] = x > hi[k] ? x : hi[k];
+        }
+    for (int k = 0; k < 3; ++k)
+    {
+        m->tex_min[k] = lo[k];
+        m->tex_ext[k] = hi[k] - lo[k];
+    }
+    double cells = (double)m->nv;
+    if (m->depth > 0) cells = (double)((size_t)m->depth * m->depth * m->depth);
+    const double alpha = pow(cells / (m->tex_ext[0] * m->tex_ext[1] * m->tex_ext[2]), 1 / 3.0);
+    for (int k = 0; k < 3; ++k)
+    {
+        const double e = alpha * m->tex_ext[k];
+        m->tex_size[k] = (int)round(e > 1.0 ? e : 1.0);
+    }
+    const size_t n = (size_t)m->tex_size[0] * m->tex_size[1] * m->tex_size[2];
+    free(m->tex);
+    m->tex = (m3*)malloc(sizeof(m3) * n);
+    unsigned char* set = (unsigned char*)calloc(n, 1);
+    for (size_t c = 0; c < n; ++c) m->tex[c] = mdiag(1, 1, 1);
+    double cs[3];
+    for (int k = 0; k < 3; ++k) cs[k] = m->tex_ext[k] / (double)m->tex_size[k];
+    for (int64_t e = 0; e < m->nbg; ++e)
+    {
+        double bmin[3] = {INFINITY, INFINITY, INFINITY}, bmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int v = 0; v < 4; ++v)
+            for (int k = 0; k < 3; ++k)
+            {
+                const double x = m->pos[3 * (size_t)m->bg[8 * e + v] + k];
+                bmin[k] = x < bmin[k] ? x : bmin[k];
+                bmax[k] = x > bmax[k] ? x : bmax[k];
+            }
+        int a[3], b[3];
+        tex_cell(m, bmin, a);
+        tex_cell(m, bmax, b);
+        for (int k = 0; k < 3; ++k)
+        {
+            a[k] = a[k] - 1 < 0 ? 0 : a[k] - 1;
+            b[k] = b[k] + 1 > m->tex_size[k] - 1 ? m->tex_size[k] - 1 : b[k] + 1;
+        }
+        for (int z = a[2]; z <= b[2]; ++z)
+            for (int y = a[1]; y <= b[1]; ++y)
+                for (int x = a[0]; x <= b[0]; ++x)
+                {
+                    const size_t c = tex_index(m, x, y, z);
+                    if (set[c]) continue;
+                    const v3 p = V(m->tex_min[0] + cs[0] * ((double)x + 0.5), m->tex_min[1] + cs[1] * ((double)y + 0.5),
+                                   m->tex_min[2] + cs[2] * ((double)z + 0.5));
+                    m->tex[c] = local_metric(m, p, (uint32_t)e);
+                    set[c] = 1;
+                }
+    }
+    free(set);
+}
+
+/* glm::mix of two metrics: a + (b - a) t, per entry */
+static m3 mmix(m3 a, m3 b, double t) { return madd(a, mscale(msub(b, a), t)); }
+
+/* TextureSampler::metricAt (TextureSampler.cpp:450-488): trilinear between
+ * the eight cell centres around the point, clamped at the grid's border */
+static m3 tex_metric(const om_mesh* m, v3 p)
+{
+    const double pc[3] = {p.x, p.y, p.z};
+    double cs[3], cp0[3], a[3];
+    int i0[3], i1[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        cs[k] = m->tex_ext[k] / (double)m->tex_size[k];
+        const double minb = m->tex_min[k], maxb = m->tex_min[k] + m->tex_ext[k] - cs[k] * 1.5;
+        const double q = pc[k] + (-cs[k]) / 2.0;
+        cp0[k] = q < minb ? minb : q > maxb ? maxb : q;
+    }
+    tex_cell(m, cp0, i0);
+    for (int k = 0; k < 3; ++k)
+    {
+        i1[k] = i0[k] + 1 < m->tex_size[k] - 1 ? i0[k] + 1 : m->tex_size[k] - 1;
+        const double c0 = cs[k] * ((double)i0[k] + 0.5);
+        const double t = (pc[k] - (m->tex_min[k] + c0)) / cs[k];
+        a[k] = t < 0.0 ? 0.0 : t > 1.0 ? 1.0 : t;
+    }
+    const m3 m000 = m->tex[tex_index(m, i0[0], i0[1], i0[2])], m100 = m->tex[tex_index(m, i1[0], i0[1], i0[2])];
+    const m3 m010 = m->tex[tex_index(m, i0[0], i1[1], i0[2])], m110 = m->tex[tex_index(m, i1[0], i1[1], i0[2])];
+    const m3 m001 = m->tex[tex_index(m, i0[0], i0[1], i1[2])], m101 = m->tex[tex_index(m, i1[0], i0[1], i1[2])];
+    const m3 m011 = m->tex[tex_index(m, i0[0], i1[1], i1[2])], m111 = m->tex[tex_index(m, i1[0], i1[1], i1[2])];
+    const m3 mx00 = mmix(m000, m100, a[0]), mx10 = mmix(m010, m110, a[0]);
+    const m3 mx01 = mmix(m001, m101, a[0]), mx11 = mmix(m011, m111, a[0]);
+    const m3 mxy0 = mmix(mx00, mx10, a[1]), mxy1 = mmix(mx01, mx11, a[1]);
+    return mmix(mxy0, mxy1, a[2]);
+}
+
+void om_set_discretization_depth(om_mesh* m, int32_t depth) { m->depth = depth; }
+
 void om_set_crew(om_mesh* m, int32_t sampler, int32_t measurer, int32_t evaluator,
                  double scaling, double aspect_ratio)
 {
@@ -601,7 +866,12 @@ void om_set_crew(om_mesh* m, int32_t sampler, int32_t measurer, int32_t evaluato
     m->rot = mrotate(id, 3.14159265358979323846 / 4.0, V(0, 0, 1));
     m->rot = mrotate(m->rot, 3.14159265358979323846 / 4.0, V(0, -1, 0));
     m->rotinv = mtranspose(m->rot);
-    if (sampler == OM_SAMPLER_LOCAL) build_background(m);
+    /* GpuMeshCharacter::updateSampling: updateAnalyticalMetric at crew set-up;
+     * the kd-tree and texture samplers sample a local sampler built the same
+     * way (KdTreeSampler.cpp:157-161, TextureSampler.cpp:257-267) */
+    if (sampler >= OM_SAMPLER_LOCAL) build_background(m);
+    if (sampler == OM_SAMPLER_KDTREE) build_kdtree(m);
+    if (sampler == OM_SAMPLER_TEXTURE) build_texture(m);
 }
 
 void om_get_pos(const om_mesh* m, double* out) { memcpy(out, m->pos, sizeof(double) * 3 * (size_t)m->nv); }
@@ -843,6 +1113,10 @@ static m3 metric_at(const om_mesh* m, v3 p)
         return analytic_metric(m, p);
     case OM_SAMPLER_LOCAL:
         return local_metric(m, p, tl_cache);
+    case OM_SAMPLER_KDTREE:
+        return kd_metric(m, p);
+    case OM_SAMPLER_TEXTURE:
+        return tex_metric(m, p);
     case OM_SAMPLER_SINE:
     {
         /* sine-graded anisotropic metric s^2 * diag(1 + 9 sin^2(4 pi x), 1, 1):

@@ -33,6 +33,8 @@ extern "C" {
 #define OM_SAMPLER_ANALYTIC 1
 #define OM_SAMPLER_SINE 2
 #define OM_SAMPLER_LOCAL 3 /* LocalSampler: the analytic metric on a background copy of the mesh */
+#define OM_SAMPLER_KDTREE 4 /* KdTreeSampler: the local metric sampled once per kd-tree leaf */
+#define OM_SAMPLER_TEXTURE 5 /* TextureSampler: the local metric sampled on a grid, trilinear */
 
 #define OM_MEASURER_METRIC_FREE 0
 #define OM_MEASURER_METRIC_WISE 1
@@ -71,6 +73,10 @@ void om_destroy(om_mesh* m);
  * id (plane: point, normal; segment: a, b; point: position). */
 void om_set_constraints(om_mesh* m, int32_t n, const int32_t* kind,
                         const double* params);
+/* AbstractSampler::setDiscretizationDepth (Samplers/AbstractSampler.cpp:61-64):
+ * the kd-tree height / texture resolution; -1 (the default) picks it from the
+ * vertex count.  Takes effect at the next om_set_crew. */
+void om_set_discretization_depth(om_mesh* m, int32_t depth);
 void om_set_crew(om_mesh* m, int32_t sampler, int32_t measurer,
                  int32_t evaluator, double scaling, double aspect_ratio);
 

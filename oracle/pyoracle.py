@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libgm_oracle.so")
 
-SAMPLER = {"uniform": 0, "analytic": 1, "sine": 2, "local": 3}
+SAMPLER = {"uniform": 0, "analytic": 1, "sine": 2, "local": 3, "kdtree": 4, "texture": 5}
 MEASURER = {"metric_free": 0, "metric_wise": 1}
 EVALUATOR = {"mean_ratio": 0, "metric_conformity": 1}
 SMOOTHER = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3, "spring_laplace": 4,
@@ -37,10 +37,16 @@ REFERENCE_PARAMS = {
 
 def build(force: bool = False) -> str:
     src = os.path.join(HERE, "gm_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    sort_src = os.path.join(HERE, "om_sort.cpp")
+    newest = max(os.path.getmtime(src), os.path.getmtime(sort_src), os.path.getmtime(os.path.join(HERE, "gm_oracle.h")))
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < newest:
         os.makedirs(BUILD_DIR, exist_ok=True)
-        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB_PATH,
-                               src, "-lm", "-lpthread"])
+        obj_c = os.path.join(BUILD_DIR, "gm_oracle.o")
+        obj_s = os.path.join(BUILD_DIR, "om_sort.o")
+        flags = ["-O2", "-ffp-contract=off", "-fPIC"]
+        subprocess.check_call(["gcc", *flags, "-c", src, "-o", obj_c])
+        subprocess.check_call(["g++", *flags, "-std=c++17", "-c", sort_src, "-o", obj_s])
+        subprocess.check_call(["g++", "-shared", "-o", LIB_PATH, obj_c, obj_s, "-lm", "-lpthread"])
     return LIB_PATH
 
 
@@ -58,6 +64,7 @@ def lib():
         L.om_destroy.argtypes = [vp]
         L.om_set_constraints.argtypes = [vp, i32, vp, vp]
         L.om_set_crew.argtypes = [vp, i32, i32, i32, dbl, dbl]
+        L.om_set_discretization_depth.argtypes = [vp, i32]
         L.om_get_pos.argtypes = [vp, vp]
         L.om_set_pos.argtypes = [vp, vp]
         L.om_element_quality.restype = dbl
@@ -88,7 +95,7 @@ class OracleMesh:
 
     def __init__(self, pos, tets, pris, hexs, cid, con_kind, con_param,
                  sampler="uniform", measurer="metric_free", evaluator="mean_ratio",
-                 scaling=1.0, aspect_ratio=1.0):
+                 scaling=1.0, aspect_ratio=1.0, depth=-1):
         L = lib()
         self._keep = [np.ascontiguousarray(pos, np.float64), np.ascontiguousarray(tets, np.uint32),
                       np.ascontiguousarray(pris, np.uint32), np.ascontiguousarray(hexs, np.uint32),
@@ -99,6 +106,7 @@ class OracleMesh:
         ck = np.ascontiguousarray(con_kind, np.int32)
         cp = np.ascontiguousarray(con_param, np.float64).reshape(-1, 6)
         L.om_set_constraints(self.h, ck.shape[0], _p(ck), _p(cp))
+        L.om_set_discretization_depth(self.h, int(depth))
         L.om_set_crew(self.h, SAMPLER[sampler], MEASURER[measurer], EVALUATOR[evaluator],
                       float(scaling), float(aspect_ratio))
 

@@ -16,7 +16,7 @@ import refbuild
 BOUNDARY = {"free": 0, "box": 1, "sphere": 2, "tet": 3, "pipe": 4, "shell": 5}
 SMOOTHER = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3, "spring_laplace": 4,
             "quality_laplace": 5}
-SAMPLER = {"uniform": 0, "analytic": 1, "sine": 2, "local": 3}
+SAMPLER = {"uniform": 0, "analytic": 1, "sine": 2, "local": 3, "kdtree": 4, "texture": 5}
 EVALUATOR = {"mean_ratio": 0, "metric_conformity": 1}
 
 _lib = None
@@ -49,7 +49,7 @@ def lib():
         L.ref_ngroups.argtypes = [vp]
         L.ref_get_groups.argtypes = [vp, vp, vp, vp]
         L.ref_get_tets.argtypes = [vp, vp]
-        L.ref_set_crew.argtypes = [vp, i32, i32, dbl, dbl]
+        L.ref_set_crew.argtypes = [vp, i32, i32, dbl, dbl, i32]
         L.ref_evaluate.argtypes = [vp, i32, vp]
         L.ref_element_quality.restype = dbl
         L.ref_element_quality.argtypes = [vp, i32, i64]
@@ -105,8 +105,9 @@ class RefMesh:
         lib().ref_get_groups(self.h, _p(base), _p(members), _p(ranges))
         return base, members[:base[-1]].copy(), ranges.reshape(-1, 6)
 
-    def set_crew(self, sampler="uniform", evaluator="mean_ratio", scaling=1.0, aspect_ratio=1.0):
-        lib().ref_set_crew(self.h, SAMPLER[sampler], EVALUATOR[evaluator], float(scaling), float(aspect_ratio))
+    def set_crew(self, sampler="uniform", evaluator="mean_ratio", scaling=1.0, aspect_ratio=1.0, depth=-1):
+        lib().ref_set_crew(self.h, SAMPLER[sampler], EVALUATOR[evaluator], float(scaling), float(aspect_ratio),
+                           int(depth))
 
     def evaluate(self, thread: bool = False) -> dict:
         out = np.zeros(23, np.float64)

@@ -34,7 +34,9 @@
 #include "Evaluators/MetricConformityEvaluator.h"
 #include "Measurers/AbstractMeasurer.h"
 #include "Samplers/AnalyticSampler.h"
+#include "Samplers/KdTreeSampler.h"
 #include "Samplers/LocalSampler.h"
+#include "Samplers/TextureSampler.h"
 #include "Samplers/UniformSampler.h"
 #include "Smoothers/ElementWise/GetmeSmoother.h"
 #include "Smoothers/ElementWise/VertexAccum.h"
@@ -197,19 +199,24 @@ void ref_get_tets(void* h, uint32_t* out)
         for (int k = 0; k < 4; ++k) out[4 * i + k] = r->mesh.tets[i].v[k];
 }
 
-// sampler: 0 uniform, 1 analytic, 2 sine, 3 local; evaluator: 0 mean ratio, 1 metric conformity
-void ref_set_crew(void* h, int sampler, int evaluator, double scaling, double aspect)
+// sampler: 0 uniform, 1 analytic, 2 sine, 3 local, 4 kd-tree, 5 texture;
+// evaluator: 0 mean ratio, 1 metric conformity; depth: the discretization
+// depth of the kd-tree and texture samplers (-1: from the vertex count)
+void ref_set_crew(void* h, int sampler, int evaluator, double scaling, double aspect, int depth)
 {
     Ref* r = static_cast<Ref*>(h);
     if (sampler == 1) r->sampler.reset(new AnalyticSampler());
     else if (sampler == 2) r->sampler.reset(new SineSampler());
     else if (sampler == 3) r->sampler.reset(new LocalSampler());
+    else if (sampler == 4) r->sampler.reset(new KdTreeSampler());
+    else if (sampler == 5) r->sampler.reset(new TextureSampler());
     else r->sampler.reset(new UniformSampler());
     r->sampler->setScaling(scaling);
     r->sampler->setAspectRatio(aspect);
-    // GpuMeshCharacter::updateSampling: the local sampler's background mesh
-    // and vertex metrics from the mesh as it is now
-    if (sampler == 3) r->sampler->updateAnalyticalMetric(r->mesh);
+    r->sampler->setDiscretizationDepth(depth);
+    // GpuMeshCharacter::updateSampling: the background mesh (and the kd-tree
+    // or texture sampled from it) from the mesh as it is now
+    if (sampler >= 3) r->sampler->updateAnalyticalMetric(r->mesh);
     if (evaluator == 1) r->evaluator.reset(new MetricConformityEvaluator());
     else r->evaluator.reset(new MeanRatioEvaluator());
     r->crew.setSampler(r->mesh, r->sampler);

@@ -249,6 +249,39 @@ template <class T> tmat4<T> rotate(const tmat4<T>& m, T angle, const tvec3<T>& v
     return r;
 }
 
+// ---- used by TextureSampler ----
+template <class T> bool operator==(const tmat3<T>& a, const tmat3<T>& b) { return a[0] == b[0] && a[1] == b[1] && a[2] == b[2]; }
+template <class T> bool operator!=(const tmat3<T>& a, const tmat3<T>& b) { return !(a == b); }
+// round half away from zero per component (std::round)
+template <class T> tvec3<T> round(const tvec3<T>& v) { return tvec3<T>(std::round(v.x), std::round(v.y), std::round(v.z)); }
+template <class T> tvec3<bool> lessThan(const tvec3<T>& a, const tvec3<T>& b) { return tvec3<bool>(a.x < b.x, a.y < b.y, a.z < b.z); }
+inline bool all(const tvec3<bool>& v) { return v.x && v.y && v.z; }
+template <class T> tmat4<T> operator*(const tmat4<T>& a, const tmat4<T>& b)
+{
+    tmat4<T> r;
+    for (int j = 0; j < 4; ++j)
+        for (int i = 0; i < 4; ++i)
+            r[j][i] = a[0][i] * b[j][0] + a[1][i] * b[j][1] + a[2][i] * b[j][2] + a[3][i] * b[j][3];
+    return r;
+}
+template <class T> tmat4<T>& operator*=(tmat4<T>& a, const tmat4<T>& b) { a = a * b; return a; }
+// gtc/matrix_transform: m * S(v), m * T(v)
+template <class T> tmat4<T> scale(const tmat4<T>& m, const tvec3<T>& v)
+{
+    tmat4<T> r;
+    r[0] = tvec4<T>(m[0].x * v.x, m[0].y * v.x, m[0].z * v.x, m[0].w * v.x);
+    r[1] = tvec4<T>(m[1].x * v.y, m[1].y * v.y, m[1].z * v.y, m[1].w * v.y);
+    r[2] = tvec4<T>(m[2].x * v.z, m[2].y * v.z, m[2].z * v.z, m[2].w * v.z);
+    r[3] = m[3];
+    return r;
+}
+template <class T> tmat4<T> translate(const tmat4<T>& m, const tvec3<T>& v)
+{
+    tmat4<T> r(m);
+    for (int i = 0; i < 4; ++i) r[3][i] = m[0][i] * v.x + m[1][i] * v.y + m[2][i] * v.z + m[3][i];
+    return r;
+}
+
 typedef tvec2<double> dvec2;
 typedef tvec3<double> dvec3;
 typedef tvec4<double> dvec4;

@@ -29,6 +29,14 @@ void updateCudaLocalTets(const std::vector<GpuLocalTet>&) { cuda_driver_called("
 void updateCudaLocalCache(const std::vector<GLuint>&) { cuda_driver_called("updateCudaLocalCache"); }
 void updateCudaRefVerts(const std::vector<GpuVert>&) { cuda_driver_called("updateCudaRefVerts"); }
 void updateCudaRefMetrics(const std::vector<GpuMetric>&) { cuda_driver_called("updateCudaRefMetrics"); }
+void installCudaKdTreeSampler() { cuda_driver_called("installCudaKdTreeSampler"); }
+void updateCudaKdNodes(const std::vector<GpuKdNode>&) { cuda_driver_called("updateCudaKdNodes"); }
+void installCudaTextureSampler() { cuda_driver_called("installCudaTextureSampler"); }
+void updateCudaSamplerTextures(const std::vector<glm::vec4>&, const std::vector<glm::vec4>&, const glm::mat4&,
+                               const glm::ivec3)
+{
+    cuda_driver_called("updateCudaSamplerTextures");
+}
 void installCudaGetmeSmoother() { cuda_driver_called("installCudaGetmeSmoother"); }
 void installCudaNelderMeadSmoother(float, int, float, float, float, float, float)
 {

@@ -27,7 +27,8 @@ SOURCES = [
     "Evaluators/AbstractEvaluator.cpp", "Evaluators/MeanRatioEvaluator.cpp", "Evaluators/MetricConformityEvaluator.cpp",
     "Measurers/AbstractMeasurer.cpp", "Measurers/MetricFreeMeasurer.cpp", "Measurers/MetricWiseMeasurer.cpp",
     "Samplers/AbstractSampler.cpp", "Samplers/AnalyticSampler.cpp", "Samplers/UniformSampler.cpp",
-    "Samplers/LocalSampler.cpp", "DataStructures/TriSet.cpp",
+    "Samplers/LocalSampler.cpp", "DataStructures/TriSet.cpp", "Samplers/KdTreeSampler.cpp",
+    "Samplers/TextureSampler.cpp",
     "Boundaries/AbstractBoundary.cpp", "Boundaries/BoxBoundary.cpp", "Boundaries/SphereBoundary.cpp",
     "Boundaries/TetBoundary.cpp", "Boundaries/PipeBoundary.cpp", "Boundaries/ShellBoundary.cpp",
     "Boundaries/BoundaryFree.cpp", "Boundaries/Constraints/AbstractConstraint.cpp",

@@ -28,6 +28,14 @@ CASES = {
                     dict(sampler="uniform", evaluator="mean_ratio")),
     "sphere_mc_8": (lambda: meshgen.sphere_mesh(8, 0.25, 1), "sphere",
                     dict(sampler="sine", evaluator="metric_conformity", scaling=4.0)),
+    # the background-mesh samplers: local (walk + barycentric), kd-tree
+    # (leaf samples), texture (grid samples, trilinear)
+    "mixed_local_4": (lambda: meshgen.box_mesh(4, "mixed", 0.15, 21, gaussian=True), "box",
+                      dict(sampler="local", evaluator="metric_conformity", scaling=2.0, aspect_ratio=3.0)),
+    "mixed_kdtree_4": (lambda: meshgen.box_mesh(4, "mixed", 0.15, 22, gaussian=True), "box",
+                       dict(sampler="kdtree", evaluator="metric_conformity", scaling=2.0, aspect_ratio=3.0)),
+    "mixed_texture_4": (lambda: meshgen.box_mesh(4, "mixed", 0.15, 23, gaussian=True), "box",
+                        dict(sampler="texture", evaluator="metric_conformity", scaling=2.0, aspect_ratio=3.0)),
 }
 SMOOTHERS = ["nelder_mead", "gradient_descent", "spawn_search", "getme", "spring_laplace", "quality_laplace"]
 
@@ -37,10 +45,13 @@ def make(name):
     raw = build()
     out = dict(pos=raw.pos, tets=raw.tets, pris=raw.pris, hexs=raw.hexs, cid=raw.cid, con_kind=raw.con_kind,
                con_param=raw.con_param, boundary=boundary, sampler=crew["sampler"], evaluator=crew["evaluator"],
-               scaling=crew.get("scaling", 1.0))
+               scaling=crew.get("scaling", 1.0), aspect_ratio=crew.get("aspect_ratio", 1.0),
+               depth=crew.get("depth", -1))
     ref = pyref.RefMesh(raw, boundary)
-    ref.set_crew(**crew)
+    # the harness reads the permutation from the vertex cache words, which
+    # the background-mesh samplers overwrite with their walk caches
     out["perm"] = ref.perm()
+    ref.set_crew(**crew)
     base, members, ranges = ref.groups()
     out.update(group_base=base, members=members, ranges=ranges)
     e = ref.evaluate()
@@ -63,7 +74,7 @@ def make_json():
 
 
 if __name__ == "__main__":
-    for n in CASES:
+    for n in (sys.argv[1:] or CASES):
         make(n)
         print("wrote", n)
     make_json()

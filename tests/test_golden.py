@@ -30,7 +30,9 @@ def oracle(d, raw):
     sampler = str(d["sampler"])
     measurer = "metric_free" if sampler == "uniform" else "metric_wise"
     return pr, pyoracle.OracleMesh.from_raw(pr, sampler=sampler, measurer=measurer, evaluator=str(d["evaluator"]),
-                                            scaling=float(d["scaling"]))
+                                            scaling=float(d["scaling"]),
+                                            aspect_ratio=float(d.get("aspect_ratio", 1.0)),
+                                            depth=int(d.get("depth", -1)))
 
 
 def test_fixtures_exist():

@@ -37,6 +37,23 @@ LOCAL_CASES = {
                      dict(sampler="local", evaluator="metric_conformity", scaling=2.0, aspect_ratio=3.0)),
     "mixed_local_mr": (lambda: meshgen.box_mesh(4, "mixed", 0.1, 7), "box",
                        dict(sampler="local", evaluator="mean_ratio", scaling=2.0, aspect_ratio=3.0)),
+    # KdTreeSampler: one local-metric sample per kd-tree leaf (piecewise
+    # constant); TextureSampler: local-metric samples at grid cell centres,
+    # trilinear in between
+    "mixed_kdtree_mc": (lambda: meshgen.box_mesh(4, "mixed", 0.15, 8, gaussian=True), "box",
+                        dict(sampler="kdtree", evaluator="metric_conformity", scaling=2.0, aspect_ratio=3.0)),
+    "tet_kdtree_mr": (lambda: meshgen.box_mesh(5, "tet", 0.25, 9), "box",
+                      dict(sampler="kdtree", evaluator="mean_ratio", scaling=3.0, aspect_ratio=2.0)),
+    "mixed_texture_mc": (lambda: meshgen.box_mesh(4, "mixed", 0.15, 10, gaussian=True), "box",
+                         dict(sampler="texture", evaluator="metric_conformity", scaling=2.0, aspect_ratio=3.0)),
+    "hex_texture_mr": (lambda: meshgen.box_mesh(4, "hex", 0.1, 11), "box",
+                       dict(sampler="texture", evaluator="mean_ratio", scaling=3.0, aspect_ratio=2.0)),
+    "tet_texture_depth": (lambda: meshgen.box_mesh(4, "tet", 0.2, 12), "box",
+                          dict(sampler="texture", evaluator="metric_conformity", scaling=2.0, aspect_ratio=3.0,
+                               depth=3)),
+    "mixed_kdtree_depth": (lambda: meshgen.box_mesh(4, "mixed", 0.1, 13), "box",
+                           dict(sampler="kdtree", evaluator="metric_conformity", scaling=2.0, aspect_ratio=3.0,
+                                depth=2)),
 }
 
 
@@ -49,7 +66,8 @@ def setup(case):
     pr = M.permute_mesh(raw, perm)
     measurer = "metric_wise" if crew["sampler"] != "uniform" else "metric_free"
     orc = pyoracle.OracleMesh.from_raw(pr, sampler=crew["sampler"], measurer=measurer, evaluator=crew["evaluator"],
-                                       scaling=crew.get("scaling", 1.0), aspect_ratio=crew.get("aspect_ratio", 1.0))
+                                       scaling=crew.get("scaling", 1.0), aspect_ratio=crew.get("aspect_ratio", 1.0),
+                                       depth=crew.get("depth", -1))
     return raw, ref, perm, groups, pr, orc
 
 
@@ -144,7 +162,7 @@ def test_local_sampler_smoothing_matches_reference(case, smoother):
     assert np.array_equal(ref.pos, orc.pos)
 
 
-@pytest.mark.parametrize("case", ["mixed_local_mr"])
+@pytest.mark.parametrize("case", ["mixed_local_mr", "mixed_kdtree_mc", "mixed_texture_mc"])
 def test_local_sampler_getme_matches_reference(case):
     raw, ref, perm, groups, pr, orc = setup(case)
     ref.smooth("getme", 1)
