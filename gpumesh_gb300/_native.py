@@ -17,7 +17,7 @@ GM_OK = 0
 STATUS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupported",
           5: "timeout", 6: "invalid state"}
 
-SAMPLERS = {"uniform": 0, "analytic": 1, "sine": 2, "local": 3}
+SAMPLERS = {"uniform": 0, "analytic": 1, "sine": 2, "local": 3, "kdtree": 4, "texture": 5}
 MEASURERS = {"metric_free": 0, "metric_wise": 1}
 EVALUATORS = {"mean_ratio": 0, "metric_conformity": 1}
 SMOOTHERS = {"nelder_mead": 0, "gradient_descent": 1, "spawn_search": 2, "getme": 3, "spring_laplace": 4,
@@ -87,6 +87,9 @@ def lib():
         "gm_mesh_clone": [vp, vp],
         "gm_mesh_build_local_background": [vp],
         "gm_mesh_set_local_background": [vp, u32, vp, u32, vp, vp],
+        "gm_mesh_set_discretization_depth": [vp, i32],
+        "gm_mesh_set_kd_nodes": [vp, u32, vp, vp, vp],
+        "gm_mesh_set_texture": [vp, vp, vp, vp, vp],
         "gm_mesh_device_bytes": [vp, ctypes.POINTER(u64)],
         "gm_mesh_restore_positions": [vp],
         "gm_probe_fp32_tflops": [ctypes.POINTER(ctypes.c_double)],

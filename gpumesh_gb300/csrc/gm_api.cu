@@ -26,7 +26,7 @@ namespace {
 
 void set_crew(gm_mesh* m, int sampler, int measurer, int evaluator, double scaling, double aspect)
 {
-    require(sampler >= 0 && sampler <= GM_SAMPLER_LOCAL, "unknown sampler");
+    require(sampler >= 0 && sampler <= GM_SAMPLER_TEXTURE, "unknown sampler");
     require(measurer >= 0 && measurer <= 1, "unknown measurer");
     require(evaluator >= 0 && evaluator <= 1, "unknown evaluator");
     Crew c = m->crew;
@@ -64,30 +64,9 @@ void set_crew(gm_mesh* m, int sampler, int measurer, int evaluator, double scali
     rot(A, pi / 4.0, 0, -1, 0, c.rot);
     for (int j = 0; j < 3; ++j)
         for (int r = 0; r < 3; ++r) c.rotinv[j * 3 + r] = c.rot[r * 3 + j];
-    c.local = nullptr;
-    if (sampler == GM_SAMPLER_LOCAL)
-    {
-        // GpuMeshCharacter::updateSampling rebuilds the background when the
-        // scaling or the aspect ratio changes (GpuMeshCharacter.cpp:1115-1129)
-        const auto& L = m->local;
-        if (!L || (L->from_mesh && (L->scaling != scaling || L->aspect != aspect)))
-            m->local = local_background_from_mesh(m, c);
-        c.local = m->local->field.p;
-    }
+    // the background mesh, kd-tree or texture the sampler samples
+    prepare_sampler(m, c);
     m->crew = c;  // only once everything above succeeded
-}
-
-// a new topology: the local sampler's background follows it while the local
-// sampler is installed, and is dropped otherwise (rebuilt when installed)
-void topology_changed(gm_mesh* m)
-{
-    if (m->crew.sampler == GM_SAMPLER_LOCAL)
-    {
-        m->local = local_background_from_mesh(m, m->crew);
-        m->crew.local = m->local->field.p;
-    }
-    else
-        m->local.reset();
 }
 
 void update_patch_shape(gm_mesh* m, const uint32_t* ve_off_host)
@@ -526,7 +505,7 @@ gm_status gm_mesh_upload(gm_mesh* m, uint32_t nv, const double* xyz, const int32
         upload(m->hexs, reinterpret_cast<const uint4*>(hexs), (size_t)nh * 2, m->stream);
         upload_csr(m, ve_off, ve, vv_off, vv);
         GM_CUDA(cudaStreamSynchronize(m->stream));
-        topology_changed(m);
+        sampler_topology_changed(m);
     });
 }
 
@@ -697,10 +676,26 @@ gm_status gm_mesh_build_local_background(gm_mesh* m)
     return guarded([&] {
         require(m != nullptr, "null mesh");
         drop_job(m);
-        m->local = local_background_from_mesh(m, m->crew);
-        if (m->crew.sampler == GM_SAMPLER_LOCAL) m->crew.local = m->local->field.p;
+        // LocalSampler / KdTreeSampler / TextureSampler::updateAnalyticalMetric:
+        // everything sampled again from the mesh as it is now
+        auto bg = local_background_from_mesh(m, m->crew);
+        m->local = bg;
+        if (m->kd && !m->kd->given) m->kd.reset();
+        if (m->tex && !m->tex->given) m->tex.reset();
+        Crew c = m->crew;
+        prepare_sampler(m, c);
+        m->crew = c;
     });
 }
+
+namespace {
+// a part handed over by the caller: installed, and the field re-assembled
+// while a background-mesh sampler is installed
+void refresh_crew(gm_mesh* m)
+{
+    if (m->crew.sampler >= GM_SAMPLER_LOCAL) m->crew.local = assemble_field(m);
+}
+}  // namespace
 
 gm_status gm_mesh_set_local_background(gm_mesh* m, uint32_t ntets, const uint32_t* tets8, uint32_t nverts,
                                        const double* xyz, const double* metrics6)
@@ -709,7 +704,55 @@ gm_status gm_mesh_set_local_background(gm_mesh* m, uint32_t ntets, const uint32_
         require(m != nullptr, "null mesh");
         drop_job(m);
         m->local = local_background_given(m, ntets, tets8, nverts, xyz, metrics6);
-        if (m->crew.sampler == GM_SAMPLER_LOCAL) m->crew.local = m->local->field.p;
+        refresh_crew(m);
+    });
+}
+
+gm_status gm_mesh_set_kd_nodes(gm_mesh* m, uint32_t n, const int32_t* children2, const double* separators4,
+                               const double* metrics6)
+{
+    return guarded([&] {
+        require(m != nullptr, "null mesh");
+        drop_job(m);
+        m->kd = kdtree_given(m, n, children2, separators4, metrics6);
+        refresh_crew(m);
+    });
+}
+
+gm_status gm_mesh_set_texture(gm_mesh* m, const int32_t* dims3, const double* min3, const double* extents3,
+                              const double* metrics6)
+{
+    return guarded([&] {
+        require(m != nullptr, "null mesh");
+        drop_job(m);
+        m->tex = texture_given(m, dims3, min3, extents3, metrics6);
+        refresh_crew(m);
+    });
+}
+
+gm_status gm_mesh_set_discretization_depth(gm_mesh* m, int32_t depth)
+{
+    return guarded([&] {
+        require(m != nullptr, "null mesh");
+        require(depth < 4096, "discretization depth out of range");
+        const int old = m->depth;
+        if ((depth < 0 ? -1 : depth) == old) return;
+        drop_job(m);
+        m->depth = depth < 0 ? -1 : depth;
+        if (m->crew.sampler == GM_SAMPLER_KDTREE || m->crew.sampler == GM_SAMPLER_TEXTURE)
+        {
+            Crew c = m->crew;
+            try
+            {
+                prepare_sampler(m, c);
+            }
+            catch (...)
+            {
+                m->depth = old;
+                throw;
+            }
+            m->crew = c;
+        }
     });
 }
 
@@ -747,7 +790,11 @@ gm_status gm_mesh_clone(gm_mesh* dst, const gm_mesh* src)
         dst->n_members = src->n_members;
         dst->group_base = src->group_base;
         dst->crew = src->crew;
-        dst->local = src->local;  // shared, so dst->crew.local stays valid
+        dst->local = src->local;  // shared parts; dst assembles its own field
+        dst->kd = src->kd;
+        dst->tex = src->tex;
+        dst->depth = src->depth;
+        if (dst->crew.sampler >= GM_SAMPLER_LOCAL) dst->crew.local = assemble_field(dst);
         dst->ks = src->ks;
         dst->maxe = src->maxe;
         dst->warps_per_block = src->warps_per_block;
@@ -765,7 +812,7 @@ gm_status gm_mesh_device_bytes(const gm_mesh* m, uint64_t* bytes)
         b += m->con.cap * sizeof(Constraint) + m->parts.cap * sizeof(EvalPartial) + m->corners.cap * sizeof(float4);
         b += m->saved.cap * sizeof(float4) + m->def_v.cap * 4 + (m->def_old.cap + m->def_new.cap) * sizeof(float4);
         b += m->quality.cap * sizeof(Quality);
-        if (m->local) b += m->local->bytes();
+        b += sampler_bytes(m);
         *bytes = b;
     });
 }

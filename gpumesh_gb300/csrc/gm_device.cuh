@@ -25,7 +25,10 @@ constexpr int kTet = 0;
 constexpr int kPri = 2;
 constexpr int kHex = 3;
 
-enum : int { kSamplerUniform = 0, kSamplerAnalytic = 1, kSamplerSine = 2, kSamplerLocal = 3 };
+enum : int { kSamplerUniform = 0, kSamplerAnalytic = 1, kSamplerSine = 2, kSamplerLocal = 3, kSamplerKdTree = 4,
+              kSamplerTexture = 5 };
+// bound of a kd-tree descent (trees are built at most this deep)
+constexpr int kKdMaxDepth = 64;
 enum : int { kMeasurerMetricFree = 0, kMeasurerMetricWise = 1 };
 enum : int { kEvalMeanRatio = 0, kEvalMetricConformity = 1 };
 enum : int
@@ -58,6 +61,19 @@ struct LocalField
     uint32_t nt, np, ne;     // tets, prisms and elements the caches were built for
     int g[3];
     double lo[3], inv_h[3];
+    // KdTreeSampler: nodes in pre-order; children (-1: none), separator plane
+    // (normal xyz, offset w), per node the leaf metric xx yy zz xy xz yz
+    const int2* kd_child;
+    const float4* kd_sepf;
+    const double4* kd_sepd;
+    const float* kd_mf;
+    const double* kd_md;
+    // TextureSampler: metric samples at the cell centres of a tg[0] x tg[1] x
+    // tg[2] grid over [tmin, tmin + text], x fastest
+    int tg[3];
+    double tmin[3], text[3];
+    const float* tex_mf;
+    const double* tex_md;
 };
 
 // the element a metric is sampled for, as a walk start hint:
@@ -71,7 +87,7 @@ struct Crew
     int sampler, measurer, evaluator, pad;
     double scaling, scaling2, scaling3, aspect;
     double rot[9], rotinv[9];  // column-major, AbstractSampler::_rotMat / _rotInv
-    const LocalField* local;   // kSamplerLocal only
+    const LocalField* local;   // kSamplerLocal, kSamplerKdTree, kSamplerTexture
 };
 
 // one boundary constraint (index = constraint id)
@@ -313,23 +329,10 @@ __device__ __forceinline__ uint32_t local_start_elem(const LocalField& L, uint32
     return e < L.ne ? __ldg(&L.ecache[e]) : kNoHint;  // a mesh since re-uploaded: no cache
 }
 
+// the walk from background tet t to the tet holding p, then the interpolation
 template <class R>
-__device__ __noinline__ Sym3<R> local_metric(const LocalField& L, V3<R> p, uint32_t hint)
+__device__ __forceinline__ Sym3<R> local_walk(const LocalField& L, V3<R> p, uint32_t t)
 {
-    uint32_t t = local_start_elem(L, hint);
-    if (t == kNoHint)
-    {
-        int ci[3];
-        const R pc[3] = {p.x, p.y, p.z};
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-        {
-            const R f = (pc[k] - (R)L.lo[k]) * (R)L.inv_h[k];
-            int i = f > R(0) ? (int)f : 0;
-            ci[k] = i < L.g[k] ? i : L.g[k] - 1;
-        }
-        t = L.cell[((size_t)ci[2] * L.g[1] + ci[1]) * L.g[0] + ci[0]];
-    }
     uint4 tv = __ldg(&L.tv[t]);
     V3<R> vp[4] = {local_pos<R>(L, tv.x), local_pos<R>(L, tv.y), local_pos<R>(L, tv.z), local_pos<R>(L, tv.w)};
     R coor[4];
@@ -417,6 +420,125 @@ __device__ __noinline__ Sym3<R> local_metric(const LocalField& L, V3<R> p, uint3
 }
 
 template <class R>
+__device__ __noinline__ Sym3<R> local_metric(const LocalField& L, V3<R> p, uint32_t hint)
+{
+    uint32_t t = local_start_elem(L, hint);
+    if (t == kNoHint)
+    {
+        int ci[3];
+        const R pc[3] = {p.x, p.y, p.z};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            const R f = (pc[k] - (R)L.lo[k]) * (R)L.inv_h[k];
+            int i = f > R(0) ? (int)f : 0;
+            ci[k] = i < L.g[k] ? i : L.g[k] - 1;
+        }
+        t = L.cell[((size_t)ci[2] * L.g[1] + ci[1]) * L.g[0] + ci[0]];
+    }
+    return local_walk(L, p, t);
+}
+
+// KdTreeSampler::metricAt (Samplers/KdTreeSampler.cpp:218-247; the CUDA
+// driver resources/cuda/Sampling/KdTree.cu:24-45): descend to the leaf on the
+// side of each node's separator plane, return the leaf's metric
+template <class R>
+__device__ __noinline__ Sym3<R> kd_metric(const LocalField& L, V3<R> p)
+{
+    int node = 0;
+    for (int depth = 0; depth < kKdMaxDepth; ++depth)
+    {
+        const int2 ch = __ldg(&L.kd_child[node]);
+        if (ch.x < 0 && ch.y < 0) break;
+        R d;
+        if constexpr (sizeof(R) == 8)
+        {
+            const double4 s = L.kd_sepd[node];
+            d = p.x * s.x + p.y * s.y + p.z * s.z - s.w;
+        }
+        else
+        {
+            const float4 s = __ldg(&L.kd_sepf[node]);
+            d = p.x * s.x + p.y * s.y + p.z * s.z - s.w;
+        }
+        const int next = d < R(0) ? ch.x : ch.y;
+        if (next < 0) break;
+        node = next;
+    }
+    R m[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j)
+    {
+        if constexpr (sizeof(R) == 8) m[j] = (R)L.kd_md[6 * (size_t)node + j];
+        else m[j] = (R)__ldg(&L.kd_mf[6 * (size_t)node + j]);
+    }
+    return Sym3<R>{m[0], m[1], m[2], m[3], m[4], m[5]};
+}
+
+// TextureSampler::metricAt (Samplers/TextureSampler.cpp:450-488): trilinear
+// interpolation between the eight cell centres around p, clamped at the
+// grid's border; glm::mix(a, b, t) = a + (b - a) t per entry
+template <class R>
+__device__ __forceinline__ void tex_cell_metric(const LocalField& L, int i, int j, int k, R* m)
+{
+    const size_t c = ((size_t)k * L.tg[1] + j) * L.tg[0] + i;
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+    {
+        if constexpr (sizeof(R) == 8) m[q] = (R)L.tex_md[6 * c + q];
+        else m[q] = (R)__ldg(&L.tex_mf[6 * c + q]);
+    }
+}
+
+template <class R>
+__device__ __noinline__ Sym3<R> tex_metric(const LocalField& L, V3<R> p)
+{
+    const R pc[3] = {p.x, p.y, p.z};
+    int i0[3], i1[3];
+    R a[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        const R ext = (R)L.text[k], mn = (R)L.tmin[k];
+        const int n = L.tg[k];
+        const R cs = ext / (R)n;
+        const R minb = mn, maxb = mn + ext - cs * R(1.5);
+        const R q = pc[k] + (-cs) / R(2);
+        const R t1 = q < minb ? minb : q;     // glm::max(q, minb)
+        const R cp0 = maxb < t1 ? maxb : t1;  // glm::min(., maxb)
+        // cellId: truncation, then clamped to the grid; cp0 is clamped above,
+        // so |r| <= n + 1 (a NaN converts to 0)
+        const R r = (cp0 - mn) / ext * (R)n;
+        int c = (int)r;
+        c = c < 0 ? 0 : (c > n - 1 ? n - 1 : c);
+        i0[k] = c;
+        i1[k] = c + 1 < n - 1 ? c + 1 : n - 1;
+        const R c0 = cs * ((R)c + R(0.5));
+        const R f = (pc[k] - (mn + c0)) / cs;
+        a[k] = f < R(0) ? R(0) : (f > R(1) ? R(1) : f);
+    }
+    R m000[6], m100[6], m010[6], m110[6], m001[6], m101[6], m011[6], m111[6];
+    tex_cell_metric(L, i0[0], i0[1], i0[2], m000);
+    tex_cell_metric(L, i1[0], i0[1], i0[2], m100);
+    tex_cell_metric(L, i0[0], i1[1], i0[2], m010);
+    tex_cell_metric(L, i1[0], i1[1], i0[2], m110);
+    tex_cell_metric(L, i0[0], i0[1], i1[2], m001);
+    tex_cell_metric(L, i1[0], i0[1], i1[2], m101);
+    tex_cell_metric(L, i0[0], i1[1], i1[2], m011);
+    tex_cell_metric(L, i1[0], i1[1], i1[2], m111);
+    R r[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+    {
+        const R x00 = m000[q] + (m100[q] - m000[q]) * a[0], x10 = m010[q] + (m110[q] - m010[q]) * a[0];
+        const R x01 = m001[q] + (m101[q] - m001[q]) * a[0], x11 = m011[q] + (m111[q] - m011[q]) * a[0];
+        const R y0 = x00 + (x10 - x00) * a[1], y1 = x01 + (x11 - x01) * a[1];
+        r[q] = y0 + (y1 - y0) * a[2];
+    }
+    return Sym3<R>{r[0], r[1], r[2], r[3], r[4], r[5]};
+}
+
+template <class R>
 __device__ __forceinline__ Sym3<R> metric_at(const Crew& c, V3<R> p, uint32_t hint = kNoHint)
 {
     if (c.sampler == kSamplerSine)
@@ -428,6 +550,8 @@ __device__ __forceinline__ Sym3<R> metric_at(const Crew& c, V3<R> p, uint32_t hi
     }
     if (c.sampler == kSamplerAnalytic) return analytic_metric(c, p);
     if (c.sampler == kSamplerLocal) return local_metric(*c.local, p, hint);
+    if (c.sampler == kSamplerKdTree) return kd_metric(*c.local, p);
+    if (c.sampler == kSamplerTexture) return tex_metric(*c.local, p);
     R s2 = (R)c.scaling2;
     return {s2, s2, s2, R(0), R(0), R(0)};
 }

@@ -120,8 +120,10 @@ void upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s)
 // the smoother parameter block of the C ABI (GM_PARAMS doubles), with defaults
 SmoothParams parse_smooth_params(int smoother, const double* params);
 
-// LocalSampler's background mesh in device memory, with the LocalField that
-// points into it (the crew's `local`); shared by a mesh and its clones
+// LocalSampler's background mesh in device memory.  `part` holds the local
+// members of a LocalField pointing into the buffers, `field` a device copy of
+// it alone (the walks of the kd-tree and texture builds); host copies of the
+// positions and tets serve those builds.  Shared by a mesh and its clones.
 struct LocalBackground
 {
     DBuf<uint4> tv, tn;
@@ -130,16 +132,47 @@ struct LocalBackground
     DBuf<float> mf;
     DBuf<uint32_t> cell, ecache;
     DBuf<LocalField> field;
+    LocalField part{};
+    std::vector<double> pd_h;
+    std::vector<uint4> tv_h;
     uint32_t nbg = 0, nref = 0;
     bool from_mesh = false;  // built from the mesh (analytic vertex metrics) rather than given
     double scaling = 0.0, aspect = 0.0;
     size_t bytes() const
     {
-        return tv.cap * 32 + pf.cap * 16 + pd.cap * 8 + md.cap * 8 + mf.cap * 4 + (cell.cap + ecache.cap) * 4 +
-               sizeof(LocalField);
+        return (tv.cap + tn.cap) * 16 + pf.cap * 16 + pd.cap * 8 + md.cap * 8 + mf.cap * 4 +
+               (cell.cap + ecache.cap) * 4 + sizeof(LocalField);
     }
 };
 
+// KdTreeSampler's nodes (pre-order) and TextureSampler's grid in device
+// memory; `given` when handed over by the caller rather than built from the
+// mesh (then kept across scaling changes and topology uploads)
+struct KdTreeData
+{
+    DBuf<int2> child;
+    DBuf<float4> sepf;
+    DBuf<double4> sepd;
+    DBuf<float> mf;
+    DBuf<double> md;
+    uint32_t n = 0;
+    bool given = false;
+    int depth = -1;
+    double scaling = 0.0, aspect = 0.0;
+    size_t bytes() const { return child.cap * 8 + sepf.cap * 16 + sepd.cap * 32 + mf.cap * 4 + md.cap * 8; }
+};
+
+struct TextureData
+{
+    DBuf<float> mf;
+    DBuf<double> md;
+    int g[3] = {0, 0, 0};
+    double lo[3] = {0, 0, 0}, ext[3] = {0, 0, 0};
+    bool given = false;
+    int depth = -1;
+    double scaling = 0.0, aspect = 0.0;
+    size_t bytes() const { return mf.cap * 4 + md.cap * 8; }
+};
 
 }  // namespace gm
 
@@ -185,8 +218,13 @@ struct gm_mesh
     DBuf<int> job_counter;    // passes done
     DBuf<Quality> job_fresh;  // evaluation of the pass just run
     uint32_t job_max_passes = 0;
-    // LocalSampler background (crew.local points into it)
+    // background-mesh samplers: the parts, and the LocalField assembled from
+    // them that crew.local points to
     std::shared_ptr<LocalBackground> local;
+    std::shared_ptr<KdTreeData> kd;
+    std::shared_ptr<TextureData> tex;
+    DBuf<LocalField> field;
+    int depth = -1;  // AbstractSampler::discretizationDepth
 
     MeshView view() const
     {
@@ -213,7 +251,7 @@ struct gm_mesh
     int variant() const
     {
         if (crew.evaluator == GM_EVALUATOR_METRIC_CONFORMITY)  // general metric, or a diagonal one
-            return (crew.sampler == GM_SAMPLER_ANALYTIC || crew.sampler == GM_SAMPLER_LOCAL) ? kVarMC : kVarMCDiag;
+            return (crew.sampler == GM_SAMPLER_UNIFORM || crew.sampler == GM_SAMPLER_SINE) ? kVarMCDiag : kVarMC;
         return crew.measurer == GM_MEASURER_METRIC_WISE ? kVarMRWise : kVarMRFree;
     }
     // variant of the GETMe element pass, whose volumes also follow the measurer
@@ -229,10 +267,27 @@ struct gm_mesh
 };
 
 namespace gm {
-// LocalSampler backgrounds (gm_local.cu): from the resident mesh with the
-// analytic metric of `crew` at its vertices, or given by the caller
+// Background-mesh samplers (gm_local.cu).  LocalSampler backgrounds: from
+// the resident mesh with the analytic metric of `crew` at its vertices, or
+// given by the caller; kd-trees and textures: sampled from a background built
+// from the mesh, or given.
 std::shared_ptr<LocalBackground> local_background_from_mesh(gm_mesh* m, const Crew& crew);
 std::shared_ptr<LocalBackground> local_background_given(gm_mesh* m, uint32_t ntets, const uint32_t* tets8,
                                                         uint32_t nverts, const double* xyz, const double* metrics6);
+std::shared_ptr<KdTreeData> kdtree_from_mesh(gm_mesh* m, const LocalBackground& bg, const Crew& crew, int depth);
+std::shared_ptr<KdTreeData> kdtree_given(gm_mesh* m, uint32_t n, const int32_t* children2, const double* sep4,
+                                         const double* metrics6);
+std::shared_ptr<TextureData> texture_from_mesh(gm_mesh* m, const LocalBackground& bg, const Crew& crew, int depth);
+std::shared_ptr<TextureData> texture_given(gm_mesh* m, const int32_t* dims3, const double* lo3, const double* ext3,
+                                           const double* metrics6);
+// builds what crew c's sampler needs (keeping what is still valid), commits
+// the parts to the mesh and points c.local at the assembled field
+void prepare_sampler(gm_mesh* m, Crew& c);
+// uploads the LocalField assembled from the mesh's parts; its device address
+const LocalField* assemble_field(gm_mesh* m);
+// a new topology: parts built from the old mesh are dropped, and rebuilt
+// while a background-mesh sampler is installed
+void sampler_topology_changed(gm_mesh* m);
+size_t sampler_bytes(const gm_mesh* m);
 }  // namespace gm
 

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -360,10 +361,416 @@ std::shared_ptr<LocalBackground> finish(const std::vector<uint4>& tv, const std:
     f.nt = nt;
     f.np = np;
     f.ne = (uint32_t)first.size();
+    bg->part = f;
+    bg->pd_h = pd;
+    bg->tv_h = tv;
     upload(bg->field, &f, 1, s);
     GM_CUDA(cudaStreamSynchronize(s));
     return bg;
 }
+
+// the local metric at points, each walk from its own start tet (FP64)
+__global__ void __launch_bounds__(128) local_query_kernel(const LocalField* __restrict__ L, const double* __restrict__ pts,
+                                                          const uint32_t* __restrict__ start, uint32_t n,
+                                                          double* __restrict__ out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const V3<double> p{pts[3 * (size_t)i], pts[3 * (size_t)i + 1], pts[3 * (size_t)i + 2]};
+    const Sym3<double> M = local_walk<double>(*L, p, start[i]);
+    const double m[6] = {M.xx, M.yy, M.zz, M.xy, M.xz, M.yz};
+    for (int j = 0; j < 6; ++j) out[6 * (size_t)i + j] = m[j];
+}
+
+// LocalSampler::metricAt on the device for a batch of points
+std::vector<double> local_queries(const LocalBackground& bg, const std::vector<double>& pts,
+                                  const std::vector<uint32_t>& start, cudaStream_t s)
+{
+    const uint32_t n = (uint32_t)start.size();
+    std::vector<double> out((size_t)6 * n);
+    if (!n) return out;
+    DBuf<double> d_pts, d_out;
+    DBuf<uint32_t> d_start;
+    upload(d_pts, pts.data(), pts.size(), s);
+    upload(d_start, start.data(), start.size(), s);
+    d_out.reserve((size_t)6 * n);
+    local_query_kernel<<<(n + 127) / 128, 128, 0, s>>>(bg.field.p, d_pts.p, d_start.p, n, d_out.p);
+    GM_CUDA(cudaGetLastError());
+    GM_CUDA(cudaMemcpyAsync(out.data(), d_out.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GM_CUDA(cudaStreamSynchronize(s));
+    return out;
+}
+
+// per vertex the last background tet holding it (the walk cache the
+// reference's background build leaves on each vertex)
+std::vector<uint32_t> vertex_caches(const LocalBackground& bg)
+{
+    std::vector<uint32_t> vc(bg.nref, 0);
+    for (size_t t = 0; t < bg.tv_h.size(); ++t)
+    {
+        const uint4 q = bg.tv_h[t];
+        vc[q.x] = vc[q.y] = vc[q.z] = vc[q.w] = (uint32_t)t;
+    }
+    return vc;
+}
+
+template <class D>
+void upload_metrics(D& data, const std::vector<double>& md, cudaStream_t s)
+{
+    std::vector<float> mf(md.size());
+    for (size_t i = 0; i < md.size(); ++i) mf[i] = (float)md[i];
+    upload(data.md, md.data(), md.size(), s);
+    upload(data.mf, mf.data(), mf.size(), s);
+}
+
+void upload_kd(KdTreeData& kd, const std::vector<int2>& child, const std::vector<double4>& sep,
+               const std::vector<double>& md, cudaStream_t s)
+{
+    std::vector<float4> sf(sep.size());
+    for (size_t i = 0; i < sep.size(); ++i)
+        sf[i] = make_float4((float)sep[i].x, (float)sep[i].y, (float)sep[i].z, (float)sep[i].w);
+    kd.n = (uint32_t)child.size();
+    upload(kd.child, child.data(), child.size(), s);
+    upload(kd.sepd, sep.data(), sep.size(), s);
+    upload(kd.sepf, sf.data(), sf.size(), s);
+    upload_metrics(kd, md, s);
+    GM_CUDA(cudaStreamSynchronize(s));
+}
+
+// KdTreeSampler::build (Samplers/KdTreeSampler.cpp:268-372), nodes numbered
+// in the pre-order of buildGpuBuffers (:374-397)
+struct KdBuilder
+{
+    const std::vector<double>& pd;
+    const std::vector<uint32_t>& vcache;
+    std::vector<int2> child;
+    std::vector<double4> sep;
+    std::vector<double> qpts;
+    std::vector<uint32_t> qstart, qnode;
+
+    double at(uint32_t v, int a) const { return pd[3 * (size_t)v + a]; }
+
+    int build(int height, std::vector<uint32_t>& xs, std::vector<uint32_t>& ys, std::vector<uint32_t>& zs)
+    {
+        const int id = (int)child.size();
+        child.push_back(make_int2(-1, -1));
+        sep.push_back(make_double4(0, 0, 0, 0));
+        const size_t n = xs.size();
+        if (height > 0 && n > 3)
+        {
+            const double ex = at(xs.back(), 0) - at(xs.front(), 0);
+            const double ey = at(ys.back(), 1) - at(ys.front(), 1);
+            const double ez = at(zs.back(), 2) - at(zs.front(), 2);
+            int axis = 0;
+            const std::vector<uint32_t>* list = &xs;
+            if (ey >= ex && ey >= ez) axis = 1, list = &ys;
+            else if (ez >= ex && ez >= ey) axis = 2, list = &zs;
+            const size_t r = n / 2, l = r - 1;
+            const uint32_t sl = (*list)[l], sr = (*list)[r];
+            // dot(axis, separator position) of a unit axis is that coordinate
+            const double sv = n % 2 == 0 ? (at(sl, axis) + at(sr, axis)) / 2.0 : at(sr, axis);
+            sep[id] = make_double4(axis == 0, axis == 1, axis == 2, sv);
+            std::vector<uint32_t> L[3], R[3];
+            std::vector<uint32_t>* src[3] = {&xs, &ys, &zs};
+            for (int q = 0; q < 3; ++q)
+            {
+                for (uint32_t v : *src[q])
+                {
+                    const double d = at(v, axis) - sv;
+                    if (d <= 0.0) L[q].push_back(v);
+                    if (d >= 0.0) R[q].push_back(v);
+                }
+                std::vector<uint32_t>().swap(*src[q]);
+            }
+            const int left = build(height - 1, L[0], L[1], L[2]);
+            child[id].x = left;
+            const int right = build(height - 1, R[0], R[1], R[2]);
+            child[id].y = right;
+        }
+        else
+        {
+            double mean[3] = {0, 0, 0};
+            for (uint32_t v : xs)
+                for (int a = 0; a < 3; ++a) mean[a] += at(v, a);
+            for (int a = 0; a < 3; ++a) qpts.push_back(mean[a] / (double)n);
+            qstart.push_back(vcache[xs.front()]);
+            qnode.push_back((uint32_t)id);
+        }
+        return id;
+    }
+};
+
+}  // namespace
+
+std::shared_ptr<KdTreeData> kdtree_from_mesh(gm_mesh* m, const LocalBackground& bg, const Crew& crew, int depth)
+{
+    const uint32_t nv = bg.nref;
+    require(nv > 0, "the kd-tree sampler needs an uploaded mesh");
+    int height = depth;
+    if (height < 0) height = (int)std::log2(std::ceil(nv / 3.0));
+    require(height < kKdMaxDepth, "kd-tree depth above " + std::to_string(kKdMaxDepth - 1));
+    const std::vector<uint32_t> vc = vertex_caches(bg);
+    std::vector<uint32_t> sorted[3];
+    for (int a = 0; a < 3; ++a)
+    {
+        sorted[a].resize(nv);
+        std::iota(sorted[a].begin(), sorted[a].end(), 0u);
+        const double* pd = bg.pd_h.data();
+        std::sort(sorted[a].begin(), sorted[a].end(),
+                  [pd, a](uint32_t x, uint32_t y) { return pd[3 * (size_t)x + a] < pd[3 * (size_t)y + a]; });
+    }
+    KdBuilder b{bg.pd_h, vc, {}, {}, {}, {}, {}};
+    b.build(height, sorted[0], sorted[1], sorted[2]);
+    const std::vector<double> leaf = local_queries(bg, b.qpts, b.qstart, m->stream);
+    // inner nodes keep the identity (MeshMetric's default), never returned
+    std::vector<double> md((size_t)6 * b.child.size(), 0.0);
+    for (size_t i = 0; i < b.child.size(); ++i) md[6 * i] = md[6 * i + 1] = md[6 * i + 2] = 1.0;
+    for (size_t q = 0; q < b.qnode.size(); ++q)
+        for (int j = 0; j < 6; ++j) md[6 * (size_t)b.qnode[q] + j] = leaf[6 * q + j];
+    auto kd = std::make_shared<KdTreeData>();
+    upload_kd(*kd, b.child, b.sep, md, m->stream);
+    kd->given = false;
+    kd->depth = depth;
+    kd->scaling = crew.scaling;
+    kd->aspect = crew.aspect;
+    return kd;
+}
+
+std::shared_ptr<KdTreeData> kdtree_given(gm_mesh* m, uint32_t n, const int32_t* children2, const double* sep4,
+                                         const double* metrics6)
+{
+    require(children2 && sep4 && metrics6, "null argument");
+    require(n > 0 && n < (1u << 30), "empty or too large kd-tree");
+    std::vector<int2> child(n);
+    std::vector<double4> sep(n);
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        const int32_t l = children2[2 * (size_t)i], r = children2[2 * (size_t)i + 1];
+        // pre-order: children come after their parent, so every descent ends
+        require((l == -1 || ((uint32_t)l > i && (uint32_t)l < n)) && (r == -1 || ((uint32_t)r > i && (uint32_t)r < n)),
+                "kd-tree node " + std::to_string(i) + " names a child out of pre-order");
+        child[i] = make_int2(l, r);
+        sep[i] = make_double4(sep4[4 * (size_t)i], sep4[4 * (size_t)i + 1], sep4[4 * (size_t)i + 2],
+                              sep4[4 * (size_t)i + 3]);
+    }
+    std::vector<double> md(metrics6, metrics6 + 6 * (size_t)n);
+    for (double x : md) require(std::isfinite(x), "non-finite kd-tree metric");
+    auto kd = std::make_shared<KdTreeData>();
+    upload_kd(*kd, child, sep, md, m->stream);
+    kd->given = true;
+    return kd;
+}
+
+namespace {
+
+// TextureSampler::cellId (TextureSampler.cpp:513-524)
+void tex_cell_host(const TextureData& t, const double* pos, int* id)
+{
+    for (int k = 0; k < 3; ++k)
+    {
+        const int c = (int)((pos[k] - t.lo[k]) / t.ext[k] * (double)t.g[k]);
+        id[k] = std::min(std::max(c, 0), t.g[k] - 1);
+    }
+}
+
+}  // namespace
+
+// TextureSampler::buildGrid (TextureSampler.cpp:275-448)
+std::shared_ptr<TextureData> texture_from_mesh(gm_mesh* m, const LocalBackground& bg, const Crew& crew, int depth)
+{
+    require(bg.nref > 0, "the texture sampler needs an uploaded mesh");
+    auto t = std::make_shared<TextureData>();
+    double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+    for (uint32_t v = 0; v < bg.nref; ++v)
+        for (int k = 0; k < 3; ++k)
+        {
+            const double x = bg.pd_h[3 * (size_t)v + k];
+            lo[k] = x < lo[k] ? x : lo[k];
+            hi[k] = hi[k] < x ? x : hi[k];
+        }
+    for (int k = 0; k < 3; ++k)
+    {
+        t->lo[k] = lo[k];
+        t->ext[k] = hi[k] - lo[k];
+    }
+    double cells = (double)bg.nref;
+    if (depth > 0) cells = (double)((size_t)depth * depth * depth);
+    const double alpha = std::pow(cells / (t->ext[0] * t->ext[1] * t->ext[2]), 1 / 3.0);
+    size_t total = 1;
+    for (int k = 0; k < 3; ++k)
+    {
+        const double e = alpha * t->ext[k];
+        const double g = std::round(e > 1.0 ? e : 1.0);
+        require(g < 4096.0, "texture grid too large (a flat mesh?)");
+        t->g[k] = (int)g;
+        total *= (size_t)t->g[k];
+    }
+    require(total <= (size_t)1 << 28, "texture grid too large");
+    // the first tet (in order) whose cell box, grown by one, holds a cell
+    // samples it, its walk starting there; cells no box reaches keep the
+    // identity
+    std::vector<uint32_t> owner(total, kNoTet);
+    std::vector<double> qpts;
+    std::vector<uint32_t> qstart, qcell;
+    double cs[3];
+    for (int k = 0; k < 3; ++k) cs[k] = t->ext[k] / (double)t->g[k];
+    for (size_t e = 0; e < bg.tv_h.size(); ++e)
+    {
+        const uint4 q = bg.tv_h[e];
+        const uint32_t vv[4] = {q.x, q.y, q.z, q.w};
+        double bmin[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, bmax[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+        for (uint32_t v : vv)
+            for (int k = 0; k < 3; ++k)
+            {
+                const double x = bg.pd_h[3 * (size_t)v + k];
+                bmin[k] = x < bmin[k] ? x : bmin[k];
+                bmax[k] = bmax[k] < x ? x : bmax[k];
+            }
+        int a[3], b[3];
+        tex_cell_host(*t, bmin, a);
+        tex_cell_host(*t, bmax, b);
+        for (int k = 0; k < 3; ++k)
+        {
+            a[k] = std::max(a[k] - 1, 0);
+            b[k] = std::min(b[k] + 1, t->g[k] - 1);
+        }
+        for (int z = a[2]; z <= b[2]; ++z)
+            for (int y = a[1]; y <= b[1]; ++y)
+                for (int x = a[0]; x <= b[0]; ++x)
+                {
+                    const size_t c = ((size_t)z * t->g[1] + y) * t->g[0] + x;
+                    if (owner[c] != kNoTet) continue;
+                    owner[c] = (uint32_t)e;
+                    qpts.push_back(t->lo[0] + cs[0] * ((double)x + 0.5));
+                    qpts.push_back(t->lo[1] + cs[1] * ((double)y + 0.5));
+                    qpts.push_back(t->lo[2] + cs[2] * ((double)z + 0.5));
+                    qstart.push_back((uint32_t)e);
+                    qcell.push_back((uint32_t)c);
+                }
+    }
+    const std::vector<double> res = local_queries(bg, qpts, qstart, m->stream);
+    std::vector<double> md(6 * total, 0.0);
+    for (size_t c = 0; c < total; ++c) md[6 * c] = md[6 * c + 1] = md[6 * c + 2] = 1.0;
+    for (size_t q = 0; q < qcell.size(); ++q)
+        for (int j = 0; j < 6; ++j) md[6 * (size_t)qcell[q] + j] = res[6 * q + j];
+    upload_metrics(*t, md, m->stream);
+    GM_CUDA(cudaStreamSynchronize(m->stream));
+    t->given = false;
+    t->depth = depth;
+    t->scaling = crew.scaling;
+    t->aspect = crew.aspect;
+    return t;
+}
+
+std::shared_ptr<TextureData> texture_given(gm_mesh* m, const int32_t* dims3, const double* lo3, const double* ext3,
+                                           const double* metrics6)
+{
+    require(dims3 && lo3 && ext3 && metrics6, "null argument");
+    auto t = std::make_shared<TextureData>();
+    size_t total = 1;
+    for (int k = 0; k < 3; ++k)
+    {
+        require(dims3[k] > 0 && dims3[k] < 4096, "texture dimensions out of range");
+        require(std::isfinite(lo3[k]) && std::isfinite(ext3[k]) && ext3[k] > 0.0, "texture bounds must be finite");
+        t->g[k] = dims3[k];
+        t->lo[k] = lo3[k];
+        t->ext[k] = ext3[k];
+        total *= (size_t)dims3[k];
+    }
+    require(total <= (size_t)1 << 28, "texture grid too large");
+    std::vector<double> md(metrics6, metrics6 + 6 * total);
+    for (double x : md) require(std::isfinite(x), "non-finite texture metric");
+    upload_metrics(*t, md, m->stream);
+    GM_CUDA(cudaStreamSynchronize(m->stream));
+    t->given = true;
+    return t;
+}
+
+const LocalField* assemble_field(gm_mesh* m)
+{
+    LocalField f{};
+    if (m->local) f = m->local->part;
+    if (m->kd)
+    {
+        f.kd_child = m->kd->child.p;
+        f.kd_sepf = m->kd->sepf.p;
+        f.kd_sepd = m->kd->sepd.p;
+        f.kd_mf = m->kd->mf.p;
+        f.kd_md = m->kd->md.p;
+    }
+    if (m->tex)
+    {
+        for (int k = 0; k < 3; ++k)
+        {
+            f.tg[k] = m->tex->g[k];
+            f.tmin[k] = m->tex->lo[k];
+            f.text[k] = m->tex->ext[k];
+        }
+        f.tex_mf = m->tex->mf.p;
+        f.tex_md = m->tex->md.p;
+    }
+    upload(m->field, &f, 1, m->stream);
+    GM_CUDA(cudaStreamSynchronize(m->stream));
+    return m->field.p;
+}
+
+void prepare_sampler(gm_mesh* m, Crew& c)
+{
+    c.local = nullptr;
+    if (c.sampler < GM_SAMPLER_LOCAL) return;
+    auto built_here = [&](const std::shared_ptr<LocalBackground>& b) {
+        return b && b->from_mesh && b->scaling == c.scaling && b->aspect == c.aspect;
+    };
+    std::shared_ptr<LocalBackground> bg = m->local;
+    std::shared_ptr<KdTreeData> kd = m->kd;
+    std::shared_ptr<TextureData> tex = m->tex;
+    // GpuMeshCharacter::updateSampling rebuilds the sampling when the scaling
+    // or the aspect ratio changes (GpuMeshCharacter.cpp:1115-1129); a given
+    // background, kd-tree or texture is the caller's and stays
+    if (c.sampler == GM_SAMPLER_LOCAL && (!bg || (bg->from_mesh && !built_here(bg))))
+        bg = local_background_from_mesh(m, c);
+    auto source = [&]() {
+        if (!built_here(bg)) bg = local_background_from_mesh(m, c);
+        return bg;
+    };
+    if (c.sampler == GM_SAMPLER_KDTREE &&
+        !(kd && (kd->given || (kd->depth == m->depth && kd->scaling == c.scaling && kd->aspect == c.aspect))))
+    {
+        std::shared_ptr<LocalBackground> keep = bg;
+        kd = kdtree_from_mesh(m, *source(), c, m->depth);
+        if (keep && !keep->from_mesh) bg = keep;  // a given background stays the local sampler's
+    }
+    if (c.sampler == GM_SAMPLER_TEXTURE &&
+        !(tex && (tex->given || (tex->depth == m->depth && tex->scaling == c.scaling && tex->aspect == c.aspect))))
+    {
+        std::shared_ptr<LocalBackground> keep = bg;
+        tex = texture_from_mesh(m, *source(), c, m->depth);
+        if (keep && !keep->from_mesh) bg = keep;
+    }
+    m->local = bg;
+    m->kd = kd;
+    m->tex = tex;
+    c.local = assemble_field(m);
+}
+
+void sampler_topology_changed(gm_mesh* m)
+{
+    if (m->local && m->local->from_mesh) m->local.reset();
+    if (m->kd && !m->kd->given) m->kd.reset();
+    if (m->tex && !m->tex->given) m->tex.reset();
+    if (m->crew.sampler >= GM_SAMPLER_LOCAL) prepare_sampler(m, m->crew);
+}
+
+size_t sampler_bytes(const gm_mesh* m)
+{
+    size_t b = m->field.cap * sizeof(LocalField);
+    if (m->local) b += m->local->bytes();
+    if (m->kd) b += m->kd->bytes();
+    if (m->tex) b += m->tex->bytes();
+    return b;
+}
+
+namespace {
 
 template <class T>
 std::vector<T> fetch(const DBuf<T>& b, size_t n, cudaStream_t s)

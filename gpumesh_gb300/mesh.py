@@ -117,9 +117,19 @@ class AbstractSampler:
     def __init__(self):
         self._scaling = 1.0
         self._aspect = 1.0
+        self._depth = -1
 
     def isMetricWise(self) -> bool:
         return self.metric_wise
+
+    def discretizationDepth(self) -> int:
+        return self._depth
+
+    def setDiscretizationDepth(self, depth: int):
+        """AbstractSampler::setDiscretizationDepth: the kd-tree height /
+        texture resolution of the sampled samplers; -1 picks it from the
+        vertex count."""
+        self._depth = int(depth)
 
     def scaling(self) -> float:
         return self._scaling
@@ -157,8 +167,22 @@ class LocalSampler(AbstractSampler):
 
     def updateAnalyticalMetric(self, mesh):
         dev = mesh.device()
+        dev.set_discretization_depth(self.discretizationDepth())
         dev.set_crew(self.kind, "metric_wise", "mean_ratio", self.scaling(), self.aspectRatio())
         dev.build_local_background()
+
+
+class KdTreeSampler(LocalSampler):
+    """Samplers/KdTreeSampler.cpp: the local metric sampled once per leaf of
+    a kd-tree over the vertices (median splits on the widest extent),
+    constant inside a leaf."""
+    kind = "kdtree"
+
+
+class TextureSampler(LocalSampler):
+    """Samplers/TextureSampler.cpp: the local metric sampled at the cell
+    centres of a grid of about one cell per vertex, trilinear in between."""
+    kind = "texture"
 
 
 class SineSampler(AbstractSampler):
@@ -302,6 +326,30 @@ class DeviceMesh:
         """The local sampler's background from the resident mesh (the crew's
         scaling and aspect ratio)."""
         N.check(N.lib().gm_mesh_build_local_background(self.h))
+
+    def set_discretization_depth(self, depth: int):
+        N.check(N.lib().gm_mesh_set_discretization_depth(self.h, int(depth)))
+
+    def set_kd_nodes(self, children2: np.ndarray, separators4: np.ndarray, metrics6: np.ndarray):
+        """kd-tree nodes in pre-order: children (-1: none), separator plane
+        (normal, offset), metric (xx yy zz xy xz yz)."""
+        c = np.ascontiguousarray(children2, np.int32).reshape(-1, 2)
+        sp = np.ascontiguousarray(separators4, np.float64).reshape(-1, 4)
+        m = np.ascontiguousarray(metrics6, np.float64).reshape(-1, 6)
+        if not (c.shape[0] == sp.shape[0] == m.shape[0]):
+            raise ValueError("one separator and one metric per node")
+        N.check(N.lib().gm_mesh_set_kd_nodes(self.h, c.shape[0], N.ptr(c), N.ptr(sp), N.ptr(m)))
+
+    def set_texture(self, dims, lo, extents, metrics6: np.ndarray):
+        """Metric samples at the cell centres of a dims grid over
+        [lo, lo + extents], x fastest."""
+        d = np.ascontiguousarray(dims, np.int32).reshape(3)
+        a = np.ascontiguousarray(lo, np.float64).reshape(3)
+        e = np.ascontiguousarray(extents, np.float64).reshape(3)
+        m = np.ascontiguousarray(metrics6, np.float64).reshape(-1, 6)
+        if m.shape[0] != int(np.prod(d)):
+            raise ValueError("one metric per texture cell")
+        N.check(N.lib().gm_mesh_set_texture(self.h, N.ptr(d), N.ptr(a), N.ptr(e), N.ptr(m)))
 
     def set_local_background(self, tets8: np.ndarray, verts: np.ndarray, metrics6: np.ndarray):
         """A background given as the reference's GpuLocalTet records (4
@@ -504,6 +552,7 @@ class MeshCrew:
         self._evaluator = evaluator
 
     def install(self, dev: DeviceMesh):
+        dev.set_discretization_depth(self._sampler.discretizationDepth())
         dev.set_crew(self._sampler.kind, self._measurer.kind, self._evaluator.kind,
                      self._sampler.scaling(), self._sampler.aspectRatio())
 
@@ -527,6 +576,7 @@ class AbstractEvaluator:
 
     def evaluateMeshQualityCuda(self, mesh: Mesh, sampler, measurer, histogram: QualityHistogram):
         dev = mesh.device()
+        dev.set_discretization_depth(sampler.discretizationDepth())
         dev.set_crew(sampler.kind, measurer.kind, self.kind, sampler.scaling(), sampler.aspectRatio())
         h = dev.evaluate()
         histogram.__dict__.update(h.__dict__)

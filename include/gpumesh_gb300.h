@@ -52,6 +52,11 @@ typedef int gm_status;
 #define GM_SAMPLER_ANALYTIC 1
 #define GM_SAMPLER_SINE 2
 #define GM_SAMPLER_LOCAL 3
+/* KdTreeSampler (Samplers/KdTreeSampler.cpp:218-247: the local metric
+ * sampled once per kd-tree leaf) and TextureSampler (TextureSampler.cpp:
+ * 450-488: the local metric sampled at grid cell centres, trilinear) */
+#define GM_SAMPLER_KDTREE 4
+#define GM_SAMPLER_TEXTURE 5
 /* measurers: MetricFreeMeasurer, MetricWiseMeasurer (Measurers/) */
 #define GM_MEASURER_METRIC_FREE 0
 #define GM_MEASURER_METRIC_WISE 1
@@ -229,6 +234,27 @@ gm_status gm_mesh_build_local_background(gm_mesh* mesh);
  * start from a uniform grid over the background. */
 gm_status gm_mesh_set_local_background(gm_mesh* mesh, uint32_t ntets, const uint32_t* tets8, uint32_t nverts,
                                        const double* xyz, const double* metrics6);
+/* GM_SAMPLER_KDTREE / GM_SAMPLER_TEXTURE sample a local-sampler background
+ * built from the resident mesh, as KdTreeSampler / TextureSampler::
+ * updateAnalyticalMetric do (KdTreeSampler.cpp:116-180, 268-372;
+ * TextureSampler.cpp:257-448), when installed; rebuilt on a scaling, aspect
+ * ratio or depth change and by gm_mesh_build_local_background.
+ * AbstractSampler::setDiscretizationDepth (AbstractSampler.cpp:61-64): the
+ * kd-tree height / texture resolution, -1 (default) from the vertex count. */
+gm_status gm_mesh_set_discretization_depth(gm_mesh* mesh, int32_t depth);
+/* Replaces updateCudaKdNodes (resources/cuda/Sampling/KdTree.cu:58-87;
+ * KdTreeSampler::updateCudaData, KdTreeSampler.cpp:94-103): n nodes in
+ * pre-order (children after their parent), per node its left and right child
+ * (-1: none), its separator plane (normal xyz, offset w: a point p goes left
+ * when dot(p, n) - w < 0) and its metric (xx yy zz xy xz yz). */
+gm_status gm_mesh_set_kd_nodes(gm_mesh* mesh, uint32_t n, const int32_t* children2, const double* separators4,
+                               const double* metrics6);
+/* Replaces updateCudaSamplerTextures (resources/cuda/Sampling/Texture.cu:
+ * 66-147): metric samples at the cell centres of a dims3 grid over
+ * [min3, min3 + extents3], x fastest (6 doubles per cell), read as
+ * TextureSampler::metricAt reads its grid. */
+gm_status gm_mesh_set_texture(gm_mesh* mesh, const int32_t* dims3, const double* min3, const double* extents3,
+                              const double* metrics6);
 
 /* Copy a resident mesh (topology, groups, constraints, crew, positions)
  * device to device into `dst`: a new job on an existing topology needs only
