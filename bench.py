@@ -82,9 +82,11 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="C5: arrival window")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="C5: mean arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0, help="C5: HBM admission budget")
-    ap.add_argument("--only", choices=["eval", "eval_tet", "relocate", "batch", "eval_roofline"], default=None,
+    ap.add_argument("--only", choices=["eval", "eval_tet", "relocate", "batch", "eval_roofline", "rows"],
+                    default=None,
                     help="profiling driver: a few launches of one kernel family, no JSON line "
-                         "(eval_roofline: the two evaluation roofline objects, as JSON)")
+                         "(eval_roofline: the two evaluation roofline objects, as JSON; rows: the "
+                         "samplers, Laplace smoothers and JSON mesh files on the C2 mesh, as JSON)")
     return ap.parse_args()
 
 
@@ -529,7 +531,9 @@ def profile_driver(args):
     from gpumesh_gb300 import mesh as M
     from gpumesh_gb300 import meshgen, workloads
 
-    if args.only == "eval_roofline":
+    if args.only == "rows":
+        print(json.dumps(rows_measurement(torch)), flush=True)
+    elif args.only == "eval_roofline":
         stream = torch.cuda.Stream()
         peak = hbm_peak_gbs()
         print(json.dumps({"roofline_eval": eval_roofline(torch, stream, peak, "hex"),
@@ -569,6 +573,100 @@ def profile_driver(args):
             dev.smooth_pass(smoother, params)
         print("relocate", dev.evaluate().as_dict()["mean"])
     torch.cuda.synchronize()
+
+
+def rows_measurement(torch):
+    """The rows widened beyond the headline path, on the C2 sphere (283,409
+    vertices, 1,608,576 tets): per sampler the time to build its sampling
+    (background mesh, kd-tree, texture) and one metric-conformity evaluation
+    (5 metric samples per tet), beside the FP64 oracle's evaluation on all
+    host cores; one pass of each Laplace smoother beside the oracle on a
+    sample of its first colour; one JSON write and read of the mesh."""
+    import os
+    import tempfile
+
+    from gpumesh_gb300 import mesh as M
+    from gpumesh_gb300 import meshio
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    w, raw, groups = prepare("C2")
+    crew = w.crew(raw)
+    stream = torch.cuda.Stream()
+    threads = os.cpu_count() or 1
+    out = {"mesh": "C2 sphere 80^3 clipped tets", "vertices": int(raw.nv), "tets": int(raw.tets.shape[0]),
+           "cpu_threads": threads, "samplers": {}, "laplace": {}, "json": {}}
+
+    def timed(fn, reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        fn()
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    dev = M.DeviceMesh(raw, groups, stream=stream.cuda_stream)
+    for sampler in ("uniform", "analytic", "local", "kdtree", "texture"):
+        t0 = time.perf_counter()
+        dev.set_crew(sampler, "metric_wise", "metric_conformity", crew["scaling"], 3.0)
+        torch.cuda.synchronize()
+        build_s = time.perf_counter() - t0
+        ms = timed(lambda: dev.evaluate_async(0), 10)
+        q = dev.evaluate().as_dict()
+        t0 = time.perf_counter()
+        orc = pyoracle.OracleMesh.from_raw(raw, sampler=sampler, measurer="metric_wise",
+                                           evaluator="metric_conformity", scaling=crew["scaling"], aspect_ratio=3.0)
+        cpu_build_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        o = orc.evaluate(nthreads=threads)
+        cpu_s = time.perf_counter() - t0
+        orc.close()
+        out["samplers"][sampler] = {
+            "build_s": round(build_s, 4), "eval_ms": round(ms, 4),
+            "metric_samples_per_s": 5 * raw.tets.shape[0] / (ms * 1e-3),
+            "cpu_build_s": round(cpu_build_s, 3), "cpu_eval_s": round(cpu_s, 3),
+            "speedup_eval": round(cpu_s / (ms * 1e-3), 1),
+            # the C2 start has inverted tets (harmonic mean 0): compare the
+            # minimum
+            "min": q["min"], "oracle_min": o["min"], "abs_diff_min": abs(q["min"] - o["min"]),
+            "count": q["count"], "oracle_count": o["count"]}
+    dev.set_crew(**crew)
+    for smoother in ("spring_laplace", "quality_laplace"):
+        saved = dev.fetch_positions()
+        ms = timed(lambda: dev.smooth_pass(smoother, None), 3)
+        dev.upload_positions(saved)
+        movable = int(np.count_nonzero(raw.cid >= 0))
+        # the oracle on the first eighth of every colour, scaled
+        base = groups.group_base
+        sample_base, sample_members = [0], []
+        for g in range(len(base) - 1):
+            m = groups.members[base[g]:base[g + 1]]
+            sample_members.append(m[: max(1, m.size // 8)])
+            sample_base.append(sample_base[-1] + sample_members[-1].size)
+        orc = pyoracle.OracleMesh.from_raw(raw, **crew)
+        t0 = time.perf_counter()
+        orc.smooth_pass(smoother, np.array(sample_base, np.int64), np.concatenate(sample_members), nthreads=threads)
+        cpu_s = time.perf_counter() - t0
+        orc.close()
+        out["laplace"][smoother] = {"pass_ms": round(ms, 4), "relocations_per_s": movable / (ms * 1e-3),
+                                    "cpu_relocations_per_s": sample_base[-1] / cpu_s,
+                                    "cpu_sample_vertices": int(sample_base[-1])}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "c2.json")
+        t0 = time.perf_counter()
+        meshio.write_json(path, raw, precision="exact")
+        wr = time.perf_counter() - t0
+        size = os.path.getsize(path)
+        t0 = time.perf_counter()
+        back = meshio.read_json(path)
+        rd = time.perf_counter() - t0
+        out["json"] = {"bytes": size, "write_s": round(wr, 3), "read_s": round(rd, 3),
+                       "exact_round_trip": bool(np.array_equal(back.pos, raw.pos))}
+    return out
 
 
 def bench_batched(args, rank, world, local):
