@@ -82,7 +82,7 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="C5: arrival window")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="C5: mean arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0, help="C5: HBM admission budget")
-    ap.add_argument("--only", choices=["eval", "eval_tet", "relocate", "batch", "eval_roofline", "rows"],
+    ap.add_argument("--only", choices=["eval", "eval_tet", "eval_local", "relocate", "batch", "eval_roofline", "rows"],
                     default=None,
                     help="profiling driver: a few launches of one kernel family, no JSON line "
                          "(eval_roofline: the two evaluation roofline objects, as JSON; rows: the "
@@ -538,6 +538,15 @@ def profile_driver(args):
         peak = hbm_peak_gbs()
         print(json.dumps({"roofline_eval": eval_roofline(torch, stream, peak, "hex"),
                           "roofline_eval_tet": eval_roofline(torch, stream, peak, "tet")}), flush=True)
+    elif args.only == "eval_local":
+        # metric-conformity evaluation of the C2 mesh under the local sampler
+        # (a background walk per Keast point), 4 launches
+        w, raw, groups = prepare("C2")
+        dev = M.DeviceMesh(raw, None)
+        dev.set_crew("local", "metric_wise", "metric_conformity", w.crew(raw)["scaling"], 3.0)
+        for _ in range(4):
+            h = dev.evaluate()
+        print("eval_local", h.minimumQuality(), h.sampleCount())
     elif args.only in ("eval", "eval_tet"):
         if args.only == "eval":
             raw = meshgen.box_mesh(128, "hex", 0.15, 2, gaussian=True)
