@@ -608,15 +608,21 @@ def rows_measurement(torch):
            "cpu_threads": threads, "samplers": {}, "laplace": {}, "json": {}}
 
     def timed(fn, reps):
+        # queued behind a sleep kernel, so no launch waits for Python; the
+        # median of 3 rounds
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         fn()
         torch.cuda.synchronize()
-        a.record(stream)
-        for _ in range(reps):
-            fn()
-        b.record(stream)
-        torch.cuda.synchronize()
-        return a.elapsed_time(b) / reps
+        rounds = []
+        for _ in range(3):
+            gpu_ahead(torch, stream, 5.0)
+            a.record(stream)
+            for _ in range(reps):
+                fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            rounds.append(a.elapsed_time(b) / reps)
+        return statistics.median(rounds)
 
     dev = M.DeviceMesh(raw, groups, stream=stream.cuda_stream)
     for sampler in ("uniform", "analytic", "local", "kdtree", "texture"):

@@ -54,7 +54,7 @@ struct LocalField
     const uint4* tn;      // neighbour across the face opposite vertex k (0xffffffff: none)
     const float4* pf;     // background vertex positions
     const double* pd;     // the same in FP64, 3 per vertex
-    const float* mf;      // vertex metrics xx yy zz xy xz yz
+    const float4* mf;     // vertex metrics, 2 per vertex: (xx yy zz xy), (xz yz 0 0)
     const double* md;
     const uint32_t* cell;    // grid cell -> start tet
     const uint32_t* ecache;  // element (tets, prisms, hexes) -> its first background tet; null: none
@@ -66,13 +66,13 @@ struct LocalField
     const int2* kd_child;
     const float4* kd_sepf;
     const double4* kd_sepd;
-    const float* kd_mf;
+    const float4* kd_mf;  // 2 per node, as mf
     const double* kd_md;
     // TextureSampler: metric samples at the cell centres of a tg[0] x tg[1] x
     // tg[2] grid over [tmin, tmin + text], x fastest
     int tg[3];
     double tmin[3], text[3];
-    const float* tex_mf;
+    const float4* tex_mf;  // 2 per cell, as mf
     const double* tex_md;
 };
 
@@ -288,6 +288,19 @@ __device__ __forceinline__ V3<R> local_pos(const LocalField& L, uint32_t v)
     }
 }
 
+// a metric stored as two float4 (xx yy zz xy), (xz yz 0 0): two vector loads
+template <class R>
+__device__ __forceinline__ void metric_pair(const float4* base, size_t i, R* m)
+{
+    const float4 a = __ldg(&base[2 * i]), b = __ldg(&base[2 * i + 1]);
+    m[0] = (R)a.x;
+    m[1] = (R)a.y;
+    m[2] = (R)a.z;
+    m[3] = (R)a.w;
+    m[4] = (R)b.x;
+    m[5] = (R)b.y;
+}
+
 template <class R>
 __device__ __forceinline__ bool local_params(const V3<R>* vp, V3<R> p, R coor[4])
 {
@@ -408,7 +421,7 @@ __device__ __forceinline__ Sym3<R> local_walk(const LocalField& L, V3<R> p, uint
         if constexpr (sizeof(R) == 8)
             for (int j = 0; j < 6; ++j) m6[j] = (R)L.md[6 * (size_t)vv[k] + j];
         else
-            for (int j = 0; j < 6; ++j) m6[j] = (R)__ldg(&L.mf[6 * (size_t)vv[k] + j]);
+            metric_pair(L.mf, vv[k], m6);
         M.xx += coor[k] * m6[0];
         M.yy += coor[k] * m6[1];
         M.zz += coor[k] * m6[2];
@@ -466,12 +479,13 @@ __device__ __noinline__ Sym3<R> kd_metric(const LocalField& L, V3<R> p)
         node = next;
     }
     R m[6];
-#pragma unroll
-    for (int j = 0; j < 6; ++j)
+    if constexpr (sizeof(R) == 8)
     {
-        if constexpr (sizeof(R) == 8) m[j] = (R)L.kd_md[6 * (size_t)node + j];
-        else m[j] = (R)__ldg(&L.kd_mf[6 * (size_t)node + j]);
+#pragma unroll
+        for (int j = 0; j < 6; ++j) m[j] = (R)L.kd_md[6 * (size_t)node + j];
     }
+    else
+        metric_pair(L.kd_mf, (size_t)node, m);
     return Sym3<R>{m[0], m[1], m[2], m[3], m[4], m[5]};
 }
 
@@ -482,12 +496,13 @@ template <class R>
 __device__ __forceinline__ void tex_cell_metric(const LocalField& L, int i, int j, int k, R* m)
 {
     const size_t c = ((size_t)k * L.tg[1] + j) * L.tg[0] + i;
-#pragma unroll
-    for (int q = 0; q < 6; ++q)
+    if constexpr (sizeof(R) == 8)
     {
-        if constexpr (sizeof(R) == 8) m[q] = (R)L.tex_md[6 * c + q];
-        else m[q] = (R)__ldg(&L.tex_mf[6 * c + q]);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) m[q] = (R)L.tex_md[6 * c + q];
     }
+    else
+        metric_pair(L.tex_mf, c, m);
 }
 
 template <class R>

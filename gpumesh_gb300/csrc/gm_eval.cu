@@ -16,10 +16,12 @@ namespace gm {
 constexpr int kEvalThreads = 256;
 constexpr int kEvalUnroll = 1;  // elements per thread per iteration of the single-type streams
 // resident blocks per SM the register allocation aims for: the gather
-// streams are latency bound, so they trade registers for resident warps
+// streams are latency bound, so they trade registers for resident warps (the
+// general-metric variants at 2 blocks keep 128 registers: none or a few
+// dozen bytes of spills, against 1 block per SM at their natural 130-167)
 template <int VAR, int SET>
 constexpr int kEvalMinBlocks = VAR == kVarMRFree ? (SET == 9 ? 4 : SET == 4 ? 6 : 1)
-                               : VAR == kVarMCDiag ? (SET == 4 ? 4 : 1) : 1;
+                               : VAR == kVarMCDiag ? (SET == 4 ? 4 : 1) : 2;
 
 // SET: 4 = tets only, 8 = any element types, 9 = hexes only
 // returns the element's histogram bucket

@@ -129,7 +129,7 @@ struct LocalBackground
     DBuf<uint4> tv, tn;
     DBuf<float4> pf;
     DBuf<double> pd, md;
-    DBuf<float> mf;
+    DBuf<float4> mf;  // 2 per vertex
     DBuf<uint32_t> cell, ecache;
     DBuf<LocalField> field;
     LocalField part{};
@@ -140,7 +140,7 @@ struct LocalBackground
     double scaling = 0.0, aspect = 0.0;
     size_t bytes() const
     {
-        return (tv.cap + tn.cap) * 16 + pf.cap * 16 + pd.cap * 8 + md.cap * 8 + mf.cap * 4 +
+        return (tv.cap + tn.cap) * 16 + pf.cap * 16 + pd.cap * 8 + md.cap * 8 + mf.cap * 16 +
                (cell.cap + ecache.cap) * 4 + sizeof(LocalField);
     }
 };
@@ -153,25 +153,25 @@ struct KdTreeData
     DBuf<int2> child;
     DBuf<float4> sepf;
     DBuf<double4> sepd;
-    DBuf<float> mf;
+    DBuf<float4> mf;  // 2 per node
     DBuf<double> md;
     uint32_t n = 0;
     bool given = false;
     int depth = -1;
     double scaling = 0.0, aspect = 0.0;
-    size_t bytes() const { return child.cap * 8 + sepf.cap * 16 + sepd.cap * 32 + mf.cap * 4 + md.cap * 8; }
+    size_t bytes() const { return child.cap * 8 + sepf.cap * 16 + sepd.cap * 32 + mf.cap * 16 + md.cap * 8; }
 };
 
 struct TextureData
 {
-    DBuf<float> mf;
+    DBuf<float4> mf;  // 2 per cell
     DBuf<double> md;
     int g[3] = {0, 0, 0};
     double lo[3] = {0, 0, 0}, ext[3] = {0, 0, 0};
     bool given = false;
     int depth = -1;
     double scaling = 0.0, aspect = 0.0;
-    size_t bytes() const { return mf.cap * 4 + md.cap * 8; }
+    size_t bytes() const { return mf.cap * 16 + md.cap * 8; }
 };
 
 }  // namespace gm

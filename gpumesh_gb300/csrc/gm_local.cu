@@ -298,18 +298,29 @@ void start_grid(const std::vector<uint4>& tv, const std::vector<double>& pd, Loc
 }
 
 __global__ void __launch_bounds__(256) vertex_metrics_kernel(Crew c, const double* __restrict__ pd, uint32_t n,
-                                                             double* __restrict__ md, float* __restrict__ mf)
+                                                             double* __restrict__ md, float4* __restrict__ mf)
 {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
     const Sym3<double> M = analytic_metric<double>(c, V3<double>{pd[3 * (size_t)v], pd[3 * (size_t)v + 1],
                                                                   pd[3 * (size_t)v + 2]});
     const double m[6] = {M.xx, M.yy, M.zz, M.xy, M.xz, M.yz};
-    for (int j = 0; j < 6; ++j)
+    for (int j = 0; j < 6; ++j) md[6 * (size_t)v + j] = m[j];
+    mf[2 * (size_t)v] = make_float4((float)m[0], (float)m[1], (float)m[2], (float)m[3]);
+    mf[2 * (size_t)v + 1] = make_float4((float)m[4], (float)m[5], 0.f, 0.f);
+}
+
+// FP32 copies of 6-entry metrics as float4 pairs (xx yy zz xy), (xz yz 0 0)
+std::vector<float4> metric_pairs(const double* md, size_t n)
+{
+    std::vector<float4> mf(2 * n);
+    for (size_t i = 0; i < n; ++i)
     {
-        md[6 * (size_t)v + j] = m[j];
-        mf[6 * (size_t)v + j] = (float)m[j];
+        const double* m = md + 6 * i;
+        mf[2 * i] = make_float4((float)m[0], (float)m[1], (float)m[2], (float)m[3]);
+        mf[2 * i + 1] = make_float4((float)m[4], (float)m[5], 0.f, 0.f);
     }
+    return mf;
 }
 
 // uploads the background; the vertex metrics are the given ones, or the
@@ -336,11 +347,10 @@ std::shared_ptr<LocalBackground> finish(const std::vector<uint4>& tv, const std:
     upload(bg->cell, cell.data(), cell.size(), s);
     if (!first.empty()) upload(bg->ecache, first.data(), first.size(), s);
     bg->md.reserve((size_t)6 * nref);
-    bg->mf.reserve((size_t)6 * nref);
+    bg->mf.reserve((size_t)2 * nref);
     if (metrics_host)
     {
-        std::vector<float> m32((size_t)6 * nref);
-        for (size_t i = 0; i < m32.size(); ++i) m32[i] = (float)metrics_host[i];
+        const std::vector<float4> m32 = metric_pairs(metrics_host, nref);
         upload(bg->md, metrics_host, (size_t)6 * nref, s);
         upload(bg->mf, m32.data(), m32.size(), s);
     }
@@ -417,8 +427,7 @@ std::vector<uint32_t> vertex_caches(const LocalBackground& bg)
 template <class D>
 void upload_metrics(D& data, const std::vector<double>& md, cudaStream_t s)
 {
-    std::vector<float> mf(md.size());
-    for (size_t i = 0; i < md.size(); ++i) mf[i] = (float)md[i];
+    const std::vector<float4> mf = metric_pairs(md.data(), md.size() / 6);
     upload(data.md, md.data(), md.size(), s);
     upload(data.mf, mf.data(), mf.size(), s);
 }
