@@ -456,11 +456,17 @@ struct KdBuilder
     std::vector<double4> sep;
     std::vector<double> qpts;
     std::vector<uint32_t> qstart, qnode;
+    // vertices on a separator go to both sides, so coincident coordinates can
+    // make the lists grow with the height: the build stops at a budget
+    size_t entries = 0, budget = 0;
 
     double at(uint32_t v, int a) const { return pd[3 * (size_t)v + a]; }
 
     int build(int height, std::vector<uint32_t>& xs, std::vector<uint32_t>& ys, std::vector<uint32_t>& zs)
     {
+        entries += xs.size();
+        if (entries > budget)
+            throw ApiError(GM_ERR_UNSUPPORTED, "kd-tree build: too many vertices on separators for this depth");
         const int id = (int)child.size();
         child.push_back(make_int2(-1, -1));
         sep.push_back(make_double4(0, 0, 0, 0));
@@ -528,7 +534,7 @@ std::shared_ptr<KdTreeData> kdtree_from_mesh(gm_mesh* m, const LocalBackground& 
         std::sort(sorted[a].begin(), sorted[a].end(),
                   [pd, a](uint32_t x, uint32_t y) { return pd[3 * (size_t)x + a] < pd[3 * (size_t)y + a]; });
     }
-    KdBuilder b{bg.pd_h, vc, {}, {}, {}, {}, {}};
+    KdBuilder b{bg.pd_h, vc, {}, {}, {}, {}, {}, 0, (size_t)64 * nv + 4096};
     b.build(height, sorted[0], sorted[1], sorted[2]);
     const std::vector<double> leaf = local_queries(bg, b.qpts, b.qstart, m->stream);
     // inner nodes keep the identity (MeshMetric's default), never returned
