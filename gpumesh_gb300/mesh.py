@@ -663,6 +663,34 @@ class QualityLaplaceSmoother(AbstractSmoother):
     kind = "quality_laplace"
 
 
+# The reference's multi-thread-per-vertex smoothers run Nelder-Mead and
+# gradient descent with the parameters their CUDA drivers install; their
+# kernels spread one patch's elements (or sample positions) over several
+# threads, a decomposition the warp-per-vertex kernels here already make.
+class MultiElemNMSmoother(NelderMeadSmoother):
+    """Smoothers/VertexWise/MultiElemNMSmoother.cpp: Nelder-Mead with the
+    constants of :7-13, those of NelderMeadSmoother."""
+
+
+class MultiElemGradDsntSmoother(GradientDescentSmoother):
+    """Smoothers/VertexWise/MultiElemGradDsntSmoother.cpp: gradient descent
+    with the constants its CUDA driver installs (:7-8): 5 cycles, node shift
+    local size / 25."""
+
+    def __init__(self, params=None):
+        super().__init__(params if params is not None else [1.0 / 25.0, 5])
+
+
+class MultiPosGradDsntSmoother(MultiElemGradDsntSmoother):
+    """Smoothers/VertexWise/MultiPosGradDsntSmoother.cpp (:7-8, the same
+    constants)."""
+
+
+class PatchGradDsntSmoother(MultiElemGradDsntSmoother):
+    """Smoothers/VertexWise/PatchGradDsntSmoother.cpp (:7-8, the same
+    constants)."""
+
+
 SMOOTHER_CLASSES = {"nelder_mead": NelderMeadSmoother, "gradient_descent": GradientDescentSmoother,
                     "spawn_search": SpawnSearchSmoother, "getme": GetmeSmoother,
                     "spring_laplace": SpringLaplaceSmoother, "quality_laplace": QualityLaplaceSmoother}

@@ -222,6 +222,31 @@ def test_host_mirror_api_matches_the_c_abi_path():
     assert hist.harmonicMean() > sm.passes[0].histogram.harmonicMean()
 
 
+def test_multi_thread_smoother_classes_run_their_driver_constants():
+    """MultiElemNM / MultiElemGradDsnt / MultiPosGradDsnt / PatchGradDsnt run
+    Nelder-Mead and gradient descent with the constants their CUDA drivers
+    install: the same final positions as the plain classes given those
+    parameters, and gradient descent's differ from its own defaults."""
+    from gpumesh_gb300 import mesh as M
+
+    raw = meshgen.box_mesh(5, "mixed", 0.2, 12)
+
+    def run(sm):
+        m = M.Mesh(raw)
+        m.compileTopology()
+        crew = M.MeshCrew()
+        crew.setSampler(m, M.UniformSampler())
+        crew.setEvaluator(m, M.MeanRatioEvaluator())
+        sm.smoothMesh(m, crew, "CUDA", M.Schedule(relocationPassCount=2))
+        return np.array(m.verts)
+
+    assert np.array_equal(run(M.MultiElemNMSmoother()), run(M.NelderMeadSmoother()))
+    gd25 = run(M.GradientDescentSmoother([1.0 / 25.0, 5]))
+    for cls in (M.MultiElemGradDsntSmoother, M.MultiPosGradDsntSmoother, M.PatchGradDsntSmoother):
+        assert np.array_equal(run(cls()), gd25), cls.__name__
+    assert not np.array_equal(gd25, run(M.GradientDescentSmoother()))
+
+
 # ---- Laplace smoothers (SpringLaplaceSmoother, QualityLaplaceSmoother) ----
 # Both move toward AbstractMeasurer::computeVertexEquilibrium: spring
 # Laplace without a quality test (no decision, so every vertex agrees with
