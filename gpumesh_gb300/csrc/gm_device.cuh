@@ -43,6 +43,12 @@ enum : int
     kConPipeCircle = 7    // PipeBoundary::Y*CircleEdge: a pipe-end circle, centre in a
 };
 
+// a kd-tree separator plane in FP64: normal xyz, offset w
+struct alignas(32) Plane4d
+{
+    double x, y, z, w;
+};
+
 // LocalSampler's background mesh in device memory (Samplers/LocalSampler.cpp:
 // 352-429): the mesh as it was when the crew was set, split into tets, their
 // face neighbours, the analytic metric at its vertices, and a uniform grid
@@ -65,7 +71,7 @@ struct LocalField
     // (normal xyz, offset w), per node the leaf metric xx yy zz xy xz yz
     const int2* kd_child;
     const float4* kd_sepf;
-    const double4* kd_sepd;
+    const Plane4d* kd_sepd;
     const float4* kd_mf;  // 2 per node, as mf
     const double* kd_md;
     // TextureSampler: metric samples at the cell centres of a tg[0] x tg[1] x
@@ -466,7 +472,7 @@ __device__ __noinline__ Sym3<R> kd_metric(const LocalField& L, V3<R> p)
         R d;
         if constexpr (sizeof(R) == 8)
         {
-            const double4 s = L.kd_sepd[node];
+            const Plane4d s = L.kd_sepd[node];
             d = p.x * s.x + p.y * s.y + p.z * s.z - s.w;
         }
         else

@@ -152,7 +152,7 @@ struct KdTreeData
 {
     DBuf<int2> child;
     DBuf<float4> sepf;
-    DBuf<double4> sepd;
+    DBuf<Plane4d> sepd;
     DBuf<float4> mf;  // 2 per node
     DBuf<double> md;
     uint32_t n = 0;

@@ -432,7 +432,7 @@ void upload_metrics(D& data, const std::vector<double>& md, cudaStream_t s)
     upload(data.mf, mf.data(), mf.size(), s);
 }
 
-void upload_kd(KdTreeData& kd, const std::vector<int2>& child, const std::vector<double4>& sep,
+void upload_kd(KdTreeData& kd, const std::vector<int2>& child, const std::vector<Plane4d>& sep,
                const std::vector<double>& md, cudaStream_t s)
 {
     std::vector<float4> sf(sep.size());
@@ -453,7 +453,7 @@ struct KdBuilder
     const std::vector<double>& pd;
     const std::vector<uint32_t>& vcache;
     std::vector<int2> child;
-    std::vector<double4> sep;
+    std::vector<Plane4d> sep;
     std::vector<double> qpts;
     std::vector<uint32_t> qstart, qnode;
     // vertices on a separator go to both sides, so coincident coordinates can
@@ -469,7 +469,7 @@ struct KdBuilder
             throw ApiError(GM_ERR_UNSUPPORTED, "kd-tree build: too many vertices on separators for this depth");
         const int id = (int)child.size();
         child.push_back(make_int2(-1, -1));
-        sep.push_back(make_double4(0, 0, 0, 0));
+        sep.push_back(Plane4d{0, 0, 0, 0});
         const size_t n = xs.size();
         if (height > 0 && n > 3)
         {
@@ -484,7 +484,7 @@ struct KdBuilder
             const uint32_t sl = (*list)[l], sr = (*list)[r];
             // dot(axis, separator position) of a unit axis is that coordinate
             const double sv = n % 2 == 0 ? (at(sl, axis) + at(sr, axis)) / 2.0 : at(sr, axis);
-            sep[id] = make_double4(axis == 0, axis == 1, axis == 2, sv);
+            sep[id] = Plane4d{axis == 0 ? 1.0 : 0.0, axis == 1 ? 1.0 : 0.0, axis == 2 ? 1.0 : 0.0, sv};
             std::vector<uint32_t> L[3], R[3];
             std::vector<uint32_t>* src[3] = {&xs, &ys, &zs};
             for (int q = 0; q < 3; ++q)
@@ -557,7 +557,7 @@ std::shared_ptr<KdTreeData> kdtree_given(gm_mesh* m, uint32_t n, const int32_t* 
     require(children2 && sep4 && metrics6, "null argument");
     require(n > 0 && n < (1u << 30), "empty or too large kd-tree");
     std::vector<int2> child(n);
-    std::vector<double4> sep(n);
+    std::vector<Plane4d> sep(n);
     for (uint32_t i = 0; i < n; ++i)
     {
         const int32_t l = children2[2 * (size_t)i], r = children2[2 * (size_t)i + 1];
@@ -565,8 +565,8 @@ std::shared_ptr<KdTreeData> kdtree_given(gm_mesh* m, uint32_t n, const int32_t* 
         require((l == -1 || ((uint32_t)l > i && (uint32_t)l < n)) && (r == -1 || ((uint32_t)r > i && (uint32_t)r < n)),
                 "kd-tree node " + std::to_string(i) + " names a child out of pre-order");
         child[i] = make_int2(l, r);
-        sep[i] = make_double4(sep4[4 * (size_t)i], sep4[4 * (size_t)i + 1], sep4[4 * (size_t)i + 2],
-                              sep4[4 * (size_t)i + 3]);
+        sep[i] = Plane4d{sep4[4 * (size_t)i], sep4[4 * (size_t)i + 1], sep4[4 * (size_t)i + 2],
+                         sep4[4 * (size_t)i + 3]};
     }
     std::vector<double> md(metrics6, metrics6 + 6 * (size_t)n);
     for (double x : md) require(std::isfinite(x), "non-finite kd-tree metric");
