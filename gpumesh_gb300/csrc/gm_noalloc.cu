@@ -129,6 +129,9 @@ extern "C" gm_status gm_evaluate_noalloc(uint32_t nv, const void* pos, uint32_t 
     if (!pos || !out || nv == 0) return fail(GM_ERR_INVALID_ARG, "gm_evaluate_noalloc: null positions or output");
     if ((nt && !tets) || (np && !pris) || (nh && !hexs))
         return fail(GM_ERR_INVALID_ARG, "gm_evaluate_noalloc: null connectivity");
+    if (sampler >= GM_SAMPLER_LOCAL && sampler <= GM_SAMPLER_TEXTURE)
+        return fail(GM_ERR_UNSUPPORTED, "gm_evaluate_noalloc: the background-mesh samplers need a resident mesh "
+                                        "(gm_mesh_set_crew, gm_evaluate)");
     if (sampler < 0 || sampler > 2 || measurer < 0 || measurer > 1 || evaluator < 0 || evaluator > 1)
         return fail(GM_ERR_INVALID_ARG, "gm_evaluate_noalloc: unknown sampler, measurer or evaluator");
     if (total == 0) return fail(GM_ERR_INVALID_ARG, "gm_evaluate_noalloc: mesh has no elements");

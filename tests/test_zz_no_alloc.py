@@ -71,3 +71,16 @@ def test_noalloc_rejects_meshes_above_its_limit():
                                      0, 0, 0, 1.0, 1.0, out.data_ptr(), None)
     assert st == 4
     assert b"at most 16777216 elements" in N.lib().gm_last_error()
+
+
+def test_noalloc_rejects_the_background_samplers():
+    # a background mesh, kd-tree or texture lives with a resident mesh
+    torch = pytest.importorskip("torch")
+    raw = meshgen.box_mesh(2, "tet", 0.0, 0)
+    pos, tets, pris, hexs = device_inputs(torch, raw)
+    out = torch.zeros(ctypes.sizeof(N.Quality), dtype=torch.uint8, device="cuda")
+    for name in ("local", "kdtree", "texture"):
+        st = N.lib().gm_evaluate_noalloc(raw.nv, pos.data_ptr(), raw.tets.shape[0], tets.data_ptr(), 0, None, 0,
+                                         None, N.SAMPLERS[name], 1, 1, 1.0, 1.0, out.data_ptr(), None)
+        assert st == 4
+        assert b"need a resident mesh" in N.lib().gm_last_error()
