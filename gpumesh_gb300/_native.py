@@ -93,6 +93,7 @@ def lib():
         "gm_mesh_device_bytes": [vp, ctypes.POINTER(u64)],
         "gm_mesh_restore_positions": [vp],
         "gm_probe_fp32_tflops": [ctypes.POINTER(ctypes.c_double)],
+        "gm_launch_count": [ctypes.POINTER(ctypes.c_uint64)],
         "gm_batch_create": [ctypes.POINTER(vp), vp, u32],
         "gm_batch_destroy": [vp],
         "gm_batch_stream": [vp, ctypes.POINTER(vp)],

@@ -46,6 +46,7 @@ static cudaError_t launch_accept_t(const RelocLaunch& L)
     unsigned blocks = (L.count + L.warps_per_block - 1) / L.warps_per_block;
     accept_kernel<VAR, MAXK><<<blocks, 32 * L.warps_per_block, smem, L.stream>>>(L.m, L.crew, L.def, L.slot_base,
                                                                                L.count, L.maxe);
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -12,8 +13,25 @@
 #include <string>
 #include <vector>
 
-
 #include "gm_host.h"
+
+namespace gm {
+
+static std::atomic<unsigned long long> g_launches{0};
+static thread_local CaptureTally* tl_tally = nullptr;
+
+void note_launch()
+{
+    if (tl_tally) ++tl_tally->kernels;
+    else g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+void add_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+CaptureTally::CaptureTally() : prev(tl_tally) { tl_tally = this; }
+CaptureTally::~CaptureTally() { tl_tally = prev; }
+
+}  // namespace gm
 
 namespace gm {
 static thread_local std::string g_last_error;
@@ -253,8 +271,9 @@ void enqueue_evaluate(gm_mesh* m, Quality* out)
 {
     uint32_t total = m->nt + m->np + m->nh;
     int nb = evaluate_blocks(total, m->sm_count);
-    if (m->parts.reserve(nb))  // a fresh scratch starts with its ticket and bucket totals at 0
+    if (m->parts.reserve(eval_scratch_slots(nb)))  // a fresh scratch starts with its ticket and bucket totals at 0
         GM_CUDA(cudaMemsetAsync(m->parts.p, 0, kEvalScratchHead, m->stream));
+    // the launch uses at most nb blocks, whose scratch the reservation holds
     GM_CUDA(launch_evaluate(m->variant(), m->elem_set(), m->view(), m->crew, m->parts.p, nb, out, m->stream));
 }
 
@@ -1005,12 +1024,14 @@ gm_status gm_job_prepare(gm_mesh* m, int32_t smoother, const double* params, uin
             cudaGraphDestroy(g);
             throw ApiError(GM_ERR_CUDA, std::string("job graph: ") + cudaGetErrorString(e));
         }
+        CaptureTally body_kernels;
         try
         {
             enqueue_pass(m, smoother, sp);
             enqueue_evaluate(m, m->job_fresh.p);
             job_rule_kernel<<<1, 32, 0, m->stream>>>(m->quality.p, m->job_fresh.p, m->job_counter.p, min_gain,
                                                      (int)max_passes, loop);
+            note_launch();
             GM_CUDA(cudaGetLastError());
         }
         catch (...)
@@ -1031,6 +1052,7 @@ gm_status gm_job_prepare(gm_mesh* m, int32_t smoother, const double* params, uin
         }
         m->job_graph = g;
         m->job_max_passes = max_passes;
+        m->job_body_kernels = body_kernels.kernels;
     });
 }
 
@@ -1068,11 +1090,20 @@ gm_status gm_job_result(gm_mesh* m, uint32_t* passes, gm_quality* first, gm_qual
         GM_CUDA(cudaStreamSynchronize(m->stream));
         require(c >= 0 && (uint32_t)c <= m->job_max_passes, "job counter out of range");
         *passes = (uint32_t)c;
+        add_launches((unsigned long long)c * m->job_body_kernels);  // the loop body ran c times
         if (first)
             GM_CUDA(cudaMemcpyAsync(first, m->quality.p, sizeof(Quality), cudaMemcpyDeviceToHost, m->stream));
         if (last)
             GM_CUDA(cudaMemcpyAsync(last, m->quality.p + c, sizeof(Quality), cudaMemcpyDeviceToHost, m->stream));
         GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+gm_status gm_launch_count(uint64_t* count)
+{
+    return guarded([&] {
+        require(count != nullptr, "null output");
+        *count = g_launches.load(std::memory_order_relaxed);
     });
 }
 

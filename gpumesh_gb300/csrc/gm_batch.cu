@@ -415,6 +415,7 @@ static cudaError_t launch_batch_t(const BatchArgs& a, const SmoothParams& sp, in
     // every CTA must be resident: never more than the occupancy allows
     int cps = (ctas_per_sm <= 0 || ctas_per_sm > occ) ? occ : ctas_per_sm;
     kern<<<sm_count * cps, 32 * wpb, smem, s>>>(a, sp);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -572,6 +573,8 @@ cudaError_t launch_batch_evaluate(const BatchMesh* meshes, uint32_t nmesh, const
     default: return cudaErrorNotSupported;
     }
     batch_eval_finalize_kernel<<<(nmesh + 7) / 8, 256, 0, s>>>(meshes, mesh_block, nmesh, parts, out);
+    note_launch();
+    note_launch();
     return cudaGetLastError();
 }
 

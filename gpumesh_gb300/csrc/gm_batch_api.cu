@@ -40,6 +40,7 @@ struct gm_batch
     std::vector<Segment> host_segs;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
+    unsigned long long graph_kernels = 0;  // kernels of one replay of the captured pass
 
     BatchArgs args() const
     {
@@ -351,6 +352,7 @@ gm_status gm_batch_capture_pass(gm_batch* b, int32_t smoother, const double* par
         if (eval_slot >= 0) ensure_slots(b, (uint32_t)eval_slot);
         drop_graph(b);
         GM_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        CaptureTally graph_kernels;
         try
         {
             enqueue_pass(b, smoother, sp);
@@ -365,6 +367,7 @@ gm_status gm_batch_capture_pass(gm_batch* b, int32_t smoother, const double* par
         }
         GM_CUDA(cudaStreamEndCapture(b->stream, &b->graph));
         GM_CUDA(cudaGraphInstantiate(&b->graph_exec, b->graph, 0));
+        b->graph_kernels = graph_kernels.kernels;
     });
 }
 
@@ -373,6 +376,7 @@ gm_status gm_batch_replay(gm_batch* b)
     return guarded([&] {
         require(b && b->graph_exec, "no captured pass");
         GM_CUDA(cudaGraphLaunch(b->graph_exec, b->stream));
+        add_launches(b->graph_kernels);
     });
 }
 

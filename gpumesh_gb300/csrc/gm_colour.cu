@@ -150,6 +150,7 @@ void device_colours(const HostMeshView& in, const std::vector<uint32_t>& e_off, 
     {
         if (round > movable) throw std::runtime_error("device colouring did not converge");
         colour_round_kernel<<<blocks, 256, 0, s>>>(cm, a.p, b.p, ctr.p, ctr.p + 1);
+        note_launch();
         GM_CUDA(cudaGetLastError());
         GM_CUDA(cudaMemcpy(h, ctr.p, sizeof(h), cudaMemcpyDeviceToHost));
         if (h[1]) throw ApiError(GM_ERR_UNSUPPORTED, "device colouring needs more than 128 colours");

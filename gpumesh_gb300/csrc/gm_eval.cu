@@ -9,6 +9,8 @@
 // on scheduling.  The bucket of a non-positive quality is 0.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "gm_launch.h"
 
 namespace gm {
@@ -300,29 +302,42 @@ int evaluate_blocks(uint32_t total, int sm_count)
 
 // nblocks is the partial buffer's capacity; the grid is one wave: the
 // kernel's resident blocks per SM times the SMs, or fewer for a small mesh
+//
+// The one-wave size is looked up once per (kernel variant, device) and kept
+// in an atomic word per device (resident blocks per SM in the high half, SMs
+// in the low half; 0 = not looked up yet), so concurrent first calls from
+// several host threads, or on several devices, each read a complete value.
+constexpr int kEvalMaxDevices = 64;
+
 template <int VAR, int SET>
 static void launch_eval_t(const MeshView& m, const Crew& crew, EvalPartial* parts, int nblocks, Quality* out,
                           cudaStream_t s)
 {
-    static int per_sm = 0, sms = 0;
-    if (per_sm == 0)
+    static std::atomic<uint32_t> wave[kEvalMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kEvalMaxDevices) dev = 0;
+    uint32_t w = wave[dev].load(std::memory_order_relaxed);
+    if (w == 0)
     {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        int per_sm = 0, sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, evaluate_kernel<VAR, SET>, kEvalThreads, 0) !=
-                cudaSuccess || per_sm < 1)
+                cudaSuccess || per_sm < 1 || sms < 1)
         {
             per_sm = 8;
             sms = 152;
         }
+        w = ((uint32_t)per_sm << 16) | (uint32_t)sms;
+        wave[dev].store(w, std::memory_order_relaxed);
     }
+    const int per_sm = (int)(w >> 16), sms = (int)(w & 0xffffu);
     const uint32_t total = m.nt + m.np + m.nh;
     const long per_block = (long)kEvalThreads * kEvalUnroll;  // elements a block covers per iteration
     long grid = ((long)total + per_block - 1) / per_block;
     grid = grid < (long)per_sm * sms ? grid : (long)per_sm * sms;
     grid = grid < nblocks ? grid : nblocks;
     evaluate_kernel<VAR, SET><<<(unsigned)(grid < 1 ? 1 : grid), kEvalThreads, 0, s>>>(m, crew, parts, out);
+    note_launch();
 }
 
 cudaError_t launch_evaluate(int variant, int maxk, const MeshView& m, const Crew& crew, EvalPartial* parts,
@@ -365,6 +380,7 @@ __global__ void __launch_bounds__(256) ffma_probe_kernel(int iters, float* sink)
 cudaError_t launch_ffma_probe(int blocks, int threads, int iters, float* sink, cudaStream_t s)
 {
     ffma_probe_kernel<<<blocks, threads, 0, s>>>(iters, sink);
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -57,6 +57,7 @@ cudaError_t launch_getme_elements(int variant, const MeshView& m, const Crew& cr
     case kVarMC: getme_elements_kernel<kVarMC><<<blocks, 256, 0, s>>>(m, crew, lambda, corners); break;
     default: getme_elements_kernel<kVarMCWise><<<blocks, 256, 0, s>>>(m, crew, lambda, corners); break;
     }
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -145,6 +146,7 @@ static cudaError_t launch_update_t(const RelocLaunch& L, const float4* corners)
     unsigned blocks = (L.count + L.warps_per_block - 1) / L.warps_per_block;
     getme_update_kernel<VAR, MAXK><<<blocks, 32 * L.warps_per_block, smem, L.stream>>>(
         L.m, L.crew, L.sp, corners, L.members, L.count, L.maxe, L.ctr, L.def, L.slot_base);
+    note_launch();
     return cudaGetLastError();
 }
 

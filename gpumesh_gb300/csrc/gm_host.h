@@ -218,6 +218,7 @@ struct gm_mesh
     DBuf<int> job_counter;    // passes done
     DBuf<Quality> job_fresh;  // evaluation of the pass just run
     uint32_t job_max_passes = 0;
+    unsigned long long job_body_kernels = 0;  // kernels of one pass of the job loop
     // background-mesh samplers: the parts, and the LocalField assembled from
     // them that crew.local points to
     std::shared_ptr<LocalBackground> local;

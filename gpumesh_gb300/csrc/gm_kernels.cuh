@@ -29,13 +29,13 @@ struct EvalPartial
     int pad;
 };
 
-// Scratch of one evaluation launch of nb blocks, carved from nb EvalPartial
+// Scratch of one evaluation launch of nb blocks, carved from EvalPartial
 // slots: a ticket word (8 bytes), the 20 bucket totals every block adds to
 // (80 bytes, padded to 88), then per block rsum[nb], min[nb], nbad[nb] as
 // structure-of-arrays so the last block reads them coalesced -- 96 + 16 nb
-// bytes, within nb * sizeof(EvalPartial).  The ticket and the totals are
-// zero between launches: a fresh scratch is cleared once, and the last block
-// of every launch resets them.
+// bytes, which eval_scratch_slots(nb) slots hold (two for a single block).
+// The ticket and the totals are zero between launches: a fresh scratch is
+// cleared once, and the last block of every launch resets them.
 struct EvalScratch
 {
     unsigned int* ticket;
@@ -46,6 +46,12 @@ struct EvalScratch
 };
 constexpr size_t kEvalScratchHead = 96;  // ticket + bucket totals, cleared together
 static_assert(sizeof(EvalPartial) >= kEvalScratchHead, "evaluation scratch layout");
+
+// EvalPartial slots that hold the scratch of an evaluation launch of nb blocks
+__host__ __device__ constexpr size_t eval_scratch_slots(size_t nb)
+{
+    return (kEvalScratchHead + 16 * nb + sizeof(EvalPartial) - 1) / sizeof(EvalPartial);
+}
 
 __host__ __device__ inline EvalScratch eval_scratch(EvalPartial* base, int nb)
 {

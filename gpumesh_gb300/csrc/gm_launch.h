@@ -7,6 +7,21 @@
 
 namespace gm {
 
+// Kernel launches made by this library, reported by gm_launch_count.  Every
+// launch site calls note_launch() after its launch.  Outside stream capture
+// that adds one to the process-wide count; while a CaptureTally is open on
+// the calling thread (a capture begun by this library) it adds to the
+// tally, and the graph's owner adds the tally each time the graph runs.
+void note_launch();
+void add_launches(unsigned long long n);
+struct CaptureTally
+{
+    unsigned long long kernels = 0;
+    CaptureTally* prev;
+    CaptureTally();
+    ~CaptureTally();
+};
+
 // shared memory of one warp's patch; maxk: 4 = tets only, 8 = any element type
 size_t patch_smem_per_warp(int maxk, int maxe);
 

@@ -357,6 +357,7 @@ std::shared_ptr<LocalBackground> finish(const std::vector<uint4>& tv, const std:
     else
     {
         vertex_metrics_kernel<<<(nref + 255) / 256, 256, 0, s>>>(crew, bg->pd.p, nref, bg->md.p, bg->mf.p);
+        note_launch();
         GM_CUDA(cudaGetLastError());
     }
     f.nbg = bg->nbg;
@@ -405,6 +406,7 @@ std::vector<double> local_queries(const LocalBackground& bg, const std::vector<d
     upload(d_start, start.data(), start.size(), s);
     d_out.reserve((size_t)6 * n);
     local_query_kernel<<<(n + 127) / 128, 128, 0, s>>>(bg.field.p, d_pts.p, d_start.p, n, d_out.p);
+    note_launch();
     GM_CUDA(cudaGetLastError());
     GM_CUDA(cudaMemcpyAsync(out.data(), d_out.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
     GM_CUDA(cudaStreamSynchronize(s));

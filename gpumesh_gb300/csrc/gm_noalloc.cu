@@ -29,11 +29,17 @@
 
 namespace gm {
 
-// 1024 block partials: a grid of at most 1024 blocks of 256 threads.  With at
-// most 64 elements per thread (which keeps each thread's FP32 partial sum of
-// 1/q short), the largest mesh is 1024 * 256 * 64 elements.
+// 1024 block partials: a grid of at most 1024 blocks of 256 threads (the
+// evaluation launch also caps the grid at one wave, its resident blocks per
+// SM times the SMs, which is below 1024 on a 152-SM GB300 for every kernel
+// variant).  The element limit, 2^24, bounds each thread's FP32 partial sum
+// of 1/q: the smallest one-wave grid of the variants (2 resident blocks per
+// SM for the general-metric kernels, 304 blocks on 152 SMs) gives a thread
+// at most 216 elements before the FP64 block reduction; the tet and hex
+// mean-ratio kernels (4-6 blocks per SM) give at most 108.
 constexpr int kNoAllocMaxPartials = 1024;
-constexpr uint64_t kNoAllocMaxElements = (uint64_t)kNoAllocMaxPartials * 256 * 64;
+constexpr uint64_t kNoAllocMaxElements = (uint64_t)1 << 24;
+static_assert(eval_scratch_slots(kNoAllocMaxPartials) <= kNoAllocMaxPartials, "scratch of a 1024-block grid");
 
 static __device__ __align__(256) EvalPartial g_noalloc_partials[kNoAllocMaxPartials];
 
@@ -45,7 +51,11 @@ EvalPartial* g_partials_addr[kMaxDevices] = {};
 
 // The device address of g_noalloc_partials on the current device.  In host
 // code the array's name is only a host-side stand-in, so the address is
-// looked up once per device (with that device current) and cached.
+// looked up once per device (with that device current, on the first call)
+// and cached until the process exits.  A device reset (cudaDeviceReset, or
+// the primary context torn down and created again) reloads the library's
+// module, possibly at another address, so this entry point does not support
+// calls after a reset of a device it has already been called on.
 cudaError_t partials_address(int device, EvalPartial** out)
 {
     std::lock_guard<std::mutex> lock(g_setup_mutex);

@@ -122,6 +122,7 @@ static cudaError_t launch_nm_lockstep(const RelocLaunch& L)
     const unsigned blocks = (unsigned)((L.count + per_block - 1) / per_block);
     relocate_nm_lockstep_kernel<VAR><<<blocks, 32 * kNMWarpsPerBlock, smem, L.stream>>>(
         L.m, L.crew, L.sp, L.members, L.count, per_warp, L.maxe, L.ctr, L.def, L.slot_base);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -142,6 +143,7 @@ static cudaError_t launch_relocate_t(const RelocLaunch& L)
         unsigned blocks = (L.count + L.warps_per_block - 1) / L.warps_per_block;
         relocate_kernel<SMOOTHER, VAR, MAXK><<<blocks, 32 * L.warps_per_block, smem, L.stream>>>(
             L.m, L.crew, L.sp, L.members, L.count, L.maxe, L.ctr, L.def, L.slot_base);
+        note_launch();
         return cudaGetLastError();
     }
 }

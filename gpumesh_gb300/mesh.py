@@ -262,6 +262,13 @@ def node_groups_build(raw: RawMesh, permute: bool = True, order: str = "referenc
     return perm, NodeGroups(gb[:g + 1].copy(), members[:gb[g]].copy(), ranges[:6 * g].copy())
 
 
+def launch_count() -> int:
+    """Kernel launches this library has made in this process (gm_launch_count)."""
+    c = ctypes.c_uint64(0)
+    N.check(N.lib().gm_launch_count(ctypes.byref(c)))
+    return int(c.value)
+
+
 def neighbourhoods(raw: RawMesh):
     """(ve_off, ve, vv_off, vv): the vertex neighbourhoods the library builds
     for an upload (Mesh::compileNeighborhoods order, input indices)."""

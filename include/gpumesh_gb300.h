@@ -386,12 +386,25 @@ gm_status gm_job_result(gm_mesh* mesh, uint32_t* passes, gm_quality* first, gm_q
  * every GPU which loads the library holds until exit; meshes above
  * 16,777,216 elements are rejected with GM_ERR_UNSUPPORTED.  The first call
  * on a device looks up that array's device address, so make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race and must be serialised by the caller. */
+ * stream capture; the address is kept until exit, so calls after a reset of
+ * that device (cudaDeviceReset) are not supported.  All calls share the
+ * array: calls that overlap on the GPU race and must be serialised by the
+ * caller.  Precondition, not checked: every tet, prism and hex index is
+ * below nv (the kernel gathers positions by these indices, and an index out
+ * of range reads outside the position buffer). */
 gm_status gm_evaluate_noalloc(uint32_t nv, const void* pos, uint32_t nt, const uint32_t* tets, uint32_t np,
                               const uint32_t* pris, uint32_t nh, const uint32_t* hexs, int32_t sampler,
                               int32_t measurer, int32_t evaluator, double scaling, double aspect_ratio,
                               gm_quality* out, void* stream);
+
+/* No counterpart in the reference (its drivers launch on the legacy default
+ * stream and keep no count).  *count receives the number of kernel launches
+ * this library has made in this process: every direct launch counts one,
+ * and a captured graph (gm_batch_replay, a job of gm_job_launch) counts the
+ * kernels it runs, a job's loop body once per pass it ran (added when
+ * gm_job_result reads the pass count).  Kernels of other libraries are not
+ * counted.  Thread-safe. */
+gm_status gm_launch_count(uint64_t* count);
 
 /* Device peak probe: a dependent-FFMA loop over every SM; *tflops receives
  * the achieved FP32 rate (2 flops per FFMA).  The roofline denominator of

@@ -2171,3 +2171,185 @@ void om_smooth_pass(om_mesh* m, int32_t smoother, const double* params, int64_t 
     for (int t = 0; t < nthreads; ++t) m->patch_evals += c.evals[t];
     free(c.corners);
 }
+
+/* ------------------------------------------------------------------------ */
+/* NodeGroups::build (DataStructures/NodeGroups.cpp:104-122): vertex classes,  */
+/* the breadth-first greedy colouring, the (class, colour, valence) order and  */
+/* the colour-major groups of the permuted mesh                               */
+/* ------------------------------------------------------------------------ */
+
+/* the std::sort call of NodeGroups::determinePositions (om_sort.cpp) */
+void om_sort_node_order(int64_t n, const int* types, const int* groups, const int64_t* valence, int* out);
+
+#define OM_FIXED_TYPE 0
+#define OM_BOUND_TYPE 1
+#define OM_SUBSU_TYPE 2
+#define OM_INTER_TYPE 3
+#define OM_NO_GROUP (-2)
+#define OM_UNSET_GROUP (-1)
+
+/* NodeGroups::isMovableBound (NodeGroups.cpp:695-704): constrained, not fixed */
+static inline int movable_bound(const om_mesh* m, uint32_t v) { return m->cid[v] != 0 && !(m->cid[v] < 0); }
+
+/* NodeGroups::determineTypes (NodeGroups.cpp:124-241) */
+static void ng_types(const om_mesh* m, int* types)
+{
+    char* btet = (char*)calloc((size_t)m->nt + 1, 1);
+    char* bpri = (char*)calloc((size_t)m->np + 1, 1);
+    char* bhex = (char*)calloc((size_t)m->nh + 1, 1);
+    for (int64_t e = 0; e < m->nt; ++e)
+        for (int k = 0; k < 4; ++k)
+            if (movable_bound(m, m->tets[4 * e + k])) btet[e] = 1;
+    for (int64_t e = 0; e < m->np; ++e)
+        for (int k = 0; k < 6; ++k)
+            if (movable_bound(m, m->pris[6 * e + k])) bpri[e] = 1;
+    for (int64_t e = 0; e < m->nh; ++e)
+        for (int k = 0; k < 8; ++k)
+            if (movable_bound(m, m->hexs[8 * e + k])) bhex[e] = 1;
+    for (int64_t v = 0; v < m->nv; ++v)
+    {
+        if (m->cid[v] < 0) types[v] = OM_FIXED_TYPE;           /* isFixed */
+        else if (m->cid[v] != 0) types[v] = OM_BOUND_TYPE;     /* isConstrained */
+        else
+        {
+            int sub = 0;
+            for (int64_t j = m->ne_base[v]; j < m->ne_base[v + 1] && !sub; ++j)
+            {
+                const neig_elem* ne = &m->ne[j];
+                sub = (ne->type == OM_TET && btet[ne->id]) || (ne->type == OM_PRI && bpri[ne->id]) ||
+                      (ne->type == OM_HEX && bhex[ne->id]);
+            }
+            types[v] = sub ? OM_SUBSU_TYPE : OM_INTER_TYPE;
+        }
+    }
+    free(btet);
+    free(bpri);
+    free(bhex);
+}
+
+/* NodeGroups::determineGroups (NodeGroups.cpp:243-363).  The reference takes
+ * the first element of a copy of the existing colours {0 .. G-1} from which
+ * the already coloured neighbours' colours are erased (or a new colour G when
+ * none is left); here the neighbours' colours are stamped in `seen` and the
+ * lowest unstamped colour below G is taken, which is the same choice. */
+static void ng_groups(const om_mesh* m, int* groups)
+{
+    const int64_t nv = m->nv;
+    for (int64_t v = 0; v < nv; ++v) groups[v] = OM_NO_GROUP;
+    int64_t* next = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nv + 1));
+    int64_t* seen = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nv + 1)); /* colour -> last stamp */
+    int64_t nnext = 0, seek = 0, existing = 0;
+    while (nnext < nv)
+    {
+        int64_t first = nnext;
+        for (int64_t v = seek; v < nv; ++v)
+        {
+            ++seek;
+            if (groups[v] == OM_NO_GROUP)
+            {
+                groups[v] = OM_UNSET_GROUP;
+                next[nnext++] = v;
+                break;
+            }
+        }
+        for (int64_t q = first; q < nnext; ++q)
+        {
+            const int64_t vId = next[q];
+            for (int64_t j = m->ne_base[vId]; j < m->ne_base[vId + 1]; ++j)
+            {
+                int n;
+                const uint32_t* el = elem_verts(m, m->ne[j].type, m->ne[j].id, &n);
+                for (int k = 0; k < n; ++k)
+                {
+                    int* g = &groups[el[k]];
+                    if (*g == OM_NO_GROUP)
+                    {
+                        *g = OM_UNSET_GROUP;
+                        next[nnext++] = el[k];
+                    }
+                    else if (*g != OM_UNSET_GROUP)
+                        seen[*g] = vId;
+                }
+            }
+            int group = (int)existing;
+            for (int64_t c = 0; c < existing; ++c)
+                if (seen[c] != vId)
+                {
+                    group = (int)c;
+                    break;
+                }
+            if (group == existing)
+            {
+                seen[existing] = -1;
+                ++existing;
+            }
+            groups[vId] = group;
+        }
+    }
+    free(next);
+    free(seen);
+}
+
+int64_t om_node_groups_build(const om_mesh* m, uint32_t* perm, int64_t* group_base, uint32_t* members,
+                             int64_t* ranges)
+{
+    const int64_t nv = m->nv;
+    int* types = (int*)malloc(sizeof(int) * (size_t)(nv + 1));
+    int* groups = (int*)malloc(sizeof(int) * (size_t)(nv + 1));
+    int64_t* valence = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nv + 1));
+    int* indices = (int*)malloc(sizeof(int) * (size_t)(nv + 1));
+    ng_types(m, types);
+    ng_groups(m, groups);
+    /* NodeGroups::determinePositions (NodeGroups.cpp:365-450): sort by class,
+     * then colour, then the number of neighbour elements */
+    for (int64_t v = 0; v < nv; ++v) valence[v] = m->ne_base[v + 1] - m->ne_base[v];
+    om_sort_node_order(nv, types, groups, valence, indices);
+
+    /* NodeGroups::clusterNodes (NodeGroups.cpp:452-619): vertex vId of the
+     * permuted mesh is input vertex indices[vId]; every movable vertex joins
+     * its colour's undispatched list, and the first vertex of a (class,
+     * colour) run opens that class's range of the colour */
+    int64_t ngroups = 0;
+    for (int64_t v = 0; v < nv; ++v)
+        if (types[v] != OM_FIXED_TYPE && groups[v] + 1 > ngroups) ngroups = groups[v] + 1;
+    int64_t* count = (int64_t*)calloc((size_t)ngroups + 1, sizeof(int64_t));
+    memset(ranges, 0, sizeof(int64_t) * 6 * (size_t)ngroups);
+    int last_type = -1, last_group = -1;
+    for (int64_t vId = 0; vId < nv; ++vId)
+    {
+        const int old = indices[vId];
+        perm[vId] = (uint32_t)old;
+        const int type = types[old];
+        if (type != last_type)
+        {
+            last_type = type;
+            last_group = -1;
+        }
+        if (type == OM_FIXED_TYPE) continue;
+        const int g = groups[old];
+        int64_t* r = ranges + 6 * (int64_t)g + 2 * (type - 1);
+        if (g != last_group)
+        {
+            last_group = g;
+            r[0] = r[1] = vId;
+        }
+        ++r[1];
+        ++count[g];
+    }
+    group_base[0] = 0;
+    for (int64_t g = 0; g < ngroups; ++g) group_base[g + 1] = group_base[g] + count[g];
+    memset(count, 0, sizeof(int64_t) * (size_t)(ngroups + 1));
+    for (int64_t vId = 0; vId < nv; ++vId)
+    {
+        const int old = indices[vId];
+        if (types[old] == OM_FIXED_TYPE) continue;
+        const int g = groups[old];
+        members[group_base[g] + count[g]++] = (uint32_t)vId;
+    }
+    free(count);
+    free(types);
+    free(groups);
+    free(valence);
+    free(indices);
+    return ngroups;
+}

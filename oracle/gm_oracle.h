@@ -108,6 +108,15 @@ void om_smooth_pass(om_mesh* m, int32_t smoother, const double* params,
                     int64_t ngroups, const int64_t* group_base,
                     const uint32_t* members, int32_t nthreads);
 
+/* NodeGroups::build (DataStructures/NodeGroups.cpp:104-122) on the mesh as
+ * given: perm[new] = input vertex (nv), the colour-major groups of the
+ * permuted mesh -- group g is members[group_base[g] .. group_base[g+1]) --
+ * and per group the boundary / subsurface / interior ranges (6 per group).
+ * Capacities: group_base nv + 1, members nv, ranges 6 nv.  Returns the
+ * number of groups. */
+int64_t om_node_groups_build(const om_mesh* m, uint32_t* perm, int64_t* group_base, uint32_t* members,
+                             int64_t* ranges);
+
 /* patch-evaluation counter (number of patchQuality calls since the last
  * reset), used for the FLOP accounting of the relocation roofline */
 int64_t om_patch_eval_count(const om_mesh* m);

@@ -82,12 +82,37 @@ def lib():
         L.om_patch_eval_count.restype = i64
         L.om_patch_eval_count.argtypes = [vp]
         L.om_reset_patch_eval_count.argtypes = [vp]
+        L.om_node_groups_build.restype = i64
+        L.om_node_groups_build.argtypes = [vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
 
 def _p(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def permute(raw, perm: np.ndarray):
+    """The mesh with its vertices in NodeGroups' order (perm[new] = old), as
+    NodeGroups::clusterNodes renumbers it (DataStructures/NodeGroups.cpp:452-514)."""
+    import dataclasses
+
+    new_of_old = np.empty_like(perm)
+    new_of_old[perm] = np.arange(perm.size, dtype=perm.dtype)
+    return dataclasses.replace(raw, pos=np.ascontiguousarray(raw.pos[perm]),
+                               tets=new_of_old[raw.tets].astype(np.uint32),
+                               pris=new_of_old[raw.pris].astype(np.uint32),
+                               hexs=new_of_old[raw.hexs].astype(np.uint32),
+                               cid=np.ascontiguousarray(raw.cid[perm]))
+
+
+def node_groups_build(raw):
+    """NodeGroups::build by the oracle: (perm, group_base, members, ranges)."""
+    m = OracleMesh.from_raw(raw)
+    try:
+        return m.node_groups()
+    finally:
+        m.close()
 
 
 class OracleMesh:
@@ -172,6 +197,17 @@ class OracleMesh:
         gb = np.ascontiguousarray(group_base, np.int64)
         mb = np.ascontiguousarray(members, np.uint32)
         lib().om_smooth_pass(self.h, SMOOTHER[smoother], _p(prm), gb.shape[0] - 1, _p(gb), _p(mb), nthreads)
+
+    def node_groups(self):
+        """NodeGroups::build on this mesh: (perm, group_base, members, ranges)
+        with perm[new] = input vertex, the colour-major groups of the
+        permuted mesh and their boundary / subsurface / interior ranges."""
+        perm = np.zeros(self.nv, np.uint32)
+        base = np.zeros(self.nv + 1, np.int64)
+        members = np.zeros(self.nv, np.uint32)
+        ranges = np.zeros(6 * self.nv, np.int64)
+        n = lib().om_node_groups_build(self.h, _p(perm), _p(base), _p(members), _p(ranges))
+        return perm, base[:n + 1].copy(), members[:base[n]].copy(), ranges[:6 * n].reshape(-1, 6).copy()
 
     @property
     def patch_evals(self) -> int:

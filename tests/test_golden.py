@@ -1,7 +1,8 @@
 """The FP64 oracle against golden vectors produced by the reference's own
 CPU code (tests/golden/make_golden.py): evaluation and one pass of each
-smoother on small seeded meshes, and the product's NodeGroups against the
-reference's permutation and colour groups.  Runs without the reference tree."""
+smoother on small seeded meshes, and both the oracle's and the product's
+NodeGroups against the reference's permutation and colour groups.  Runs
+without the reference tree."""
 
 import glob
 import os
@@ -46,6 +47,15 @@ def test_node_groups_match_golden(path):
     assert np.array_equal(perm, d["perm"])
     assert np.array_equal(groups.group_base, d["group_base"])
     assert np.array_equal(groups.members, d["members"])
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p) for p in FIXTURES])
+def test_oracle_node_groups_match_golden(path):
+    d, raw = load(path)
+    perm, base, members, ranges = pyoracle.node_groups_build(raw)
+    assert np.array_equal(perm, d["perm"])
+    assert np.array_equal(base, d["group_base"])
+    assert np.array_equal(members, d["members"])
 
 
 @pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p) for p in FIXTURES])

@@ -81,6 +81,27 @@ def test_node_groups_match_reference(case):
     assert np.array_equal(ranges, groups.ranges)
 
 
+# the oracle's restatement of NodeGroups::build (the reference arm of the
+# benchmark colours and orders its meshes with it)
+@pytest.mark.parametrize("case", list(CASES) + list(LOCAL_CASES))
+def test_oracle_node_groups_match_reference(case):
+    build, boundary, crew = {**CASES, **LOCAL_CASES}[case]
+    raw = build()
+    ref = pyref.RefMesh(raw, boundary)
+    perm, base, members, ranges = pyoracle.node_groups_build(raw)
+    assert np.array_equal(ref.perm(), perm)
+    rb, rm, rr = ref.groups()
+    assert np.array_equal(rb, base)
+    assert np.array_equal(rm, members)
+    assert np.array_equal(rr, ranges)
+    # the oracle's permutation of the mesh is NodeGroups::clusterNodes'
+    pr = pyoracle.permute(raw, perm)
+    tets = np.zeros_like(pr.tets)
+    if tets.size:
+        pyref.lib().ref_get_tets(ref.h, pyref._p(tets))
+        assert np.array_equal(tets, pr.tets)
+
+
 @pytest.mark.parametrize("case", list(CASES))
 def test_element_and_patch_quality_match_reference(case):
     raw, ref, perm, groups, pr, orc = setup(case)
