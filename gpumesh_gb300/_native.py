@@ -94,6 +94,8 @@ def lib():
         "gm_mesh_restore_positions": [vp],
         "gm_probe_fp32_tflops": [ctypes.POINTER(ctypes.c_double)],
         "gm_launch_count": [ctypes.POINTER(ctypes.c_uint64)],
+        "gm_mesh_fetch_gpu_verts_range": [vp, u32, u32, vp],
+        "gm_mesh_upload_gpu_verts_range": [vp, u32, u32, vp],
         "gm_batch_create": [ctypes.POINTER(vp), vp, u32],
         "gm_batch_destroy": [vp],
         "gm_batch_stream": [vp, ctypes.POINTER(vp)],

@@ -881,6 +881,30 @@ gm_status gm_mesh_fetch_gpu_verts(gm_mesh* m, uint32_t nv, void* gpu_verts)
     });
 }
 
+gm_status gm_mesh_fetch_gpu_verts_range(gm_mesh* m, uint32_t first, uint32_t count, void* gpu_verts)
+{
+    return guarded([&] {
+        require(m && (count == 0 || gpu_verts), "null argument");
+        require((uint64_t)first + count <= m->nv, "vertex range out of bounds");
+        if (!count) return;
+        GM_CUDA(cudaMemcpyAsync(gpu_verts, m->pos.p + first, (size_t)count * sizeof(float4), cudaMemcpyDeviceToHost,
+                                m->stream));
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+gm_status gm_mesh_upload_gpu_verts_range(gm_mesh* m, uint32_t first, uint32_t count, const void* gpu_verts)
+{
+    return guarded([&] {
+        require(m && (count == 0 || gpu_verts), "null argument");
+        require((uint64_t)first + count <= m->nv, "vertex range out of bounds");
+        if (!count) return;
+        GM_CUDA(cudaMemcpyAsync(m->pos.p + first, gpu_verts, (size_t)count * sizeof(float4), cudaMemcpyHostToDevice,
+                                m->stream));
+        GM_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
 gm_status gm_evaluate_async(gm_mesh* m, uint32_t slot)
 {
     return guarded([&] {

@@ -182,6 +182,12 @@ gm_status gm_mesh_upload_gpu_verts(gm_mesh* mesh, uint32_t nv, const void* gpu_v
  * are already uploaded (nv must match): `gpu_verts` should be pinned host
  * memory and must stay unchanged until the stream has passed the copy. */
 gm_status gm_mesh_upload_gpu_verts_async(gm_mesh* mesh, uint32_t nv, const void* gpu_verts);
+/* Replace the copies of fetchCudaSubsurfaceVertices and
+ * sendCudaBoundaryVertices (resources/cuda/Smoothing/Utils.cu:85,117): the
+ * GpuVert records of vertices [first, first + count), device to host and
+ * host to device.  Synchronous on the mesh's stream. */
+gm_status gm_mesh_fetch_gpu_verts_range(gm_mesh* mesh, uint32_t first, uint32_t count, void* gpu_verts);
+gm_status gm_mesh_upload_gpu_verts_range(gm_mesh* mesh, uint32_t first, uint32_t count, const void* gpu_verts);
 /* Replace updateCudaTets / updateCudaPris / updateCudaHexs
  * (resources/cuda/Mesh.cu:100,126,152).  stride_words = 32-bit words per
  * element record: 4/6/8 for bare connectivity, 5/12/16 for GpuTet, GpuPri,

@@ -1518,7 +1518,15 @@ static double patch_quality(const om_mesh* m, uint32_t v)
             quality = gmin(quality, q);
         }
     }
-    if (weight > 0.0) return weight / quality;
+    if (weight > 0.0) quality = weight / quality;
+#ifdef OM_PATCH_QUALITY_FP32
+    /* Measurement variant (libgm_oracle_q32.so), not the reference: every
+     * patch quality rounded to FP32, so that the smoothers' comparisons see
+     * values at the resolution an FP32 implementation has.  It measures how
+     * far the reference's decisions depend on quality differences below
+     * FP32 resolution. */
+    quality = (double)(float)quality;
+#endif
     return quality;
 }
 

@@ -35,29 +35,37 @@ REFERENCE_PARAMS = {
 }
 
 
+def lib_path(variant: str = "") -> str:
+    """The oracle library; variant "q32" is the measurement build whose patch
+    qualities are rounded to FP32 (OM_PATCH_QUALITY_FP32 in gm_oracle.c)."""
+    return LIB_PATH if not variant else os.path.join(BUILD_DIR, f"libgm_oracle_{variant}.so")
+
+
 def build(force: bool = False) -> str:
     src = os.path.join(HERE, "gm_oracle.c")
     sort_src = os.path.join(HERE, "om_sort.cpp")
     newest = max(os.path.getmtime(src), os.path.getmtime(sort_src), os.path.getmtime(os.path.join(HERE, "gm_oracle.h")))
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < newest:
-        os.makedirs(BUILD_DIR, exist_ok=True)
-        obj_c = os.path.join(BUILD_DIR, "gm_oracle.o")
-        obj_s = os.path.join(BUILD_DIR, "om_sort.o")
-        flags = ["-O2", "-ffp-contract=off", "-fPIC"]
-        subprocess.check_call(["gcc", *flags, "-c", src, "-o", obj_c])
-        subprocess.check_call(["g++", *flags, "-std=c++17", "-c", sort_src, "-o", obj_s])
-        subprocess.check_call(["g++", "-shared", "-o", LIB_PATH, obj_c, obj_s, "-lm", "-lpthread"])
+    flags = ["-O2", "-ffp-contract=off", "-fPIC"]
+    for variant, defs in (("", []), ("q32", ["-DOM_PATCH_QUALITY_FP32"])):
+        path = lib_path(variant)
+        if force or not os.path.exists(path) or os.path.getmtime(path) < newest:
+            os.makedirs(BUILD_DIR, exist_ok=True)
+            tag = variant or "fp64"
+            obj_c = os.path.join(BUILD_DIR, f"gm_oracle_{tag}.o")
+            obj_s = os.path.join(BUILD_DIR, "om_sort.o")
+            subprocess.check_call(["gcc", *flags, *defs, "-c", src, "-o", obj_c])
+            subprocess.check_call(["g++", *flags, "-std=c++17", "-c", sort_src, "-o", obj_s])
+            subprocess.check_call(["g++", "-shared", "-o", path, obj_c, obj_s, "-lm", "-lpthread"])
     return LIB_PATH
 
 
-_lib = None
+_libs: dict = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def lib(variant: str = ""):
+    if variant not in _libs:
         build()
-        L = ctypes.CDLL(LIB_PATH)
+        L = ctypes.CDLL(lib_path(variant))
         vp, i64, i32, dbl = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_double
         L.om_create.restype = vp
         L.om_create.argtypes = [i64, vp, i64, vp, i64, vp, i64, vp, vp]
@@ -84,8 +92,8 @@ def lib():
         L.om_reset_patch_eval_count.argtypes = [vp]
         L.om_node_groups_build.restype = i64
         L.om_node_groups_build.argtypes = [vp, vp, vp, vp, vp]
-        _lib = L
-    return _lib
+        _libs[variant] = L
+    return _libs[variant]
 
 
 def _p(a: np.ndarray):
@@ -120,8 +128,8 @@ class OracleMesh:
 
     def __init__(self, pos, tets, pris, hexs, cid, con_kind, con_param,
                  sampler="uniform", measurer="metric_free", evaluator="mean_ratio",
-                 scaling=1.0, aspect_ratio=1.0, depth=-1):
-        L = lib()
+                 scaling=1.0, aspect_ratio=1.0, depth=-1, variant: str = ""):
+        self._L = L = lib(variant)
         self._keep = [np.ascontiguousarray(pos, np.float64), np.ascontiguousarray(tets, np.uint32),
                       np.ascontiguousarray(pris, np.uint32), np.ascontiguousarray(hexs, np.uint32),
                       np.ascontiguousarray(cid, np.int32)]
@@ -141,7 +149,7 @@ class OracleMesh:
 
     def close(self):
         if self.h:
-            lib().om_destroy(self.h)
+            self._L.om_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -153,38 +161,38 @@ class OracleMesh:
     @property
     def pos(self) -> np.ndarray:
         out = np.empty((self.nv, 3), np.float64)
-        lib().om_get_pos(self.h, _p(out))
+        self._L.om_get_pos(self.h, _p(out))
         return out
 
     @pos.setter
     def pos(self, value):
         v = np.ascontiguousarray(value, np.float64)
-        lib().om_set_pos(self.h, _p(v))
+        self._L.om_set_pos(self.h, _p(v))
 
     def element_quality(self, etype: int, idx: int) -> float:
-        return lib().om_element_quality(self.h, etype, idx)
+        return self._L.om_element_quality(self.h, etype, idx)
 
     def patch_quality(self, v: int) -> float:
-        return lib().om_patch_quality(self.h, v)
+        return self._L.om_patch_quality(self.h, v)
 
     def local_size(self, v: int) -> float:
-        return lib().om_local_size(self.h, v)
+        return self._L.om_local_size(self.h, v)
 
     def project(self, v: int, p) -> np.ndarray:
         a = np.ascontiguousarray(p, np.float64)
         out = np.empty(3, np.float64)
-        lib().om_project(self.h, v, _p(a), _p(out))
+        self._L.om_project(self.h, v, _p(a), _p(out))
         return out
 
     def metric_at(self, p) -> np.ndarray:
         a = np.ascontiguousarray(p, np.float64)
         out = np.empty(9, np.float64)
-        lib().om_metric_at(self.h, _p(a), _p(out))
+        self._L.om_metric_at(self.h, _p(a), _p(out))
         return out.reshape(3, 3)  # row c = column c of the GLM matrix
 
     def evaluate(self, nthreads: int = 1) -> dict:
         out = np.zeros(23, np.float64)
-        lib().om_evaluate(self.h, _p(out), nthreads)
+        self._L.om_evaluate(self.h, _p(out), nthreads)
         count = out[2]
         return {"min": out[0], "inv_sum": out[1], "count": int(count),
                 "mean": (count / out[1]) if out[1] != 0 else float("nan"),
@@ -196,7 +204,7 @@ class OracleMesh:
         prm[:len(src)] = src
         gb = np.ascontiguousarray(group_base, np.int64)
         mb = np.ascontiguousarray(members, np.uint32)
-        lib().om_smooth_pass(self.h, SMOOTHER[smoother], _p(prm), gb.shape[0] - 1, _p(gb), _p(mb), nthreads)
+        self._L.om_smooth_pass(self.h, SMOOTHER[smoother], _p(prm), gb.shape[0] - 1, _p(gb), _p(mb), nthreads)
 
     def node_groups(self):
         """NodeGroups::build on this mesh: (perm, group_base, members, ranges)
@@ -206,12 +214,12 @@ class OracleMesh:
         base = np.zeros(self.nv + 1, np.int64)
         members = np.zeros(self.nv, np.uint32)
         ranges = np.zeros(6 * self.nv, np.int64)
-        n = lib().om_node_groups_build(self.h, _p(perm), _p(base), _p(members), _p(ranges))
+        n = self._L.om_node_groups_build(self.h, _p(perm), _p(base), _p(members), _p(ranges))
         return perm, base[:n + 1].copy(), members[:base[n]].copy(), ranges[:6 * n].reshape(-1, 6).copy()
 
     @property
     def patch_evals(self) -> int:
-        return lib().om_patch_eval_count(self.h)
+        return self._L.om_patch_eval_count(self.h)
 
     def reset_patch_evals(self):
-        lib().om_reset_patch_eval_count(self.h)
+        self._L.om_reset_patch_eval_count(self.h)

@@ -16,11 +16,15 @@ positions rounded to FP32), evaluating after every pass.  Stored:
     free vertex moved by one FP32 rounding step (nextafter, direction drawn
     per coordinate from a seeded stream; three draws), giving how far the
     FP64 algorithm itself moves the final minimum, mean and positions when
-    only the input's last bit changes.  Relocation decides between
-    candidates by comparing patch qualities, so near-ties resolved the other
-    way change later colours' inputs: at full size this spread is the
-    resolution below which no FP32 implementation can be compared with the
-    FP64 one.
+    only the input's last bit changes;
+  * the FP32-resolution run: the same schedule by the oracle's measurement
+    build whose patch qualities are rounded to FP32 (libgm_oracle_q32.so),
+    so that every comparison the smoothers make (candidate against
+    candidate, a quality gain against a stop threshold) sees the values at
+    FP32 resolution.  Where a decision rests on a difference below that
+    resolution, this run and the FP64 one part ways, and later colours carry
+    the difference on: the distance between the two is what FP32 arithmetic
+    alone changes in the reference algorithm's result.
 
 C4 is sampled: every 256th of its 4,096 meshes (16 meshes), one Nelder-Mead
 pass each.
@@ -84,9 +88,10 @@ def perturbed(raw, pos32, seed):
     return p.astype(np.float64)
 
 
-def run(raw, crew, schedule, pos):
-    """The schedule from `pos`, evaluating before and after every pass."""
-    m = pyoracle.OracleMesh.from_raw(raw, **crew)
+def run(raw, crew, schedule, pos, variant=""):
+    """The schedule from `pos`, evaluating before and after every pass (with
+    the FP64 oracle's evaluator whatever the variant)."""
+    m = pyoracle.OracleMesh.from_raw(raw, **crew, variant=variant)
     m.pos = pos
     perm_base, members = raw._groups
     hist = []
@@ -99,6 +104,13 @@ def run(raw, crew, schedule, pos):
             hist.append((e["min"], e["mean"]))
     out = m.pos
     m.close()
+    if variant:
+        hist = []
+        chk = pyoracle.OracleMesh.from_raw(raw, **crew)
+        chk.pos = out
+        e = chk.evaluate(nthreads=THREADS)
+        chk.close()
+        return np.array([(e["min"], e["mean"])]), out
     return np.array(hist), out
 
 
@@ -123,6 +135,10 @@ def make_one(raw, crew, schedule):
                         float(np.max(np.linalg.norm(f2[idx] - final[idx], axis=1) / out["sample_edge"]))))
     sp = np.array(spreads)
     out.update(spread_min=sp[:, 0].max(), spread_mean=sp[:, 1].max(), spread_pos=sp[:, 2].max(), spreads=sp)
+    hq, fq = run(raw, crew, schedule, pos32, variant="q32")
+    out.update(q32_min=hq[-1, 0], q32_mean=hq[-1, 1], q32_sample_pos=fq[idx],
+               q32_dmin=abs(hq[-1, 0] - hist[-1, 0]), q32_dmean=abs(hq[-1, 1] - hist[-1, 1]),
+               q32_dpos=float(np.max(np.linalg.norm(fq[idx] - final[idx], axis=1) / out["sample_edge"])))
     return out
 
 
@@ -138,17 +154,17 @@ def make_config(name):
             o = make_one(raw, dict(sampler="uniform", measurer="metric_free", evaluator="mean_ratio"),
                          [("nelder_mead", 1, workloads.NM_PARAMS)])
             rows.append((i, int(sizes[i]), o["final_min"], o["final_mean"], o["spread_min"], o["spread_mean"],
-                         o["spread_pos"]))
+                         o["spread_pos"], o["q32_min"], o["q32_mean"]))
         np.savez_compressed(os.path.join(OUT, "C4.npz"), rows=np.array(rows, np.float64),
                             columns=np.array(["mesh", "cells", "final_min", "final_mean", "spread_min",
-                                              "spread_mean", "spread_pos"]))
+                                              "spread_mean", "spread_pos", "q32_min", "q32_mean"]))
     else:
         w = workloads.WORKLOADS[name]
         raw = coloured(w.mesh())
         o = make_one(raw, w.crew(raw), w.schedule)
         np.savez_compressed(os.path.join(OUT, name + ".npz"), **o)
         print(name, "final", o["final_min"], o["final_mean"], "spread", o["spread_min"], o["spread_mean"],
-              o["spread_pos"], flush=True)
+              o["spread_pos"], "q32", o["q32_min"], o["q32_mean"], o["q32_dpos"], flush=True)
     print(f"wrote {name} in {time.time() - t0:.0f} s", flush=True)
 
 

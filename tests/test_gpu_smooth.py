@@ -1,5 +1,6 @@
 """GPU relocation against the FP64 oracle on the same coloured mesh, in the
-same colour-major order.
+same colour-major order, from the same input (the positions rounded to FP32,
+which is what the GPU receives).
 
 Two levels of parity:
 
@@ -7,12 +8,13 @@ Two levels of parity:
   independent, so each GPU vertex must land where the oracle's does, up to
   FP32 rounding (position error / local mean edge length);
 * whole passes: both final meshes are re-evaluated by the FP64 oracle
-  evaluator and compared on min and harmonic mean.  Across colours an FP32
-  rounding in one vertex changes its neighbours' starting patches, and the
-  searches (Nelder-Mead especially) can then end in a different nearby
-  optimum; the FP64 algorithm itself moves its harmonic mean by up to ~1e-4
-  when only its input is rounded to FP32.  The harmonic-mean gate is 1e-4;
-  the min gate is per smoother and stated in each test.
+  evaluator and compared on min and harmonic mean, at 1e-4.  Where a
+  smoother's decision (candidate against candidate, a quality gain against
+  its stop threshold) rests on a quality difference below FP32 resolution,
+  the FP32 path and the FP64 oracle part ways and later colours carry the
+  difference on.  The oracle's measurement build whose patch qualities are
+  rounded to FP32 (variant "q32") measures that effect on the same case; a
+  gate above 1e-4 is twice that measured change, and the test states it.
 """
 
 import numpy as np
@@ -20,6 +22,7 @@ import pytest
 
 from gpumesh_gb300 import meshgen, workloads
 
+import pyoracle
 from helpers import coloured, device_for, edge_lengths, oracle_for
 
 pytestmark = pytest.mark.gpu
@@ -30,6 +33,7 @@ MR = dict(sampler="uniform", measurer="metric_free", evaluator="mean_ratio")
 def run_both(raw, groups, crew, schedule):
     dev = device_for(raw, groups, crew)
     orc = oracle_for(raw, crew)
+    orc.pos = raw.pos.astype(np.float32).astype(np.float64)  # the GPU's input
     for smoother, passes, params in schedule:
         for _ in range(passes):
             dev.smooth_pass(smoother, params)
@@ -80,39 +84,43 @@ def test_one_colour_metric_conformity_sphere():
         assert np.median(err) < 1e-5
 
 
-def oracle_sensitivity(raw, groups, crew, schedule, runs=4, seed=5):
-    """Spread of the FP64 oracle's final harmonic mean when its input moves
-    by one FP32 rounding (relative 2^-24 per coordinate, random sign): the
-    resolution at which a pass of this schedule is reproducible at all."""
-    base = raw.pos.astype(np.float32).astype(np.float64)
-    rng = np.random.default_rng(seed)
-    means = []
-    for _ in range(runs + 1):
-        orc = oracle_for(raw, crew)
-        orc.pos = base if not means else base * (1.0 + rng.choice([-1.0, 1.0], base.shape) * 2.0 ** -24)
+def fp32_resolution_change(raw, groups, crew, schedule):
+    """(FP64 oracle evaluation, |change|) when the oracle's patch qualities
+    are rounded to FP32 (its q32 measurement build), from the GPU's input:
+    how far FP32 resolution of the smoothers' comparisons alone moves the
+    final minimum and harmonic mean on this case."""
+    out = []
+    for variant in ("", "q32"):
+        orc = pyoracle.OracleMesh.from_raw(raw, **crew, variant=variant)
+        orc.pos = raw.pos.astype(np.float32).astype(np.float64)
         for smoother, passes, params in schedule:
             for _ in range(passes):
                 orc.smooth_pass(smoother, groups.group_base, groups.members, params=params, nthreads=4)
-        means.append(orc.evaluate()["mean"])
-    return means[0], max(abs(m - means[0]) for m in means[1:])
+        chk = oracle_for(raw, crew)
+        chk.pos = orc.pos
+        out.append(chk.evaluate())
+    a, b = out
+    return b, abs(b["min"] - a["min"]), abs(b["mean"] - a["mean"])
 
 
 def test_c1_nelder_mead_pass_quality():
-    """C1 (10^3-cell tet cube, NM 1 pass, workloads.NM_PARAMS): the harmonic
-    mean within 1e-4 of the FP64 oracle, or within the oracle's own spread
-    under one-rounding input perturbations if that is wider.  With these
-    parameters (32 cycles, convergence 1e-4) the FP64 search itself is
-    chaotic at that level: a rounding in one vertex changes its neighbours'
-    starting patches in later colours and the searches end in nearby optima
-    (the oracle's mean moves by up to ~1.5e-4).  The minimum is set by one
-    element (min 0.6146 on FP32 inputs vs 0.6223 on FP64 inputs, the same
-    0.6146 that an FP32 build of the oracle reaches), so its gate is 1e-2."""
+    """C1 (10^3-cell tet cube, NM 1 pass, workloads.NM_PARAMS) from identical
+    input.  The harmonic mean is within 1e-4 of the FP64 oracle (measured:
+    3.1e-5).  The minimum is not: one vertex's Nelder-Mead stop test (best
+    minus second-best patch quality < 1e-4) falls on the other side of the
+    threshold at FP32 resolution, the vertex ends 0.8 % of an edge away, and
+    the element that sets the minimum changes (FP64 0.62232, FP32 0.61464).
+    The FP32-resolution oracle reproduces that: its minimum is the GPU's
+    within 1e-4 (measured: 6e-8), so the gap is the algorithm's, not the
+    kernel's."""
     w = workloads.WORKLOADS["C1"]
     raw, groups = coloured(w.mesh())
     gpos, opos, gq, oq, dev = run_both(raw, groups, w.crew(raw), w.schedule)
-    ref, spread = oracle_sensitivity(raw, groups, w.crew(raw), w.schedule)
-    assert abs(gq["mean"] - ref) <= max(1e-4, 1.5 * spread), (gq["mean"], ref, spread)
-    assert abs(gq["min"] - oq["min"]) <= 1e-2, (gq["min"], oq["min"])
+    q32, dmin32, dmean32 = fp32_resolution_change(raw, groups, w.crew(raw), w.schedule)
+    assert abs(gq["mean"] - oq["mean"]) <= 1e-4, (gq["mean"], oq["mean"])
+    if abs(gq["min"] - oq["min"]) > 1e-4:
+        assert dmin32 >= 0.5 * abs(gq["min"] - oq["min"]), (gq["min"], oq["min"], dmin32)
+        assert abs(gq["min"] - q32["min"]) <= 1e-4, (gq["min"], q32["min"])
     err = rel_err(raw, gpos, opos)
     assert np.median(err) < 1e-4 and np.mean(err < 1e-3) > 0.9
 
@@ -125,15 +133,19 @@ def test_c1_nelder_mead_reference_params():
 
 
 def test_gradient_descent_and_spawn_on_sphere_metric_conformity():
+    """Two GD and two spawn-search passes on a 16^3 sphere under the
+    sine-graded metric: min and harmonic mean within max(1e-4, 2 x the
+    change FP32 resolution alone makes in the FP64 oracle on this case)."""
     raw, groups = coloured(meshgen.sphere_mesh(16, 0.25, 1))
     crew = dict(sampler="sine", measurer="metric_wise", evaluator="metric_conformity", scaling=1.0 / raw.h)
     sched = [("gradient_descent", 2, workloads.GD_PARAMS), ("spawn_search", 2, workloads.SPAWN_PARAMS)]
     gpos, opos, gq, oq, dev = run_both(raw, groups, crew, sched)
+    q32, dmin32, dmean32 = fp32_resolution_change(raw, groups, crew, sched)
     b = raw.cid == 1
     assert np.abs(np.linalg.norm(gpos[b], axis=1) - 1.0).max() < 1e-5  # boundary stays on the sphere
-    assert abs(gq["min"] - oq["min"]) <= 1e-3
+    assert abs(gq["min"] - oq["min"]) <= max(1e-4, 2 * dmin32), (gq["min"], oq["min"], dmin32)
     if np.isfinite(oq["inv_sum"]) and np.isfinite(gq["inv_sum"]):
-        assert abs(gq["mean"] - oq["mean"]) <= 1e-3
+        assert abs(gq["mean"] - oq["mean"]) <= max(1e-4, 2 * dmean32), (gq["mean"], oq["mean"], dmean32)
 
 
 def test_getme_hex():
@@ -331,8 +343,7 @@ def test_c2_schedule_quality_matches_oracle():
     one-rounding input perturbations where that is wider.  Ten passes of
     searches that compare nearly equal qualities are chaotic at that level:
     the oracle's minimum moves by ~4e-4 (one element decides it) and its mean
-    by ~7e-5.  On the full 80^3 sphere the GPU and FP64-oracle final meshes
-    differ by |dmin| = 7.5e-5 and |dmean| = 9.4e-5."""
+    by ~7e-5.  The full 80^3 sphere is compared in test_gpu_fullsize.py."""
     w = workloads.small("C2", 24)
     raw, groups = coloured(w.mesh())
     crew = w.crew(raw)
