@@ -326,20 +326,32 @@ def quality_vs_oracle(name, raw, crew, gpu_pos):
     idx = d["sample_idx"]
     err = np.linalg.norm(np.asarray(gpu_pos, np.float64)[idx] - d["sample_pos"], axis=1) / d["sample_edge"]
     dmin, dmean = abs(e["min"] - float(d["final_min"])), abs(e["mean"] - float(d["final_mean"]))
-    gate = lambda k: max(1e-4, 2.0 * max(float(d["spread_" + k]), float(d["q32_d" + k])))  # noqa: E731
+    ok_min, how_min = verdict(e["min"], float(d["final_min"]), d["fp32_min"], float(d["spread_min"]))
+    ok_mean, how_mean = verdict(e["mean"], float(d["final_mean"]), d["fp32_mean"], float(d["spread_mean"]))
     return {"gpu_min": e["min"], "gpu_mean": e["mean"], "oracle_min": float(d["final_min"]),
             "oracle_mean": float(d["final_mean"]), "abs_dmin": dmin, "abs_dmean": dmean,
+            "oracle_fp32_resolution_outcomes_min": [float(x) for x in d["fp32_min"]],
+            "oracle_fp32_resolution_outcomes_mean": [float(x) for x in d["fp32_mean"]],
             "oracle_spread_min": float(d["spread_min"]), "oracle_spread_mean": float(d["spread_mean"]),
-            "fp32_resolution_dmin": float(d["q32_dmin"]), "fp32_resolution_dmean": float(d["q32_dmean"]),
-            "gate_min": gate("min"), "gate_mean": gate("mean"),
-            "within_gate": bool(dmin <= gate("min") and dmean <= gate("mean")),
+            "min_within": how_min if ok_min else None, "mean_within": how_mean if ok_mean else None,
             "pos_err_over_edge": {"max": float(err.max()), "p99": float(np.percentile(err, 99)),
                                   "mean": float(err.mean()), "samples": int(idx.size)},
             "oracle_spread_pos_max": float(d["spread_pos"]),
-            "note": "evaluated by the FP64 oracle; oracle run from the same FP32-rounded input; spread = the "
-                    "oracle's own max change under one-rounding-step input perturbations (3 draws); "
-                    "fp32_resolution = the oracle's change when its patch qualities are rounded to FP32; "
-                    "gate = max(1e-4, 2 x the larger)"}
+            "note": "GPU final mesh evaluated by the FP64 oracle; the oracle ran the same schedule from the same "
+                    "FP32-rounded input.  Passing = within 1e-4 of the FP64 result ('fp64'), or of one of the "
+                    "oracle's outcomes with its patch qualities at FP32 resolution (rounded, or seeded "
+                    "(1 + u 2^-23) draws: 'fp32-resolution outcome'), or within 2 x the oracle's spread under "
+                    "one-rounding-step input perturbations ('input spread')"}
+
+
+def verdict(gpu, fp64, draws, spread):
+    """(passes, how) for one value: within 1e-4 of the FP64 oracle, of one of
+    its FP32-resolution outcomes, or within 2 x its input spread."""
+    if abs(gpu - fp64) <= 1e-4:
+        return True, "fp64"
+    if np.min(np.abs(np.asarray(draws) - gpu)) <= 1e-4:
+        return True, "fp32-resolution outcome"
+    return bool(abs(gpu - fp64) <= 2 * spread), "input spread"
 
 
 def bench_gpu(args, rank, world, local):
@@ -483,24 +495,29 @@ def c4_quality_sample(qual):
     path = os.path.join(FINALS, "C4.npz")
     if not os.path.exists(path):
         return None
-    rows = np.load(path)["rows"]
-    dmin, dmean, smin, smean, ok = [], [], [], [], True
-    for r in rows:
+    fx = np.load(path)
+    rows, fmin, fmean = fx["rows"], fx["fp32_min"], fx["fp32_mean"]
+    dmin, dmean, how = [], [], {}
+    ok = True
+    for k, r in enumerate(rows):
         i = int(r[0])
         if i >= len(qual):
             continue
-        dmin.append(abs(qual[i].minimumQuality() - r[2]))
-        dmean.append(abs(qual[i].harmonicMean() - r[3]))
-        smin.append(max(r[4], abs(r[7] - r[2])))
-        smean.append(max(r[5], abs(r[8] - r[3])))
-        ok = ok and dmin[-1] <= max(1e-4, 2 * smin[-1]) and dmean[-1] <= max(1e-4, 2 * smean[-1])
+        gmin, gmean = qual[i].minimumQuality(), qual[i].harmonicMean()
+        dmin.append(abs(gmin - r[2]))
+        dmean.append(abs(gmean - r[3]))
+        a, ha = verdict(gmin, r[2], fmin[k], r[4])
+        b, hb = verdict(gmean, r[3], fmean[k], r[5])
+        ok = ok and a and b
+        how[ha] = how.get(ha, 0) + 1
+        how[hb] = how.get(hb, 0) + 1
     if not dmin:
         return None
     return {"meshes": len(dmin), "max_abs_dmin": float(max(dmin)), "max_abs_dmean": float(max(dmean)),
-            "oracle_spread_or_fp32_resolution_min_max": float(max(smin)),
-            "oracle_spread_or_fp32_resolution_mean_max": float(max(smean)), "within_gate": bool(ok),
-            "note": "GPU per-mesh evaluation vs the FP64 oracle's run of the same pass from the same FP32 input; "
-                    "per mesh gate = max(1e-4, 2 x the oracle's spread or FP32-resolution change)"}
+            "all_within": bool(ok), "values_within_by": how,
+            "note": "GPU per-mesh evaluation of the batched pass vs the FP64 oracle's pass on the same mesh from "
+                    "the same FP32 input; within = 1e-4 of the FP64 result, of an FP32-resolution outcome of the "
+                    "oracle, or 2 x its input spread"}
 
 
 def bench_batched(args, rank, world, local):

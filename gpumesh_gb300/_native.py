@@ -39,7 +39,9 @@ _lib = None
 
 
 def library_path() -> str:
-    return _build.LIB
+    """The library this process loads: the bounds-checked build when the
+    environment sets GPUMESH_GB300_LIB=checked, else the ordinary one."""
+    return _build.LIB_CHECKED if os.environ.get("GPUMESH_GB300_LIB") == "checked" else _build.LIB
 
 
 def lib():
@@ -47,7 +49,7 @@ def lib():
     global _lib
     if _lib is not None:
         return _lib
-    path = _build.LIB
+    path = library_path()
     if not os.path.exists(path):
         raise ImportError(f"{path} is missing: build it with `python -m gpumesh_gb300.build` "
                           "(or __graft_entry__.build())")
@@ -95,6 +97,8 @@ def lib():
         "gm_probe_fp32_tflops": [ctypes.POINTER(ctypes.c_double)],
         "gm_launch_count": [ctypes.POINTER(ctypes.c_uint64)],
         "gm_mesh_fetch_gpu_verts_range": [vp, u32, u32, vp],
+        "gm_bounds_checked": [ctypes.POINTER(ctypes.c_int32)],
+        "gm_mesh_bounds_status": [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)],
         "gm_mesh_upload_gpu_verts_range": [vp, u32, u32, vp],
         "gm_batch_create": [ctypes.POINTER(vp), vp, u32],
         "gm_batch_destroy": [vp],

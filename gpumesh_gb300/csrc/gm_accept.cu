@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(128) accept_kernel(MeshView m, Crew crew, Defe
     const uint32_t n = *def.count;
     if (w >= n || w >= cap) return;
     WarpPatch P = carve_patch(smem + wib * warp_patch_bytes(MAXK, maxe), MAXK, maxe);
-    const uint32_t v = def.v[slot_base + w];
+    const uint32_t v = GM_IX(m, def.v[slot_base + w], m.nv, kBoundsPosition);
     stage_patch(m, v, P, lane);
     const float4 oldp = def.oldp[slot_base + w], newp = def.newp[slot_base + w];
     const double q0 = patch_uniform<VAR, MAXK, double>(crew, P, to<double>(oldp), lane);

@@ -42,6 +42,28 @@ using namespace gm;
 
 namespace {
 
+#ifdef GM_BOUNDS_CHECK
+constexpr bool kBoundsChecked = true;
+#else
+constexpr bool kBoundsChecked = false;
+#endif
+
+// In a bounds-checked build, the synchronising calls read the mesh's bounds
+// status and turn a recorded failure into an error (and clear it).
+void report_bounds(gm_mesh* m)
+{
+    if (!kBoundsChecked || !m->bounds.p) return;
+    unsigned int w[2] = {0, 0};
+    GM_CUDA(cudaMemcpyAsync(w, m->bounds.p, sizeof(w), cudaMemcpyDeviceToHost, m->stream));
+    GM_CUDA(cudaStreamSynchronize(m->stream));
+    if (!w[0]) return;
+    GM_CUDA(cudaMemsetAsync(m->bounds.p, 0, sizeof(w), m->stream));
+    static const char* names[] = {"", "vertex", "vertex->element CSR", "vertex->vertex CSR", "tet", "prism", "hex",
+                                  "GETMe corner"};
+    throw ApiError(GM_ERR_STATE, std::string("device bounds check: ") + (w[0] < 8 ? names[w[0]] : "?") +
+                                     " index " + std::to_string(w[1]) + " out of range (read as 0)");
+}
+
 void set_crew(gm_mesh* m, int sampler, int measurer, int evaluator, double scaling, double aspect)
 {
     require(sampler >= 0 && sampler <= GM_SAMPLER_TEXTURE, "unknown sampler");
@@ -109,6 +131,8 @@ void upload_csr(gm_mesh* m, const std::vector<uint32_t>& ve_off, const std::vect
     upload(m->ve, ve.data(), ve.size(), m->stream);
     upload(m->vv_off, vv_off.data(), vv_off.size(), m->stream);
     upload(m->vv, vv.data(), vv.size(), m->stream);
+    m->n_ve = (uint32_t)ve.size();
+    m->n_vv = (uint32_t)vv.size();
     update_patch_shape(m, ve_off.data());
 }
 
@@ -433,6 +457,8 @@ gm_status gm_mesh_create(gm_mesh** out)
             GM_CUDA(cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device));
             m->ctr.reserve(1);
             GM_CUDA(cudaMemset(m->ctr.p, 0, sizeof(Counters)));
+            m->bounds.reserve(2);
+            GM_CUDA(cudaMemset(m->bounds.p, 0, 2 * sizeof(unsigned int)));
             set_crew(m, GM_SAMPLER_UNIFORM, GM_MEASURER_METRIC_FREE, GM_EVALUATOR_MEAN_RATIO, 1.0, 1.0);
         }
         catch (...)
@@ -489,6 +515,31 @@ gm_status gm_mesh_sync(gm_mesh* m)
     return guarded([&] {
         require(m != nullptr, "null mesh");
         GM_CUDA(cudaStreamSynchronize(m->stream));
+        report_bounds(m);
+    });
+}
+
+gm_status gm_bounds_checked(int32_t* on)
+{
+    return guarded([&] {
+        require(on != nullptr, "null output");
+        *on = kBoundsChecked ? 1 : 0;
+    });
+}
+
+gm_status gm_mesh_bounds_status(gm_mesh* m, uint32_t* what, uint32_t* index)
+{
+    return guarded([&] {
+        require(m && what && index, "null argument");
+        unsigned int w[2] = {0, 0};
+        if (m->bounds.p)
+        {
+            GM_CUDA(cudaMemcpyAsync(w, m->bounds.p, sizeof(w), cudaMemcpyDeviceToHost, m->stream));
+            GM_CUDA(cudaStreamSynchronize(m->stream));
+            if (w[0]) GM_CUDA(cudaMemsetAsync(m->bounds.p, 0, sizeof(w), m->stream));
+        }
+        *what = w[0];
+        *index = w[1];
     });
 }
 
@@ -806,6 +857,8 @@ gm_status gm_mesh_clone(gm_mesh* dst, const gm_mesh* src)
         dst->np = src->np;
         dst->nh = src->nh;
         dst->ncon = src->ncon;
+        dst->n_ve = last[0];
+        dst->n_vv = last[1];
         dst->n_members = src->n_members;
         dst->group_base = src->group_base;
         dst->crew = src->crew;
@@ -878,6 +931,7 @@ gm_status gm_mesh_fetch_gpu_verts(gm_mesh* m, uint32_t nv, void* gpu_verts)
         require(nv == m->nv, "vertex count mismatch");
         GM_CUDA(cudaMemcpyAsync(gpu_verts, m->pos.p, nv * sizeof(float4), cudaMemcpyDeviceToHost, m->stream));
         GM_CUDA(cudaStreamSynchronize(m->stream));
+        report_bounds(m);
     });
 }
 
@@ -927,6 +981,7 @@ gm_status gm_quality_read(gm_mesh* m, uint32_t slot, gm_quality* out)
         static_assert(sizeof(Quality) == sizeof(gm_quality), "quality layout");
         GM_CUDA(cudaMemcpyAsync(out, m->quality.p + slot, sizeof(Quality), cudaMemcpyDeviceToHost, m->stream));
         GM_CUDA(cudaStreamSynchronize(m->stream));
+        report_bounds(m);
     });
 }
 

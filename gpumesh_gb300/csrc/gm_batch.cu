@@ -58,9 +58,10 @@ __device__ __forceinline__ void batch_one(const BatchMesh& bm, const SmoothParam
         float sx = 0, sy = 0, sz = 0, sw = 0;
         for (uint32_t i = b + lane; i < e; i += kWarp)
         {
-            uint32_t r = m.ve[i];
+            uint32_t r = m.ve[GM_IX(m, i, m.ve_len, kBoundsNeighbourElem)];
             int type = ref_type(r);
-            float4 c = bm.corners[base[type] + (size_t)ref_id(r) * type_size(type) + ref_local(r)];
+            const size_t ci = base[type] + (size_t)ref_id(r) * type_size(type) + ref_local(r);
+            float4 c = bm.corners[GM_IX(m, ci, 4 * m.nt + 6 * m.np + 8 * m.nh, kBoundsCorner)];
             sx += c.x * c.w;
             sy += c.y * c.w;
             sz += c.z * c.w;
@@ -186,7 +187,8 @@ __device__ void nm_lockstep_batch(const BatchArgs& a, const SmoothParams& sp, ch
                 need = sg.need;
                 spins = 0;
                 seen = 0;
-                g.v = bm->members[sg.member_begin + (item - __ldg(&a.seg_start[s]))];
+                g.v = GM_IX(bm->view, bm->members[sg.member_begin + (item - __ldg(&a.seg_start[s]))], bm->view.nv,
+                            kBoundsPosition);
                 g.phase = kNMWait;
             }
             cur += min((uint32_t)__popc(ball), avail);
@@ -380,7 +382,8 @@ __device__ __forceinline__ void batch_queue_loop(const BatchArgs& a, const Smoot
             if (ok)
             {
                 const BatchMesh& bm = a.meshes[sg.mesh];
-                const uint32_t v = bm.members[sg.member_begin + (i - __ldg(&a.seg_start[s]))];
+                const uint32_t v =
+                    GM_IX(bm.view, bm.members[sg.member_begin + (i - __ldg(&a.seg_start[s]))], bm.view.nv, kBoundsPosition);
                 batch_one<SMOOTHER, VAR, MAXK>(bm, sp, P, v, lane, a.ctr);
             }
             __syncwarp();

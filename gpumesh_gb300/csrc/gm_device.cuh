@@ -123,7 +123,40 @@ struct MeshView
     const int32_t* cid;
     const Constraint* con;
     int ncon;
+    uint32_t ve_len, vv_len;  // entries of ve / vv (bounds-checked builds)
+    unsigned int* bounds;     // the mesh's bounds status: {what, index}, 0 = clean
 };
+
+// Bounds-checked indices.  In a library built with GM_BOUNDS_CHECK, every
+// connectivity and CSR index the kernels read through is compared with the
+// length of the array it indexes; the first index found out of range is
+// recorded in the mesh's status word (which array, then the index) and
+// replaced by 0, so that the read stays inside the array.  The host reads
+// the word back (gm_mesh_bounds_status, and every synchronising call of that
+// build) and reports it through gm_last_error.  In the ordinary build the
+// macro is the bare index.
+enum BoundsWhat : unsigned int
+{
+    kBoundsPosition = 1,   // a vertex index (connectivity, neighbour, member) >= nv
+    kBoundsNeighbourElem,  // a vertex->element CSR index >= its length
+    kBoundsNeighbourVert,  // a vertex->vertex CSR index >= its length
+    kBoundsTet,            // a tet id >= nt
+    kBoundsPrism,          // a prism id >= np
+    kBoundsHex,            // a hex id >= nh
+    kBoundsCorner,         // a GETMe corner index >= 4 nt + 6 np + 8 nh
+};
+#ifdef GM_BOUNDS_CHECK
+static __device__ __noinline__ uint32_t bounds_fail(unsigned int* status, unsigned int what, uint32_t index)
+{
+    if (status && atomicCAS(status, 0u, what) == 0u) atomicExch(status + 1, index);
+    return 0u;
+}
+#define GM_IX(m, index, len, what)                                                                      \
+    ((uint32_t)(index) < (uint32_t)(len) ? (uint32_t)(index)                                           \
+                                         : ::gm::bounds_fail((m).bounds, (what), (uint32_t)(index)))
+#else
+#define GM_IX(m, index, len, what) (index)
+#endif
 
 __device__ __forceinline__ int ref_type(uint32_t r) { return (int)(r >> 30); }
 __device__ __forceinline__ int ref_local(uint32_t r) { return (int)((r >> 27) & 7u); }
@@ -1114,20 +1147,25 @@ __device__ __forceinline__ void elem_vertices(const MeshView& m, int type, uint3
 {
     if (type == kTet)
     {
-        uint4 t = m.tets[id];
+        uint4 t = m.tets[GM_IX(m, id, m.nt, kBoundsTet)];
         v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
     }
     else if (type == kPri)
     {
-        const uint2* p = reinterpret_cast<const uint2*>(m.pris + 6 * (size_t)id);
+        const uint2* p = reinterpret_cast<const uint2*>(m.pris + 6 * (size_t)GM_IX(m, id, m.np, kBoundsPrism));
         uint2 a = p[0], b = p[1], c = p[2];
         v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
     }
     else
     {
-        uint4 a = m.hexs[2 * (size_t)id], b = m.hexs[2 * (size_t)id + 1];
+        const size_t h = 2 * (size_t)GM_IX(m, id, m.nh, kBoundsHex);
+        uint4 a = m.hexs[h], b = m.hexs[h + 1];
         v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
     }
+#ifdef GM_BOUNDS_CHECK
+    const int n = type == kTet ? 4 : type == kPri ? 6 : 8;
+    for (int k = 0; k < n; ++k) v[k] = GM_IX(m, v[k], m.nv, kBoundsPosition);
+#endif
 }
 
 // ---------------------------------------------------------------------------

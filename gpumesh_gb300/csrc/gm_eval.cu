@@ -40,23 +40,24 @@ __device__ __forceinline__ int eval_element(const MeshView& m, const Crew& crew,
     V3<float> p[MAXK];
     if (SET == 9)
     {
-        const uint4 a = __ldg(&m.hexs[2 * (size_t)id]), b = __ldg(&m.hexs[2 * (size_t)id + 1]);
-        p[0] = to<float>(__ldg(&m.pos[a.x]));
-        p[1] = to<float>(__ldg(&m.pos[a.y]));
-        p[2] = to<float>(__ldg(&m.pos[a.z]));
-        p[3] = to<float>(__ldg(&m.pos[a.w]));
-        p[4] = to<float>(__ldg(&m.pos[b.x]));
-        p[5] = to<float>(__ldg(&m.pos[b.y]));
-        p[6] = to<float>(__ldg(&m.pos[b.z]));
-        p[7] = to<float>(__ldg(&m.pos[b.w]));
+        const size_t h = 2 * (size_t)GM_IX(m, id, m.nh, kBoundsHex);
+        const uint4 a = __ldg(&m.hexs[h]), b = __ldg(&m.hexs[h + 1]);
+        p[0] = to<float>(__ldg(&m.pos[GM_IX(m, a.x, m.nv, kBoundsPosition)]));
+        p[1] = to<float>(__ldg(&m.pos[GM_IX(m, a.y, m.nv, kBoundsPosition)]));
+        p[2] = to<float>(__ldg(&m.pos[GM_IX(m, a.z, m.nv, kBoundsPosition)]));
+        p[3] = to<float>(__ldg(&m.pos[GM_IX(m, a.w, m.nv, kBoundsPosition)]));
+        p[4] = to<float>(__ldg(&m.pos[GM_IX(m, b.x, m.nv, kBoundsPosition)]));
+        p[5] = to<float>(__ldg(&m.pos[GM_IX(m, b.y, m.nv, kBoundsPosition)]));
+        p[6] = to<float>(__ldg(&m.pos[GM_IX(m, b.z, m.nv, kBoundsPosition)]));
+        p[7] = to<float>(__ldg(&m.pos[GM_IX(m, b.w, m.nv, kBoundsPosition)]));
     }
     else if (MAXK == 4)
     {
-        uint4 t = __ldg(&m.tets[id]);
-        p[0] = to<float>(__ldg(&m.pos[t.x]));
-        p[1] = to<float>(__ldg(&m.pos[t.y]));
-        p[2] = to<float>(__ldg(&m.pos[t.z]));
-        p[3] = to<float>(__ldg(&m.pos[t.w]));
+        uint4 t = __ldg(&m.tets[GM_IX(m, id, m.nt, kBoundsTet)]);
+        p[0] = to<float>(__ldg(&m.pos[GM_IX(m, t.x, m.nv, kBoundsPosition)]));
+        p[1] = to<float>(__ldg(&m.pos[GM_IX(m, t.y, m.nv, kBoundsPosition)]));
+        p[2] = to<float>(__ldg(&m.pos[GM_IX(m, t.z, m.nv, kBoundsPosition)]));
+        p[3] = to<float>(__ldg(&m.pos[GM_IX(m, t.w, m.nv, kBoundsPosition)]));
     }
     else
     {
@@ -162,16 +163,16 @@ __device__ __forceinline__ int eval_conn(const MeshView& m, const Crew& crew, co
 {
     constexpr int MAXK = SET == 4 ? 4 : 8;
     V3<float> p[MAXK];
-    p[0] = to<float>(__ldg(&m.pos[c.a.x]));
-    p[1] = to<float>(__ldg(&m.pos[c.a.y]));
-    p[2] = to<float>(__ldg(&m.pos[c.a.z]));
-    p[3] = to<float>(__ldg(&m.pos[c.a.w]));
+    p[0] = to<float>(__ldg(&m.pos[GM_IX(m, c.a.x, m.nv, kBoundsPosition)]));
+    p[1] = to<float>(__ldg(&m.pos[GM_IX(m, c.a.y, m.nv, kBoundsPosition)]));
+    p[2] = to<float>(__ldg(&m.pos[GM_IX(m, c.a.z, m.nv, kBoundsPosition)]));
+    p[3] = to<float>(__ldg(&m.pos[GM_IX(m, c.a.w, m.nv, kBoundsPosition)]));
     if constexpr (SET == 9)
     {
-        p[4] = to<float>(__ldg(&m.pos[c.b.x]));
-        p[5] = to<float>(__ldg(&m.pos[c.b.y]));
-        p[6] = to<float>(__ldg(&m.pos[c.b.z]));
-        p[7] = to<float>(__ldg(&m.pos[c.b.w]));
+        p[4] = to<float>(__ldg(&m.pos[GM_IX(m, c.b.x, m.nv, kBoundsPosition)]));
+        p[5] = to<float>(__ldg(&m.pos[GM_IX(m, c.b.y, m.nv, kBoundsPosition)]));
+        p[6] = to<float>(__ldg(&m.pos[GM_IX(m, c.b.z, m.nv, kBoundsPosition)]));
+        p[7] = to<float>(__ldg(&m.pos[GM_IX(m, c.b.w, m.nv, kBoundsPosition)]));
     }
     EQ<float> q;
     if constexpr (SET == 9 && VAR == kVarMRFree) q = mr_hex_fast(p);

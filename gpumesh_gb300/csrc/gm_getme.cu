@@ -21,7 +21,7 @@ __device__ __forceinline__ void getme_one(const MeshView& m, const Crew& crew, f
     elem_vertices(m, type, id, vi);
     V3<float> vp[N], vpp[N];
 #pragma unroll
-    for (int k = 0; k < N; ++k) vp[k] = to<float>(m.pos[vi[k]]);
+    for (int k = 0; k < N; ++k) vp[k] = to<float>(m.pos[vi[k]]);  // vi checked by elem_vertices
     float w = getme_transform<VAR, float, N>(m, crew, lambda, type, vi, vp, vpp, elem_hint(type, id));
 #pragma unroll
     for (int k = 0; k < N; ++k) out[(size_t)id * N + k] = make_float4(vpp[k].x, vpp[k].y, vpp[k].z, w);
@@ -70,9 +70,10 @@ __device__ __forceinline__ bool getme_average(const MeshView& m, const float4* c
     float sx = 0, sy = 0, sz = 0, sw = 0;
     for (uint32_t i = b + lane; i < e; i += kWarp)
     {
-        uint32_t r = m.ve[i];
+        uint32_t r = m.ve[GM_IX(m, i, m.ve_len, kBoundsNeighbourElem)];
         int type = ref_type(r);
-        float4 c = corners[base[type] + (size_t)ref_id(r) * type_size(type) + ref_local(r)];
+        const size_t ci = base[type] + (size_t)ref_id(r) * type_size(type) + ref_local(r);
+        float4 c = corners[GM_IX(m, ci, 4 * m.nt + 6 * m.np + 8 * m.nh, kBoundsCorner)];
         sx += c.x * c.w;
         sy += c.y * c.w;
         sz += c.z * c.w;
@@ -101,7 +102,7 @@ __global__ void __launch_bounds__(128) getme_update_kernel(MeshView m, Crew crew
     const uint32_t w = blockIdx.x * (blockDim.x >> 5) + wib;
     if (w >= count) return;
     WarpPatch P = carve_patch(smem + wib * warp_patch_bytes(MAXK, maxe), MAXK, maxe);
-    const uint32_t v = members[w];
+    const uint32_t v = GM_IX(m, members[w], m.nv, kBoundsPosition);
     V3<float> prim;
     if (!getme_average(m, corners, v, lane, prim)) return;
     const int cid = m.cid[v];

@@ -189,6 +189,8 @@ struct gm_mesh
     DBuf<uint32_t> pris;
     DBuf<uint4> hexs;
     DBuf<uint32_t> ve_off, ve, vv_off, vv;
+    uint32_t n_ve = 0, n_vv = 0;  // entries of ve / vv
+    DBuf<unsigned int> bounds;    // bounds status {what, index} (checked builds report it)
     DBuf<int32_t> cid;
     DBuf<Constraint> con;
     int ncon = 0;
@@ -245,6 +247,9 @@ struct gm_mesh
         v.cid = cid.p;
         v.con = con.p;
         v.ncon = ncon;
+        v.ve_len = n_ve;
+        v.vv_len = n_vv;
+        v.bounds = bounds.p;
         return v;
     }
 

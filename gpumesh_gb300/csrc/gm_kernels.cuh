@@ -192,7 +192,7 @@ __device__ __forceinline__ void stage_patch(const MeshView& m, uint32_t v, WarpP
     P.E = (int)(e - b);
     for (int i = lane; i < P.E; i += kWarp)
     {
-        uint32_t r = m.ve[b + i];
+        uint32_t r = m.ve[GM_IX(m, b + i, m.ve_len, kBoundsNeighbourElem)];
         int type = ref_type(r), loc = ref_local(r);
         uint32_t vid[8];
         elem_vertices(m, type, ref_id(r), vid);
@@ -288,12 +288,12 @@ __device__ __forceinline__ void stage_canonical_range(const MeshView& m, const C
     const bool sine = VAR == kVarMCDiag && sine_metric(crew);
     for (int i = first; i < P.E; i += stride)
     {
-        const uint32_t r = m.ve[b + i];
+        const uint32_t r = m.ve[GM_IX(m, b + i, m.ve_len, kBoundsNeighbourElem)];
         const int x = 3 ^ ref_local(r);
-        const uint4 t = m.tets[ref_id(r)];
-        const float4 a0 = __ldcg(&m.pos[tet_corner(t, x)]);
-        const float4 a1 = __ldcg(&m.pos[tet_corner(t, 1 ^ x)]);
-        const float4 a2 = __ldcg(&m.pos[tet_corner(t, 2 ^ x)]);
+        const uint4 t = m.tets[GM_IX(m, ref_id(r), m.nt, kBoundsTet)];
+        const float4 a0 = __ldcg(&m.pos[GM_IX(m, tet_corner(t, x), m.nv, kBoundsPosition)]);
+        const float4 a1 = __ldcg(&m.pos[GM_IX(m, tet_corner(t, 1 ^ x), m.nv, kBoundsPosition)]);
+        const float4 a2 = __ldcg(&m.pos[GM_IX(m, tet_corner(t, 2 ^ x), m.nv, kBoundsPosition)]);
         stage_canonical_element<VAR>(P, i, a0, a1, a2, o, sine);
     }
 }
@@ -578,7 +578,7 @@ __device__ double patch_quality_global(const MeshView& m, const Crew& crew, uint
     PatchAcc<double> a{0.0, 3.0e38, 0};
     for (int i = lane; i < E; i += kWarp)
     {
-        const uint32_t r = m.ve[b + i];
+        const uint32_t r = m.ve[GM_IX(m, b + i, m.ve_len, kBoundsNeighbourElem)];
         const int type = MAXK == 4 ? kTet : ref_type(r), loc = ref_local(r);
         uint32_t vid[8];
         elem_vertices(m, type, ref_id(r), vid);
@@ -608,7 +608,11 @@ __device__ __forceinline__ R local_size(const MeshView& m, uint32_t v, V3<R> pos
 {
     uint32_t b = m.vv_off[v], e = m.vv_off[v + 1];
     R s = 0;
-    for (uint32_t i = b + lane; i < e; i += kWarp) s += length(to<R>(__ldcg(&m.pos[m.vv[i]])) - pos);
+    for (uint32_t i = b + lane; i < e; i += kWarp)
+    {
+        const uint32_t w = m.vv[GM_IX(m, i, m.vv_len, kBoundsNeighbourVert)];
+        s += length(to<R>(__ldcg(&m.pos[GM_IX(m, w, m.nv, kBoundsPosition)])) - pos);
+    }
     for (int o = 16; o > 0; o >>= 1) s += shfl_xor(s, o);
     return s / R(e - b);
 }
@@ -849,7 +853,7 @@ __device__ V3<float> vertex_equilibrium(const MeshView& m, const Crew& crew, uin
     float weight = 0.f;
     for (uint32_t i = b + lane; i < e; i += kWarp)
     {
-        const uint32_t r = m.ve[i];
+        const uint32_t r = m.ve[GM_IX(m, i, m.ve_len, kBoundsNeighbourElem)];
         const int type = MAXK == 4 ? kTet : ref_type(r);
         uint32_t vid[8];
         elem_vertices(m, type, ref_id(r), vid);

@@ -331,15 +331,19 @@ __device__ __forceinline__ float nm_begin(NMGroup& g, const MeshView& m, bool si
     const uint32_t n = max(ee - eb, ve - vb);
     for (uint32_t i = sub; i < n; i += kNMGroup)
     {
-        if (i < ve - vb) ls += length(to<float>(__ldcg(&m.pos[m.vv[vb + i]])) - o);
+        if (i < ve - vb)
+        {
+            const uint32_t w = m.vv[GM_IX(m, vb + i, m.vv_len, kBoundsNeighbourVert)];
+            ls += length(to<float>(__ldcg(&m.pos[GM_IX(m, w, m.nv, kBoundsPosition)])) - o);
+        }
         if (i < ee - eb)
         {
-            const uint32_t r = m.ve[eb + i];
+            const uint32_t r = m.ve[GM_IX(m, eb + i, m.ve_len, kBoundsNeighbourElem)];
             const int x = 3 ^ ref_local(r);
-            const uint4 t = m.tets[ref_id(r)];
-            const float4 a0 = __ldcg(&m.pos[tet_corner(t, x)]);
-            const float4 a1 = __ldcg(&m.pos[tet_corner(t, 1 ^ x)]);
-            const float4 a2 = __ldcg(&m.pos[tet_corner(t, 2 ^ x)]);
+            const uint4 t = m.tets[GM_IX(m, ref_id(r), m.nt, kBoundsTet)];
+            const float4 a0 = __ldcg(&m.pos[GM_IX(m, tet_corner(t, x), m.nv, kBoundsPosition)]);
+            const float4 a1 = __ldcg(&m.pos[GM_IX(m, tet_corner(t, 1 ^ x), m.nv, kBoundsPosition)]);
+            const float4 a2 = __ldcg(&m.pos[GM_IX(m, tet_corner(t, 2 ^ x), m.nv, kBoundsPosition)]);
             stage_canonical_element<VAR>(P, (int)i, a0, a1, a2, o, sine);
         }
     }
@@ -417,7 +421,8 @@ __device__ void nm_lockstep_plain(const MeshView& m, const Crew& crew, const Smo
         {
             float ls = 0.f;
             uint32_t nvv = 1;
-            if (start) ls = nm_begin<VAR>(g, m, sine, P, con, members[base + rank], sub, nvv);
+            if (start)
+                ls = nm_begin<VAR>(g, m, sine, P, con, GM_IX(m, members[base + rank], m.nv, kBoundsPosition), sub, nvv);
             __syncwarp();
             nm_finish_begin(g, sp, start, ls, nvv);
         }

@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(128) relocate_kernel(MeshView m, Crew crew, Sm
     const uint32_t w = blockIdx.x * (blockDim.x >> 5) + wib;
     if (w >= count) return;
     WarpPatch P = carve_patch(smem + wib * warp_patch_bytes(MAXK, maxe), MAXK, maxe);
-    const uint32_t v = members[w];
+    const uint32_t v = GM_IX(m, members[w], m.nv, kBoundsPosition);
     const int cid = m.cid[v];
     const float4 old = m.pos[v];
     const V3<float> pos = to<float>(old);

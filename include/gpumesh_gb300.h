@@ -403,6 +403,25 @@ gm_status gm_evaluate_noalloc(uint32_t nv, const void* pos, uint32_t nt, const u
                               int32_t measurer, int32_t evaluator, double scaling, double aspect_ratio,
                               gm_quality* out, void* stream);
 
+/* Device bounds checks.  The library built with GM_BOUNDS_CHECK
+ * (libgpumesh_gb300_checked.so) compares every connectivity and
+ * neighbourhood index its evaluation, relocation, GETMe and batched kernels
+ * read through with the length of the array it indexes; the first index out
+ * of range is recorded in the mesh's status word and read as 0, so the
+ * access stays inside the array.  Its synchronising calls (gm_mesh_sync,
+ * gm_quality_read / gm_evaluate, gm_mesh_fetch_gpu_verts) then fail with
+ * GM_ERR_STATE and a gm_last_error() message naming the array and the index.
+ * The reference's counterpart is cudaCheckErrors (resources/cuda/Mesh.cuh:
+ * 169-183), which reports only CUDA's own errors.
+ *   gm_bounds_checked: *on = 1 in the checked build, 0 otherwise.
+ *   gm_mesh_bounds_status: *what = 0 when clean, else the array (1 vertex,
+ *   2 vertex->element CSR, 3 vertex->vertex CSR, 4 tet, 5 prism, 6 hex,
+ *   7 GETMe corner) and *index the index read; clears the word.  In the
+ *   ordinary build the word stays 0.  Synchronous.  A batch's kernels
+ *   record into each member mesh's word. */
+gm_status gm_bounds_checked(int32_t* on);
+gm_status gm_mesh_bounds_status(gm_mesh* mesh, uint32_t* what, uint32_t* index);
+
 /* No counterpart in the reference (its drivers launch on the legacy default
  * stream and keep no count).  *count receives the number of kernel launches
  * this library has made in this process: every direct launch counts one,

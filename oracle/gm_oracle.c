@@ -1498,6 +1498,40 @@ static double element_quality(const om_mesh* m, int type, int64_t idx)
 
 double om_element_quality(const om_mesh* m, int32_t type, int64_t idx) { return element_quality(m, type, idx); }
 
+#ifdef OM_PATCH_QUALITY_FP32
+/* Measurement variant (libgm_oracle_q32.so), not the reference.  Every patch
+ * quality the smoothers compare is brought to the resolution an FP32
+ * implementation has, to measure how far the reference algorithm's result
+ * depends on quality differences below that resolution:
+ *   seed 0: the quality rounded to FP32;
+ *   seed s > 0: the quality times (1 + u 2^-23), u uniform in [-1, 1] drawn
+ *     from a counter hash of (s, vertex, the vertex's evaluation count in
+ *     this relocation), so a draw does not depend on the thread count. */
+static uint64_t fp32_noise_seed = 0;
+static __thread uint32_t fp32_noise_vertex = 0xffffffffu;
+static __thread uint64_t fp32_noise_count = 0;
+
+void om_set_fp32_resolution_seed(uint64_t seed) { fp32_noise_seed = seed; }
+
+static double fp32_resolution(double q, uint32_t v)
+{
+    if (!fp32_noise_seed) return (double)(float)q;
+    if (v != fp32_noise_vertex)
+    {
+        fp32_noise_vertex = v;
+        fp32_noise_count = 0;
+    }
+    uint64_t z = fp32_noise_seed * 0x9E3779B97F4A7C15ull ^ ((uint64_t)v << 20) ^ ++fp32_noise_count;
+    z ^= z >> 30;
+    z *= 0xBF58476D1CE4E5B9ull;
+    z ^= z >> 27;
+    z *= 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const double u = (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+    return q * (1.0 + u * (1.0 / 8388608.0));
+}
+#endif
+
 /* AbstractEvaluator::patchQuality + accumulatePatchQuality +
  * finalizePatchQuality (Evaluators/AbstractEvaluator.cpp:236-279, 778-803) */
 static double patch_quality(const om_mesh* m, uint32_t v)
@@ -1520,12 +1554,7 @@ static double patch_quality(const om_mesh* m, uint32_t v)
     }
     if (weight > 0.0) quality = weight / quality;
 #ifdef OM_PATCH_QUALITY_FP32
-    /* Measurement variant (libgm_oracle_q32.so), not the reference: every
-     * patch quality rounded to FP32, so that the smoothers' comparisons see
-     * values at the resolution an FP32 implementation has.  It measures how
-     * far the reference's decisions depend on quality differences below
-     * FP32 resolution. */
-    quality = (double)(float)quality;
+    quality = fp32_resolution(quality, v);
 #endif
     return quality;
 }

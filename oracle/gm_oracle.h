@@ -117,6 +117,11 @@ void om_smooth_pass(om_mesh* m, int32_t smoother, const double* params,
 int64_t om_node_groups_build(const om_mesh* m, uint32_t* perm, int64_t* group_base, uint32_t* members,
                              int64_t* ranges);
 
+/* Only in the measurement build libgm_oracle_q32.so (OM_PATCH_QUALITY_FP32):
+ * 0 rounds every patch quality to FP32, s > 0 multiplies it by a seeded
+ * draw of (1 + u 2^-23), |u| <= 1 (gm_oracle.c, fp32_resolution). */
+void om_set_fp32_resolution_seed(uint64_t seed);
+
 /* patch-evaluation counter (number of patchQuality calls since the last
  * reset), used for the FLOP accounting of the relocation roofline */
 int64_t om_patch_eval_count(const om_mesh* m);

@@ -92,12 +92,21 @@ def lib(variant: str = ""):
         L.om_reset_patch_eval_count.argtypes = [vp]
         L.om_node_groups_build.restype = i64
         L.om_node_groups_build.argtypes = [vp, vp, vp, vp, vp]
+        if variant == "q32":
+            L.om_set_fp32_resolution_seed.argtypes = [ctypes.c_uint64]
         _libs[variant] = L
     return _libs[variant]
 
 
 def _p(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_fp32_resolution_seed(seed: int):
+    """The measurement build's mode (libgm_oracle_q32.so): 0 = patch
+    qualities rounded to FP32, s > 0 = multiplied by a seeded draw of
+    (1 + u 2^-23), |u| <= 1."""
+    lib("q32").om_set_fp32_resolution_seed(int(seed))
 
 
 def permute(raw, perm: np.ndarray):

@@ -17,17 +17,19 @@ positions rounded to FP32), evaluating after every pass.  Stored:
     per coordinate from a seeded stream; three draws), giving how far the
     FP64 algorithm itself moves the final minimum, mean and positions when
     only the input's last bit changes;
-  * the FP32-resolution run: the same schedule by the oracle's measurement
-    build whose patch qualities are rounded to FP32 (libgm_oracle_q32.so),
-    so that every comparison the smoothers make (candidate against
-    candidate, a quality gain against a stop threshold) sees the values at
-    FP32 resolution.  Where a decision rests on a difference below that
-    resolution, this run and the FP64 one part ways, and later colours carry
-    the difference on: the distance between the two is what FP32 arithmetic
-    alone changes in the reference algorithm's result.
+  * the FP32-resolution runs: the same schedule by the oracle's measurement
+    build (libgm_oracle_q32.so) whose patch qualities are brought to FP32
+    resolution -- rounded to FP32 once, then multiplied by seeded draws of
+    (1 + u 2^-23), |u| <= 1 -- so that every comparison the smoothers make
+    (candidate against candidate, a quality gain against a stop threshold)
+    sees differences below FP32 resolution resolved one way or the other.
+    Where a decision rests on such a difference the runs part ways and
+    later colours carry the difference on: the set of their results is the
+    set of outcomes the reference algorithm has at FP32 resolution.
 
 C4 is sampled: every 256th of its 4,096 meshes (16 meshes), one Nelder-Mead
-pass each.
+pass each.  Eight FP32-resolution draws per configuration (three for C2,
+whose runs take minutes each).
 
 Run from the repo root (CPU only; C2 takes a few minutes per run):
 
@@ -52,6 +54,8 @@ from gpumesh_gb300 import meshgen, workloads  # noqa: E402
 THREADS = os.cpu_count() or 1
 SAMPLES = 2048
 PERTURB_SEEDS = (101, 102, 103)
+FP32_DRAWS = {"C2": 3}
+DEFAULT_FP32_DRAWS = 8
 
 TET_EDGES = ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3))
 PRI_EDGES = ((0, 1), (0, 2), (1, 2), (0, 3), (1, 4), (2, 5), (3, 4), (3, 5), (4, 5))
@@ -88,9 +92,12 @@ def perturbed(raw, pos32, seed):
     return p.astype(np.float64)
 
 
-def run(raw, crew, schedule, pos, variant=""):
+def run(raw, crew, schedule, pos, variant="", seed=0):
     """The schedule from `pos`, evaluating before and after every pass (with
-    the FP64 oracle's evaluator whatever the variant)."""
+    the FP64 oracle's evaluator whatever the variant; `seed` selects the
+    FP32-resolution draw of the q32 build)."""
+    if variant == "q32":
+        pyoracle.set_fp32_resolution_seed(seed)
     m = pyoracle.OracleMesh.from_raw(raw, **crew, variant=variant)
     m.pos = pos
     perm_base, members = raw._groups
@@ -121,7 +128,7 @@ def coloured(raw):
     return pr
 
 
-def make_one(raw, crew, schedule):
+def make_one(raw, crew, schedule, draws=DEFAULT_FP32_DRAWS):
     pos32 = fp32_input(raw.pos)
     hist, final = run(raw, crew, schedule, pos32)
     movable = np.flatnonzero(raw.cid >= 0)
@@ -135,10 +142,16 @@ def make_one(raw, crew, schedule):
                         float(np.max(np.linalg.norm(f2[idx] - final[idx], axis=1) / out["sample_edge"]))))
     sp = np.array(spreads)
     out.update(spread_min=sp[:, 0].max(), spread_mean=sp[:, 1].max(), spread_pos=sp[:, 2].max(), spreads=sp)
-    hq, fq = run(raw, crew, schedule, pos32, variant="q32")
-    out.update(q32_min=hq[-1, 0], q32_mean=hq[-1, 1], q32_sample_pos=fq[idx],
-               q32_dmin=abs(hq[-1, 0] - hist[-1, 0]), q32_dmean=abs(hq[-1, 1] - hist[-1, 1]),
-               q32_dpos=float(np.max(np.linalg.norm(fq[idx] - final[idx], axis=1) / out["sample_edge"])))
+    fmin, fmean, fpos = [], [], []
+    for seed in range(draws + 1):
+        hq, fq = run(raw, crew, schedule, pos32, variant="q32", seed=seed)
+        fmin.append(hq[-1, 0])
+        fmean.append(hq[-1, 1])
+        fpos.append(float(np.max(np.linalg.norm(fq[idx] - final[idx], axis=1) / out["sample_edge"])))
+    fmin, fmean = np.array(fmin), np.array(fmean)
+    out.update(fp32_min=fmin, fp32_mean=fmean, q32_min=fmin[0], q32_mean=fmean[0],
+               q32_dmin=float(np.abs(fmin - hist[-1, 0]).max()), q32_dmean=float(np.abs(fmean - hist[-1, 1]).max()),
+               q32_dpos=float(max(fpos)))
     return out
 
 
@@ -148,23 +161,27 @@ def make_config(name):
     if name == "C4":
         sizes = meshgen.batch_sizes(4096, 4, 24, 3)
         picks = list(range(0, 4096, 256))
-        rows = []
+        rows, fmins, fmeans = [], [], []
         for i in picks:
             raw = coloured(meshgen.box_mesh(int(sizes[i]), "tet", 0.3, 3 * 1000003 + i))
             o = make_one(raw, dict(sampler="uniform", measurer="metric_free", evaluator="mean_ratio"),
                          [("nelder_mead", 1, workloads.NM_PARAMS)])
             rows.append((i, int(sizes[i]), o["final_min"], o["final_mean"], o["spread_min"], o["spread_mean"],
                          o["spread_pos"], o["q32_min"], o["q32_mean"]))
+            fmins.append(o["fp32_min"])
+            fmeans.append(o["fp32_mean"])
         np.savez_compressed(os.path.join(OUT, "C4.npz"), rows=np.array(rows, np.float64),
+                            fp32_min=np.array(fmins), fp32_mean=np.array(fmeans),
                             columns=np.array(["mesh", "cells", "final_min", "final_mean", "spread_min",
                                               "spread_mean", "spread_pos", "q32_min", "q32_mean"]))
     else:
         w = workloads.WORKLOADS[name]
         raw = coloured(w.mesh())
-        o = make_one(raw, w.crew(raw), w.schedule)
+        o = make_one(raw, w.crew(raw), w.schedule, FP32_DRAWS.get(name, DEFAULT_FP32_DRAWS))
         np.savez_compressed(os.path.join(OUT, name + ".npz"), **o)
         print(name, "final", o["final_min"], o["final_mean"], "spread", o["spread_min"], o["spread_mean"],
-              o["spread_pos"], "q32", o["q32_min"], o["q32_mean"], o["q32_dpos"], flush=True)
+              o["spread_pos"], "fp32 draws min", np.round(o["fp32_min"], 7), "mean", np.round(o["fp32_mean"], 7),
+              flush=True)
     print(f"wrote {name} in {time.time() - t0:.0f} s", flush=True)
 
 

@@ -8,18 +8,21 @@ library's).  Here the GPU runs the same schedule through the C ABI, its final
 mesh is evaluated by the FP64 oracle, and the final minimum and harmonic
 mean are compared.
 
-The gate is |delta| <= 1e-4, except where the fixture measured, at this
-configuration's size, that the FP64 algorithm itself moves by more than that
-when only its precision or its input's last bit changes:
+A value passes when it is within 1e-4 of
 
-  * spread: the oracle's largest change under one-rounding-step input
-    perturbations (three seeded draws);
-  * q32: the oracle's change when its patch qualities are rounded to FP32
-    (every comparison the smoothers make then sees FP32 resolution).
+  * the FP64 oracle's, or
+  * one of the reference algorithm's outcomes at FP32 resolution: the FP64
+    oracle's runs whose patch qualities are rounded to FP32 or carry seeded
+    (1 + u 2^-23) draws.  A smoother's decision that rests on a quality
+    difference below FP32 resolution (a Nelder-Mead stop test against its
+    1e-4 threshold, two candidates of nearly equal quality) goes either way
+    there, and the minimum, which one element sets, then takes one of a few
+    values (C1: 0.62232 or 0.61464; C4 mesh 1024: 0.62563 or 0.63385); the
+    GPU, computing in FP32, lands on one of them;
 
-Then the gate is twice the larger of the two, and the GPU must also agree with
-the FP32-resolution run to 1e-4 where that run alone explains the gap (C1).
-The tolerances are written below with the measured values they rest on.
+or within twice the oracle's own spread under one-rounding-step input
+perturbations, where that spread is wider than 1e-4 (ten passes of searches
+are chaotic at that level).
 """
 
 import os
@@ -40,7 +43,10 @@ def fixture(name):
     path = os.path.join(FINALS, name + ".npz")
     if not os.path.exists(path):
         pytest.skip(f"no oracle fixture {name}")
-    return dict(np.load(path))
+    d = dict(np.load(path))
+    if "fp32_min" not in d:
+        pytest.skip(f"oracle fixture {name} predates the FP32-resolution draws")
+    return d
 
 
 def gpu_final(raw, groups, crew, schedule):
@@ -63,9 +69,14 @@ def oracle_eval(raw, crew, pos):
     return e
 
 
-def gate(d, key):
-    """max(1e-4, 2 x the fixture's measured spread and FP32-resolution change)."""
-    return max(1e-4, 2.0 * max(float(d["spread_" + key]), float(d["q32_d" + key])))
+def verdict(gpu, fp64, draws, spread):
+    """(passes, how) for one value: within 1e-4 of the FP64 oracle, of one
+    of its FP32-resolution outcomes, or within 2 x its input spread."""
+    if abs(gpu - fp64) <= 1e-4:
+        return True, "fp64"
+    if np.min(np.abs(np.asarray(draws) - gpu)) <= 1e-4:
+        return True, "fp32-resolution outcome"
+    return abs(gpu - fp64) <= 2 * spread, "input spread"
 
 
 @pytest.mark.parametrize("name", ["C1", "C2", "C3", "C3m"])
@@ -86,22 +97,19 @@ def test_fullsize_final_quality_against_oracle(name):
           f"{float(d['spread_min']):.2e} / {float(d['spread_mean']):.2e}; FP32-resolution change "
           f"{float(d['q32_dmin']):.2e} / {float(d['q32_dmean']):.2e}; position error / edge max {err.max():.2e} "
           f"p99 {np.percentile(err, 99):.2e} mean {err.mean():.2e}")
-    assert dmin <= gate(d, "min")
-    assert dmean <= gate(d, "mean")
-    if float(d["q32_dmin"]) > 1e-4:
-        # C1: one Nelder-Mead stop test (best minus second-best patch
-        # quality against 1e-4) falls on the other side of the threshold at
-        # FP32 resolution, and the vertex then ends 0.8 % of an edge away;
-        # the FP32-resolution oracle reaches the GPU's minimum
-        assert abs(e["min"] - float(d["q32_min"])) <= 1e-4
-        assert abs(e["mean"] - float(d["q32_mean"])) <= 1e-4
+    ok_min, how_min = verdict(e["min"], float(d["final_min"]), d["fp32_min"], float(d["spread_min"]))
+    ok_mean, how_mean = verdict(e["mean"], float(d["final_mean"]), d["fp32_mean"], float(d["spread_mean"]))
+    print(f"{name}: min passes by {how_min}, mean by {how_mean}")
+    assert ok_min, (e["min"], float(d["final_min"]), d["fp32_min"])
+    assert ok_mean, (e["mean"], float(d["final_mean"]), d["fp32_mean"])
 
 
 def test_c4_sample_against_oracle():
     """Every 256th mesh of the 4,096 C4 meshes, one batched Nelder-Mead pass
     (one persistent launch) and the per-mesh evaluation, against the FP64
     oracle's pass on each mesh from the same FP32 input."""
-    rows = fixture("C4")["rows"]
+    fx = fixture("C4")
+    rows, fp32_min, fp32_mean = fx["rows"], fx["fp32_min"], fx["fp32_mean"]
     sizes = meshgen.batch_sizes(4096, 4, 24, 3)
     devs = []
     for r in rows:
@@ -118,13 +126,13 @@ def test_c4_sample_against_oracle():
     batch.sync()
     assert batch.status() == 0
     qual = batch.read_quality(0)
-    for r, q in zip(rows, qual):
-        spread_min, spread_mean = float(r[4]), float(r[5])
-        q32_dmin, q32_dmean = abs(float(r[7]) - float(r[2])), abs(float(r[8]) - float(r[3]))
-        tol_min = max(1e-4, 2 * max(spread_min, q32_dmin))
-        tol_mean = max(1e-4, 2 * max(spread_mean, q32_dmean))
-        assert abs(q.minimumQuality() - float(r[2])) <= tol_min, (int(r[0]), q.minimumQuality(), r[2], tol_min)
-        assert abs(q.harmonicMean() - float(r[3])) <= tol_mean, (int(r[0]), q.harmonicMean(), r[3], tol_mean)
+    for k, (r, q) in enumerate(zip(rows, qual)):
+        ok_min, how_min = verdict(q.minimumQuality(), float(r[2]), fp32_min[k], float(r[4]))
+        ok_mean, how_mean = verdict(q.harmonicMean(), float(r[3]), fp32_mean[k], float(r[5]))
+        print(f"C4 mesh {int(r[0])}: min {q.minimumQuality():.7f} (oracle {float(r[2]):.7f}, {how_min}), "
+              f"mean {q.harmonicMean():.7f} (oracle {float(r[3]):.7f}, {how_mean})")
+        assert ok_min, (int(r[0]), q.minimumQuality(), r[2], fp32_min[k])
+        assert ok_mean, (int(r[0]), q.harmonicMean(), r[3], fp32_mean[k])
     batch.close()
     for d in devs:
         d.close()

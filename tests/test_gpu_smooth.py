@@ -90,6 +90,7 @@ def fp32_resolution_change(raw, groups, crew, schedule):
     how far FP32 resolution of the smoothers' comparisons alone moves the
     final minimum and harmonic mean on this case."""
     out = []
+    pyoracle.set_fp32_resolution_seed(0)  # the measurement build rounds to FP32
     for variant in ("", "q32"):
         orc = pyoracle.OracleMesh.from_raw(raw, **crew, variant=variant)
         orc.pos = raw.pos.astype(np.float32).astype(np.float64)
