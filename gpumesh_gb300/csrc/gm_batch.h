@@ -57,5 +57,17 @@ cudaError_t launch_batch_relocate(int smoother, const BatchArgs& a, const Smooth
 cudaError_t launch_batch_evaluate(const BatchMesh* meshes, uint32_t nmesh, const EvalBlock* blocks, uint32_t nblocks,
                                   const uint32_t* mesh_block, EvalPartial* parts, Quality* out, int variant, int maxk,
                                   cudaStream_t s);
+// the general-metric variants, compiled apart (gm_batch_general_mc.cu:
+// metric conformity under the analytic and background-mesh samplers;
+// gm_batch_general_mrwise.cu: the metric-wise mean ratio) with one
+// 256-thread block per SM, the register budget of their metric evaluation
+cudaError_t launch_batch_relocate_mc(int smoother, const BatchArgs& a, const SmoothParams& sp, int maxk, int wpb,
+                                     int cps, int sm_count, cudaStream_t s);
+cudaError_t launch_batch_relocate_mrwise(int smoother, const BatchArgs& a, const SmoothParams& sp, int maxk, int wpb,
+                                         int cps, int sm_count, cudaStream_t s);
+cudaError_t launch_batch_eval_mc(const BatchMesh* meshes, const EvalBlock* blocks, uint32_t nblocks,
+                                 EvalPartial* parts, int maxk, cudaStream_t s);
+cudaError_t launch_batch_eval_mrwise(const BatchMesh* meshes, const EvalBlock* blocks, uint32_t nblocks,
+                                     EvalPartial* parts, int maxk, cudaStream_t s);
 
 }  // namespace gm

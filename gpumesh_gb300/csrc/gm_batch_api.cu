@@ -192,8 +192,7 @@ gm_status gm_batch_create(gm_batch** out, gm_mesh* const* meshes, uint32_t n)
                 require(m && m->nv && !m->group_base.empty(), "mesh " + std::to_string(i) + " has no groups");
                 require(m->device == b->device, "all meshes of a batch must live on the current device");
                 int v = m->variant();
-                require(v == kVarMRFree || v == kVarMCDiag,
-                        "the batched path runs mean ratio (metric-free) and metric conformity with a diagonal metric");
+                require(v == kVarMRFree || v == kVarMCDiag || v == kVarMC || v == kVarMRWise, "unknown kernel variant");
                 if (i == 0) b->variant = v;
                 require(v == b->variant, "all meshes of a batch must use the same evaluator and measurer");
                 b->maxk = std::max(b->maxk, m->maxk());

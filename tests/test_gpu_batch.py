@@ -120,3 +120,44 @@ def test_injected_stall_times_out_and_context_survives():
     # the device is still usable
     h = ds[0].evaluate()
     assert h.sampleCount() > 0
+
+
+# the general-metric variants (compiled apart, one 256-thread block per SM):
+# metric conformity under the analytic sampler and under the background-mesh
+# (local) sampler, and the metric-wise mean ratio under the analytic sampler
+GENERAL = {
+    "mc_analytic": dict(sampler="analytic", measurer="metric_wise", evaluator="metric_conformity", scaling=2.0,
+                        aspect_ratio=3.0),
+    "mr_wise_analytic": dict(sampler="analytic", measurer="metric_wise", evaluator="mean_ratio", scaling=2.0,
+                             aspect_ratio=3.0),
+    "mc_local": dict(sampler="local", measurer="metric_wise", evaluator="metric_conformity", scaling=2.0,
+                     aspect_ratio=3.0),
+}
+
+
+@pytest.mark.parametrize("crew_name", list(GENERAL))
+@pytest.mark.parametrize("kind", ["tet", "mixed"])
+@pytest.mark.parametrize("smoother,params", [("nelder_mead", workloads.NM_PARAMS), ("gradient_descent", None),
+                                             ("spawn_search", None), ("getme", [0.5])])
+def test_batch_general_metric_equals_plain(crew_name, kind, smoother, params):
+    """C4-style batches under a general metric run batched: mesh by mesh the
+    same positions as the plain path, and the batched evaluation the same
+    minimum, count and buckets as gm_evaluate."""
+    crew = GENERAL[crew_name]
+    ms = meshes(5, 13, kind)
+    plain = devices(ms, crew)
+    for d in plain:
+        d.smooth_pass(smoother, params)
+    batched = devices(ms, crew)
+    b = M.Batch(batched)
+    b.smooth_pass(smoother, params)
+    b.evaluate(0)
+    b.sync()
+    assert b.status() == 0
+    got = b.read_quality(0)
+    for d0, d1, q in zip(plain, batched, got):
+        assert np.array_equal(d0.fetch_positions(), d1.fetch_positions())
+        ref = d1.evaluate()
+        assert q.sampleCount() == ref.sampleCount() and q.minimumQuality() == ref.minimumQuality()
+        assert (q.buckets() == ref.buckets()).all()
+    b.close()

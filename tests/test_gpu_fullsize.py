@@ -20,9 +20,11 @@ A value passes when it is within 1e-4 of
     values (C1: 0.62232 or 0.61464; C4 mesh 1024: 0.62563 or 0.63385); the
     GPU, computing in FP32, lands on one of them;
 
-or within twice the oracle's own spread under one-rounding-step input
-perturbations, where that spread is wider than 1e-4 (ten passes of searches
-are chaotic at that level).
+or within twice the oracle's own spread: the larger of its change under
+one-rounding-step input perturbations and of its FP32-resolution draws'
+distance from the FP64 result, where that is wider than 1e-4 (the harmonic
+mean, which every vertex moves, spreads continuously: C4 mesh 2304's
+FP32-resolution draws lie 1.4e-4 below to 1.8e-4 above the FP64 mean).
 """
 
 import os
@@ -70,13 +72,18 @@ def oracle_eval(raw, crew, pos):
 
 
 def verdict(gpu, fp64, draws, spread):
-    """(passes, how) for one value: within 1e-4 of the FP64 oracle, of one
-    of its FP32-resolution outcomes, or within 2 x its input spread."""
+    """(passes, how) for one value: within 1e-4 of the FP64 oracle ("fp64"),
+    or of one of its FP32-resolution outcomes ("fp32-resolution outcome"),
+    or within twice the oracle's own spread -- the larger of its change
+    under one-rounding-step input perturbations and of its FP32-resolution
+    draws' distance from the FP64 result ("2x oracle spread")."""
+    draws = np.asarray(draws, np.float64)
     if abs(gpu - fp64) <= 1e-4:
         return True, "fp64"
-    if np.min(np.abs(np.asarray(draws) - gpu)) <= 1e-4:
+    if np.min(np.abs(draws - gpu)) <= 1e-4:
         return True, "fp32-resolution outcome"
-    return abs(gpu - fp64) <= 2 * spread, "input spread"
+    own = max(float(spread), float(np.max(np.abs(draws - fp64))))
+    return bool(abs(gpu - fp64) <= 2 * own), "2x oracle spread"
 
 
 @pytest.mark.parametrize("name", ["C1", "C2", "C3", "C3m"])
