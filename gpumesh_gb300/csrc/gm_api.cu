@@ -229,6 +229,7 @@ void ensure_deferred(gm_mesh* m)
 // acceptance launch for the vertices it handed over
 void relocate_group(gm_mesh* m, int smoother, const SmoothParams& sp, uint32_t base, uint32_t count, uint32_t slot)
 {
+    NvtxRange range("gm colour");
     if (count == 0) return;
     RelocLaunch L;
     L.variant = m->variant();
@@ -260,6 +261,7 @@ void relocate_group(gm_mesh* m, int smoother, const SmoothParams& sp, uint32_t b
 // one relocation pass: every colour in order (GETMe: the element pass first)
 void enqueue_pass(gm_mesh* m, int smoother, const SmoothParams& sp)
 {
+    NvtxRange range("gm pass");
     ensure_deferred(m);
     size_t ng = m->group_base.size() - 1;
     GM_CUDA(cudaMemsetAsync(m->def_count.p, 0, (ng + 2) * sizeof(uint32_t), m->stream));
@@ -293,6 +295,7 @@ void ensure_quality_slots(gm_mesh* m, uint32_t n)
 // one evaluation into `out` (device)
 void enqueue_evaluate(gm_mesh* m, Quality* out)
 {
+    NvtxRange range("gm evaluate");
     uint32_t total = m->nt + m->np + m->nh;
     int nb = evaluate_blocks(total, m->sm_count);
     if (m->parts.reserve(eval_scratch_slots(nb)))  // a fresh scratch starts with its ticket and bucket totals at 0
@@ -1137,6 +1140,7 @@ gm_status gm_job_prepare(gm_mesh* m, int32_t smoother, const double* params, uin
 
 gm_status gm_job_launch(gm_mesh* m)
 {
+    NvtxRange range("gm job launch");
     return guarded([&] {
         require(m && m->job_exec, "no job prepared on this mesh");
         GM_CUDA(cudaMemsetAsync(m->job_counter.p, 0, sizeof(int), m->stream));

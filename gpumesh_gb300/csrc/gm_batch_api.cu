@@ -135,6 +135,7 @@ void require_batch_smoother(int smoother)
 
 void enqueue_pass(gm_batch* b, int smoother, const SmoothParams& sp)
 {
+    NvtxRange range("gm batch pass");
     if (smoother == GM_SMOOTH_GETME)
         for (gm_mesh* m : b->meshes)
             GM_CUDA(launch_getme_elements(m->element_variant(), m->view(), m->crew, sp.lambda, m->corners.p,
@@ -165,6 +166,7 @@ void ensure_slots(gm_batch* b, uint32_t slot)
 
 void enqueue_evaluate(gm_batch* b, uint32_t slot)
 {
+    NvtxRange range("gm batch evaluate");
     GM_CUDA(launch_batch_evaluate(b->table.p, (uint32_t)b->meshes.size(), b->eval_blocks.p, b->n_eval_blocks,
                                   b->mesh_block.p, b->eval_parts.p, b->quality.p + (size_t)slot * b->meshes.size(),
                                   b->variant, b->maxk, b->stream));
@@ -372,6 +374,7 @@ gm_status gm_batch_capture_pass(gm_batch* b, int32_t smoother, const double* par
 
 gm_status gm_batch_replay(gm_batch* b)
 {
+    NvtxRange range("gm batch replay");
     return guarded([&] {
         require(b && b->graph_exec, "no captured pass");
         GM_CUDA(cudaGraphLaunch(b->graph_exec, b->stream));

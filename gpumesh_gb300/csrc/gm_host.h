@@ -10,9 +10,26 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/gpumesh_gb300.h"
 #include "gm_internal.h"
 #include "gm_launch.h"
+
+namespace gm {
+
+// An NVTX range for the lifetime of the object (per pass, per colour, per
+// evaluation, per batch or job launch), for a profiler's timeline; without
+// an attached tool a range costs one branch.
+struct NvtxRange
+{
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
+}  // namespace gm
 
 namespace gm {
 

@@ -6,7 +6,9 @@ reference tree (never copied) against the project-written stand-ins in
 oracle/ref_shim/ for its external dependencies (GLM, the CellarWorkbench log
 and GLSL wrapper, the GL loader), plus oracle/ref_stubs.cpp (the CUDA driver
 entry points, which abort if called) and the harness oracle/ref_harness.cpp.
-Nothing is built when the reference tree is absent.
+Nothing is built when the reference tree is absent.  The tree is
+GM_REFERENCE_TREE, else a directory named `reference` beside the
+repository.
 """
 
 from __future__ import annotations
@@ -19,7 +21,18 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libgmref.so")
-REF = os.environ.get("GM_REFERENCE_TREE", "/root/reference")
+
+
+
+def _reference_tree() -> str:
+    """The GpuMesh source tree: GM_REFERENCE_TREE, else a directory named
+    `reference` beside this repository's root."""
+    if os.environ.get("GM_REFERENCE_TREE"):
+        return os.environ["GM_REFERENCE_TREE"]
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
+REF = _reference_tree()
 
 SOURCES = [
     "DataStructures/Mesh.cpp", "DataStructures/NodeGroups.cpp", "DataStructures/MeshCrew.cpp",
