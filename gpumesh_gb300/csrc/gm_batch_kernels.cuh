@@ -314,7 +314,9 @@ __device__ __forceinline__ void batch_queue_loop(const BatchArgs& a, const Smoot
 
 template <int SMOOTHER, int VAR, int MAXK>
 __global__ void __launch_bounds__(256, BatchLockstep<SMOOTHER, VAR, MAXK>::on ? (VAR == kVarMRFree ? 3 : 2)
-                                      : (VAR == kVarMC || VAR == kVarMRWise) ? 1 : (MAXK == 4 ? 3 : 1))
+                                      : (VAR == kVarMC || VAR == kVarMRWise) ? 1
+                                      : (VAR == kVarMCDiag && MAXK == 4 && SMOOTHER != kSmoothGetme) ? 2
+                                      : (MAXK == 4 ? 3 : 1))
     batch_relocate_kernel(BatchArgs a, SmoothParams sp)
 {
     extern __shared__ __align__(16) char smem[];
@@ -442,7 +444,9 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchMesh* meshes
             const int n = MAXK == 4 ? 4 : type_size(type);
 #pragma unroll
             for (int k = 0; k < MAXK; ++k) p[k] = to<float>(__ldg(&m.pos[vid[k < n ? k : 0]]));
-            b = acc.add(elem_quality<VAR, MAXK, float>(crew, type, p));
+            // the element hint as gm_evaluate gives it: the background-mesh
+            // samplers start their walk at the element's first background tet
+            b = acc.add(elem_quality<VAR, MAXK, float>(crew, type, p, elem_hint(type, id)));
         }
         hist_add_warp(hist, b);
     }

