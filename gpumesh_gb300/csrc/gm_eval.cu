@@ -105,18 +105,13 @@ __device__ __forceinline__ void block_reduce(double& sum, float& mn, int& bad, d
 
 // One launch per evaluation: every block adds its bucket counts to the 20
 // totals (integer atomics: exact in any order) and stores its min / 1/q sum
-// / inverted count; the last block to finish reduces those in a fixed order
-// and writes the Quality, so the result does not depend on which block
-// finishes last.  The last block is found by a two-level ticket taken after
-// a release fence: a block counts itself in its group (blockIdx % 16), and
-// the last block of a group counts the group in the top ticket, so no
-// address takes more than nb / 16 of the blocks' returning atomics (one
-// ticket taken by all 608 blocks of a one-wave hex launch, which end
-// together, serialises those atomics at the end of every launch).
-// atomicInc wraps every ticket back to 0 and the last block clears the
-// totals, so the scratch is ready for the next launch.  (A last block that
-// also summed 20 bucket columns of every block spent tens of microseconds on
-// dependent L2 loads under the tet kernel's 40-register budget.)
+// / inverted count; the last block to finish (a ticket taken after a release
+// fence) reduces those in a fixed order and writes the Quality, so the
+// result does not depend on which block finishes last.  atomicInc wraps the
+// ticket back to 0 and the last block clears the totals, so the scratch is
+// ready for the next launch.  (A last block that also summed 20 bucket
+// columns of every block spent tens of microseconds on dependent L2 loads
+// under the tet kernel's 40-register budget.)
 struct EvalShared
 {
     int hist[20];
@@ -268,19 +263,7 @@ __device__ __forceinline__ void eval_epilogue(const EvalAcc& acc, EvalShared& sh
     }
     if (threadIdx.x < 20) __threadfence();  // every writer publishes its part of the partial
     __syncthreads();
-    if (threadIdx.x == 0)
-    {
-        const unsigned int g = blockIdx.x % kEvalTicketGroups;
-        const unsigned int gsize = ((unsigned int)nb - g + kEvalTicketGroups - 1) / kEvalTicketGroups;
-        const unsigned int ngroups = nb < kEvalTicketGroups ? (unsigned int)nb : kEvalTicketGroups;
-        bool last = atomicInc(&S.group[g], gsize - 1u) == gsize - 1u;
-        if (last)
-        {
-            __threadfence();  // the group's partials, seen through its ticket, before the top ticket
-            last = atomicInc(S.ticket, ngroups - 1u) == ngroups - 1u;
-        }
-        sh.last = last;
-    }
+    if (threadIdx.x == 0) sh.last = atomicInc(S.ticket, (unsigned int)nb - 1u) == (unsigned int)nb - 1u;
     __syncthreads();
     if (!sh.last) return;
     __threadfence();

@@ -30,24 +30,22 @@ struct EvalPartial
 };
 
 // Scratch of one evaluation launch of nb blocks, carved from EvalPartial
-// slots: 16 group tickets and the top ticket (80 bytes), the 20 bucket totals
-// every block adds to (80 bytes), then per block rsum[nb], min[nb], nbad[nb]
-// as structure-of-arrays so the last block reads them coalesced -- 160 + 16
-// nb bytes, which eval_scratch_slots(nb) slots hold.  The tickets and the
-// totals are zero between launches: a fresh scratch is cleared once, every
-// ticket wraps back to 0 as its last block takes it, and the last block of
-// every launch resets the totals.
-constexpr int kEvalTicketGroups = 16;
+// slots: a ticket word (8 bytes), the 20 bucket totals every block adds to
+// (80 bytes, padded to 88), then per block rsum[nb], min[nb], nbad[nb] as
+// structure-of-arrays so the last block reads them coalesced -- 96 + 16 nb
+// bytes, which eval_scratch_slots(nb) slots hold (two for a single block).
+// The ticket and the totals are zero between launches: a fresh scratch is
+// cleared once, and the last block of every launch resets them.
 struct EvalScratch
 {
-    unsigned int* group;   // group[g]: blocks of group g (blockIdx % 16 == g) done
-    unsigned int* ticket;  // groups done
-    unsigned int* hist;    // hist[b], summed over the blocks
+    unsigned int* ticket;
+    unsigned int* hist;  // hist[b], summed over the blocks
     double* rsum;
     float* min;
     int* nbad;
 };
-constexpr size_t kEvalScratchHead = 160;  // tickets + bucket totals, cleared together
+constexpr size_t kEvalScratchHead = 96;  // ticket + bucket totals, cleared together
+static_assert(sizeof(EvalPartial) >= kEvalScratchHead, "evaluation scratch layout");
 
 // EvalPartial slots that hold the scratch of an evaluation launch of nb blocks
 __host__ __device__ constexpr size_t eval_scratch_slots(size_t nb)
@@ -59,9 +57,8 @@ __host__ __device__ inline EvalScratch eval_scratch(EvalPartial* base, int nb)
 {
     char* p = reinterpret_cast<char*>(base);
     EvalScratch s;
-    s.group = reinterpret_cast<unsigned int*>(p);
-    s.ticket = reinterpret_cast<unsigned int*>(p + 4 * kEvalTicketGroups);
-    s.hist = reinterpret_cast<unsigned int*>(p + 80);
+    s.ticket = reinterpret_cast<unsigned int*>(p);
+    s.hist = reinterpret_cast<unsigned int*>(p + 8);
     p += kEvalScratchHead;
     s.rsum = reinterpret_cast<double*>(p);
     p += 8 * (size_t)nb;

@@ -13,7 +13,7 @@
 // library holds it (kNoAllocMaxPartials * sizeof(EvalPartial) = 104 KiB)
 // until the process exits.  All calls on one device share it and it keeps
 // the last call's contents; each call overwrites every partial it reads, and
-// the evaluation kernel returns the array's ticket words and bucket totals
+// the evaluation kernel returns the array's ticket word and bucket totals
 // (zero when the library is loaded) to zero at the end of every launch, so
 // no clearing is needed, but two calls that overlap on the GPU (for instance
 // on two streams) race on it and must be serialised by the caller.

@@ -89,9 +89,19 @@ def fp32_resolution_change(raw, groups, crew, schedule):
     are rounded to FP32 (its q32 measurement build), from the GPU's input:
     how far FP32 resolution of the smoothers' comparisons alone moves the
     final minimum and harmonic mean on this case."""
+    out = fp32_outcomes(raw, groups, crew, schedule, draws=0)
+    a, b = out[0], out[1]
+    return b, abs(b["min"] - a["min"]), abs(b["mean"] - a["mean"])
+
+
+def fp32_outcomes(raw, groups, crew, schedule, draws=4):
+    """The FP64 oracle's final evaluation from the GPU's input, then its runs
+    at FP32 resolution: patch qualities rounded to FP32, and `draws` seeded
+    (1 + u 2^-23) draws (the q32 measurement build)."""
     out = []
-    pyoracle.set_fp32_resolution_seed(0)  # the measurement build rounds to FP32
-    for variant in ("", "q32"):
+    for variant, seed in [("", 0)] + [("q32", s) for s in range(draws + 1)]:
+        if variant:
+            pyoracle.set_fp32_resolution_seed(seed)
         orc = pyoracle.OracleMesh.from_raw(raw, **crew, variant=variant)
         orc.pos = raw.pos.astype(np.float32).astype(np.float64)
         for smoother, passes, params in schedule:
@@ -100,8 +110,16 @@ def fp32_resolution_change(raw, groups, crew, schedule):
         chk = oracle_for(raw, crew)
         chk.pos = orc.pos
         out.append(chk.evaluate())
-    a, b = out
-    return b, abs(b["min"] - a["min"]), abs(b["mean"] - a["mean"])
+    return out
+
+
+def within_fp32_resolution(gpu, fp64, draws):
+    """Within 1e-4 of the FP64 result, of one of its FP32-resolution
+    outcomes, or within twice the outcomes' spread around the FP64 result."""
+    draws = np.asarray(draws, np.float64)
+    if abs(gpu - fp64) <= 1e-4 or np.min(np.abs(draws - gpu)) <= 1e-4:
+        return True
+    return abs(gpu - fp64) <= 2 * float(np.max(np.abs(draws - fp64)))
 
 
 def test_c1_nelder_mead_pass_quality():
@@ -135,18 +153,23 @@ def test_c1_nelder_mead_reference_params():
 
 def test_gradient_descent_and_spawn_on_sphere_metric_conformity():
     """Two GD and two spawn-search passes on a 16^3 sphere under the
-    sine-graded metric: min and harmonic mean within max(1e-4, 2 x the
-    change FP32 resolution alone makes in the FP64 oracle on this case)."""
+    sine-graded metric: min and harmonic mean within 1e-4 of the FP64
+    oracle, of one of its FP32-resolution outcomes (qualities rounded to
+    FP32, four seeded draws at that resolution), or within twice those
+    outcomes' spread (measured on this case: the minimum moves by ~1.4e-4
+    between draws, one element deciding it)."""
     raw, groups = coloured(meshgen.sphere_mesh(16, 0.25, 1))
     crew = dict(sampler="sine", measurer="metric_wise", evaluator="metric_conformity", scaling=1.0 / raw.h)
     sched = [("gradient_descent", 2, workloads.GD_PARAMS), ("spawn_search", 2, workloads.SPAWN_PARAMS)]
     gpos, opos, gq, oq, dev = run_both(raw, groups, crew, sched)
-    q32, dmin32, dmean32 = fp32_resolution_change(raw, groups, crew, sched)
+    runs = fp32_outcomes(raw, groups, crew, sched)
     b = raw.cid == 1
     assert np.abs(np.linalg.norm(gpos[b], axis=1) - 1.0).max() < 1e-5  # boundary stays on the sphere
-    assert abs(gq["min"] - oq["min"]) <= max(1e-4, 2 * dmin32), (gq["min"], oq["min"], dmin32)
+    assert within_fp32_resolution(gq["min"], oq["min"], [r["min"] for r in runs[1:]]), \
+        (gq["min"], oq["min"], [r["min"] for r in runs[1:]])
     if np.isfinite(oq["inv_sum"]) and np.isfinite(gq["inv_sum"]):
-        assert abs(gq["mean"] - oq["mean"]) <= max(1e-4, 2 * dmean32), (gq["mean"], oq["mean"], dmean32)
+        assert within_fp32_resolution(gq["mean"], oq["mean"], [r["mean"] for r in runs[1:]]), \
+            (gq["mean"], oq["mean"], [r["mean"] for r in runs[1:]])
 
 
 def test_getme_hex():

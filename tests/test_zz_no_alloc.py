@@ -31,24 +31,45 @@ def noalloc(torch, raw, crew, out):
                                      raw.pris.shape[0], pris.data_ptr() or None, raw.hexs.shape[0],
                                      hexs.data_ptr() or None, N.SAMPLERS[crew["sampler"]],
                                      N.MEASURERS[crew["measurer"]], N.EVALUATORS[crew["evaluator"]],
-                                     float(crew.get("scaling", 1.0)), 1.0, out.data_ptr(), None)
+                                     float(crew.get("scaling", 1.0)), float(crew.get("aspect_ratio", 1.0)),
+                                     out.data_ptr(), None)
     N.check(st)
     torch.cuda.synchronize()
     q = N.Quality.from_buffer_copy(out.cpu().numpy().tobytes())
     return M.QualityHistogram.from_native(q)
 
 
-@pytest.mark.parametrize("case", ["tet", "mixed_mc"])
+# every kernel variant the entry point selects: the tet and hex-only
+# mean-ratio streams, mixed meshes under the diagonal (sine) and the general
+# (analytic) metric, the metric-wise mean ratio, and a mesh of more than
+# 1024 x 256 elements, whose grid is the one-wave cap rather than one block
+# per 256 elements
+CASES = {
+    "tet": (lambda: meshgen.box_mesh(12, "tet", 0.3, 0),
+            dict(sampler="uniform", measurer="metric_free", evaluator="mean_ratio")),
+    "hex": (lambda: meshgen.box_mesh(10, "hex", 0.15, 2, gaussian=True),
+            dict(sampler="uniform", measurer="metric_free", evaluator="mean_ratio")),
+    "mixed_mc": (lambda: meshgen.box_mesh(7, "mixed", 0.15, 2, gaussian=True),
+                 dict(sampler="sine", measurer="metric_wise", evaluator="metric_conformity", scaling=3.0)),
+    "mixed_mc_analytic": (lambda: meshgen.box_mesh(6, "mixed", 0.1, 5),
+                          dict(sampler="analytic", measurer="metric_wise", evaluator="metric_conformity",
+                               scaling=2.0, aspect_ratio=3.0)),
+    "mixed_mr_wise": (lambda: meshgen.box_mesh(6, "mixed", 0.1, 5),
+                      dict(sampler="analytic", measurer="metric_wise", evaluator="mean_ratio", scaling=2.0,
+                           aspect_ratio=3.0)),
+    "tet_large": (lambda: meshgen.box_mesh(40, "tet", 0.3, 1),
+                  dict(sampler="uniform", measurer="metric_free", evaluator="mean_ratio")),
+}
+
+
+@pytest.mark.parametrize("case", list(CASES))
 def test_noalloc_matches_gm_evaluate_twice(case):
     torch = pytest.importorskip("torch")
-    if case == "tet":
-        raw = meshgen.box_mesh(12, "tet", 0.3, 0)
-        crew = dict(sampler="uniform", measurer="metric_free", evaluator="mean_ratio")
-    else:
-        raw = meshgen.box_mesh(7, "mixed", 0.15, 2, gaussian=True)
-        crew = dict(sampler="sine", measurer="metric_wise", evaluator="metric_conformity", scaling=3.0)
+    build, crew = CASES[case]
+    raw = build()
     dev = M.DeviceMesh(raw, None)
-    dev.set_crew(crew["sampler"], crew["measurer"], crew["evaluator"], crew.get("scaling", 1.0))
+    dev.set_crew(crew["sampler"], crew["measurer"], crew["evaluator"], crew.get("scaling", 1.0),
+                 crew.get("aspect_ratio", 1.0))
     ref = dev.evaluate()
     out = torch.zeros(ctypes.sizeof(N.Quality), dtype=torch.uint8, device="cuda")
     for _ in range(2):
