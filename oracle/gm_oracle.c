@@ -1040,14 +1040,29 @@ static int tri_intersect(v3 v1, v3 v2, v3 v3_, v3 orig, v3 dir)
  * background mesh from tet `cache` (through the face a ray from the current
  * tet's centroid, or from one of four weighted interior points, leaves), then
  * interpolate the vertex metrics barycentrically; a point outside the mesh
- * takes the clamped coordinates of the last tet */
+ * takes the clamped coordinates of the last tet.
+ *
+ * One addition: the reference's walk has no step limit, and on some inputs
+ * its rays cycle through a ring of tets and it never returns (a mixed box
+ * mesh jittered by 0.3 of a cell after one gradient-descent pass is one).
+ * Here, as on the GPU, a walk that has moved OM_LOCAL_WALK times without
+ * reaching the tet holding the point stops and takes the current tet's
+ * clamped coordinates, as an unreachable point does.  Walks that end within
+ * the limit are the reference's step for step. */
+#define OM_LOCAL_WALK 512
 static m3 local_metric(const om_mesh* m, v3 position, uint32_t cache)
 {
     const uint32_t* tet = m->bg + 8 * (size_t)cache;
     double coor[4];
     int isUnreachable = 0;
+    int steps = 0;
     while (!isUnreachable && !bg_params(m, tet, position, coor))
     {
+        if (++steps > OM_LOCAL_WALK)
+        {
+            isUnreachable = 1;
+            break;
+        }
         v3 vp[4];
         for (int k = 0; k < 4; ++k)
             vp[k] = V(m->bg_pos[3 * tet[k]], m->bg_pos[3 * tet[k] + 1], m->bg_pos[3 * tet[k] + 2]);

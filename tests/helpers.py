@@ -48,3 +48,31 @@ def edge_lengths(raw):
     np.add.at(c, e[:, 0], 1)
     np.add.at(c, e[:, 1], 1)
     return s / np.maximum(c, 1)
+
+
+def fp32_outcomes(raw, groups, crew, schedule, draws=4):
+    """The FP64 oracle's final evaluation from the GPU's input, then its runs
+    at FP32 resolution: patch qualities rounded to FP32, and `draws` seeded
+    (1 + u 2^-23) draws (the q32 measurement build)."""
+    out = []
+    for variant, seed in [("", 0)] + [("q32", s) for s in range(draws + 1)]:
+        if variant:
+            pyoracle.set_fp32_resolution_seed(seed)
+        orc = pyoracle.OracleMesh.from_raw(raw, **crew, variant=variant)
+        orc.pos = raw.pos.astype(np.float32).astype(np.float64)
+        for smoother, passes, params in schedule:
+            for _ in range(passes):
+                orc.smooth_pass(smoother, groups.group_base, groups.members, params=params, nthreads=4)
+        chk = oracle_for(raw, crew)
+        chk.pos = orc.pos
+        out.append(chk.evaluate())
+    return out
+
+
+def within_fp32_resolution(gpu, fp64, draws):
+    """Within 1e-4 of the FP64 result, of one of its FP32-resolution
+    outcomes, or within twice the outcomes' spread around the FP64 result."""
+    draws = np.asarray(draws, np.float64)
+    if abs(gpu - fp64) <= 1e-4 or np.min(np.abs(draws - gpu)) <= 1e-4:
+        return True
+    return abs(gpu - fp64) <= 2 * float(np.max(np.abs(draws - fp64)))

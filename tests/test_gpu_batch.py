@@ -11,7 +11,7 @@ import pytest
 from gpumesh_gb300 import mesh as M
 from gpumesh_gb300 import meshgen, workloads
 
-from helpers import coloured, device_for
+from helpers import coloured, device_for, fp32_outcomes, oracle_for, within_fp32_resolution
 
 pytestmark = pytest.mark.gpu
 
@@ -155,13 +155,26 @@ def test_batch_general_metric_equals_plain(crew_name, kind, smoother, params):
     b.sync()
     assert b.status() == 0
     got = b.read_quality(0)
-    for d0, d1, q in zip(plain, batched, got):
+    for (raw, groups), d0, d1, q in zip(ms, plain, batched, got):
         if smoother == "gradient_descent" and kind == "mixed":
-            # gradient descent on mixed meshes under the general metric lands
-            # a few FP32 rounding steps away (measured: at most 6e-7 in a
-            # coordinate of the [-1, 1] box) between the plain and the batched
-            # kernel, compiled apart; every other case is bit for bit
-            assert np.abs(d0.fetch_positions() - d1.fetch_positions()).max() <= 1e-5
+            # gradient descent on mixed meshes under the general metric: the
+            # plain and the batched kernel, compiled apart, contract the
+            # metric arithmetic differently, so most vertices land a few FP32
+            # rounding steps apart (measured: up to 6e-7 in a coordinate of
+            # the [-1, 1] box); where a step-acceptance comparison falls the
+            # other way at that resolution, a vertex takes another step
+            # (measured: 2.4e-4).  Both must then pass the same parity gate
+            # against the FP64 oracle; every other case is bit for bit.
+            p0, p1 = d0.fetch_positions(), d1.fetch_positions()
+            assert np.median(np.abs(p0 - p1).max(axis=1)) <= 1e-6
+            runs = fp32_outcomes(raw, groups, crew, [(smoother, 1, params)])
+            for p in (p0, p1):
+                chk = oracle_for(raw, crew)
+                chk.pos = p
+                e = chk.evaluate()
+                for k in ("min", "mean"):
+                    assert within_fp32_resolution(e[k], runs[0][k], [r[k] for r in runs[1:]]), \
+                        (k, e[k], runs[0][k], [r[k] for r in runs[1:]])
         else:
             assert np.array_equal(d0.fetch_positions(), d1.fetch_positions())
         ref = d1.evaluate()

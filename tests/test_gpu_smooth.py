@@ -23,7 +23,7 @@ import pytest
 from gpumesh_gb300 import meshgen, workloads
 
 import pyoracle
-from helpers import coloured, device_for, edge_lengths, oracle_for
+from helpers import coloured, device_for, edge_lengths, fp32_outcomes, oracle_for, within_fp32_resolution
 
 pytestmark = pytest.mark.gpu
 
@@ -92,34 +92,6 @@ def fp32_resolution_change(raw, groups, crew, schedule):
     out = fp32_outcomes(raw, groups, crew, schedule, draws=0)
     a, b = out[0], out[1]
     return b, abs(b["min"] - a["min"]), abs(b["mean"] - a["mean"])
-
-
-def fp32_outcomes(raw, groups, crew, schedule, draws=4):
-    """The FP64 oracle's final evaluation from the GPU's input, then its runs
-    at FP32 resolution: patch qualities rounded to FP32, and `draws` seeded
-    (1 + u 2^-23) draws (the q32 measurement build)."""
-    out = []
-    for variant, seed in [("", 0)] + [("q32", s) for s in range(draws + 1)]:
-        if variant:
-            pyoracle.set_fp32_resolution_seed(seed)
-        orc = pyoracle.OracleMesh.from_raw(raw, **crew, variant=variant)
-        orc.pos = raw.pos.astype(np.float32).astype(np.float64)
-        for smoother, passes, params in schedule:
-            for _ in range(passes):
-                orc.smooth_pass(smoother, groups.group_base, groups.members, params=params, nthreads=4)
-        chk = oracle_for(raw, crew)
-        chk.pos = orc.pos
-        out.append(chk.evaluate())
-    return out
-
-
-def within_fp32_resolution(gpu, fp64, draws):
-    """Within 1e-4 of the FP64 result, of one of its FP32-resolution
-    outcomes, or within twice the outcomes' spread around the FP64 result."""
-    draws = np.asarray(draws, np.float64)
-    if abs(gpu - fp64) <= 1e-4 or np.min(np.abs(draws - gpu)) <= 1e-4:
-        return True
-    return abs(gpu - fp64) <= 2 * float(np.max(np.abs(draws - fp64)))
 
 
 def test_c1_nelder_mead_pass_quality():
