@@ -31,18 +31,18 @@ struct EvalPartial
 
 // Scratch of one evaluation launch of nb blocks, carved from EvalPartial
 // slots: a ticket word (8 bytes), the 20 bucket totals every block adds to
-// (80 bytes, padded to 88), then per block rsum[nb], min[nb], nbad[nb] as
-// structure-of-arrays so the last block reads them coalesced -- 96 + 16 nb
-// bytes, which eval_scratch_slots(nb) slots hold (two for a single block).
-// The ticket and the totals are zero between launches: a fresh scratch is
-// cleared once, and the last block of every launch resets them.
+// (80 bytes, padded to 88), then one 16-byte record per block (its Σ1/q as
+// a double; its minimum's bits and its inverted count packed in the second
+// word), which the last block reads with one 16-byte load per block --
+// 96 + 16 nb bytes, which eval_scratch_slots(nb) slots hold (two for a
+// single block).  The ticket and the totals are zero between launches: a
+// fresh scratch is cleared once, and the last block of every launch resets
+// them.
 struct EvalScratch
 {
     unsigned int* ticket;
     unsigned int* hist;  // hist[b], summed over the blocks
-    double* rsum;
-    float* min;
-    int* nbad;
+    double2* rec;        // rec[block] = (Σ1/q, min | nbad << 32)
 };
 constexpr size_t kEvalScratchHead = 96;  // ticket + bucket totals, cleared together
 static_assert(sizeof(EvalPartial) >= kEvalScratchHead, "evaluation scratch layout");
@@ -53,18 +53,13 @@ __host__ __device__ constexpr size_t eval_scratch_slots(size_t nb)
     return (kEvalScratchHead + 16 * nb + sizeof(EvalPartial) - 1) / sizeof(EvalPartial);
 }
 
-__host__ __device__ inline EvalScratch eval_scratch(EvalPartial* base, int nb)
+__host__ __device__ inline EvalScratch eval_scratch(EvalPartial* base, int)
 {
     char* p = reinterpret_cast<char*>(base);
     EvalScratch s;
     s.ticket = reinterpret_cast<unsigned int*>(p);
     s.hist = reinterpret_cast<unsigned int*>(p + 8);
-    p += kEvalScratchHead;
-    s.rsum = reinterpret_cast<double*>(p);
-    p += 8 * (size_t)nb;
-    s.min = reinterpret_cast<float*>(p);
-    p += 4 * (size_t)nb;
-    s.nbad = reinterpret_cast<int*>(p);
+    s.rec = reinterpret_cast<double2*>(p + kEvalScratchHead);
     return s;
 }
 

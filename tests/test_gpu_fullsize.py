@@ -143,3 +143,48 @@ def test_c4_sample_against_oracle():
     batch.close()
     for d in devs:
         d.close()
+
+
+def test_c5_served_jobs_against_oracle():
+    """C5: a sample of the served stream's jobs (the first job of each mesh
+    kind and smoother among those of at most 20,000 tets, so that the FP64
+    oracle runs them in seconds), served together through the device job
+    graphs with the device stop rule, against the FP64 oracle running the
+    same smoother for the same number of passes on the same coloured mesh
+    from the same FP32 input; gated like the other configurations by the
+    oracle's FP32-resolution outcomes."""
+    from gpumesh_gb300 import serve
+    from helpers import edge_lengths, fp32_outcomes, within_fp32_resolution
+
+    stream = serve.poisson_stream()
+    picks, seen = [], set()
+    for spec in stream:
+        key = (spec.kind, spec.smoother)
+        t = 6 * spec.n ** 3 if spec.kind == "cube" else 3.2 * spec.n ** 3
+        if key not in seen and t <= 20000:
+            seen.add(key)
+            picks.append(spec)
+    assert len(picks) == 6
+    server = serve.Server(keep_results=True)
+    out = server.run(picks, realtime=False)
+    for spec in picks:
+        r = out.results[spec.job_id]
+        t = server.template(spec)
+        raw = M.RawMesh(pos=t.positions(spec.seed)[:, :3].astype(np.float64), tets=t.raw.tets, pris=t.raw.pris,
+                        hexs=t.raw.hexs, cid=t.raw.cid, con_kind=t.raw.con_kind, con_param=t.raw.con_param)
+        schedule = [(spec.smoother, r["passes"], server.params[spec.smoother])]
+        runs = fp32_outcomes(raw, t.groups, serve.MR, schedule)
+        e = oracle_eval(raw, serve.MR, r["pos"])
+        ref = pyoracle.OracleMesh.from_raw(raw, **serve.MR)
+        ref.pos = raw.pos.astype(np.float32).astype(np.float64)
+        for _ in range(r["passes"]):
+            ref.smooth_pass(spec.smoother, t.groups.group_base, t.groups.members,
+                            params=server.params[spec.smoother], nthreads=4)
+        err = np.linalg.norm(r["pos"] - ref.pos, axis=1) / edge_lengths(raw)
+        print(f"C5 job {spec.job_id} ({spec.kind} n={spec.n}, {spec.smoother}, {r['passes']} passes): min "
+              f"{e['min']:.7f} (oracle {runs[0]['min']:.7f}), mean {e['mean']:.7f} (oracle {runs[0]['mean']:.7f}); "
+              f"position error / edge p99 {np.percentile(err, 99):.2e} mean {err.mean():.2e}")
+        for k in ("min", "mean"):
+            assert within_fp32_resolution(e[k], runs[0][k], [x[k] for x in runs[1:]]), \
+                (spec.job_id, k, e[k], runs[0][k], [x[k] for x in runs[1:]])
+    server.close()
