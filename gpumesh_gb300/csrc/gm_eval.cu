@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <climits>
 
 #include "gm_launch.h"
 
@@ -165,6 +166,61 @@ __device__ __forceinline__ Conn<SET> load_conn(const MeshView& m, uint32_t i)
     return c;
 }
 
+// Hex mean ratio (MeanRatioEvaluator::hexQuality, the corner matrices Fk0-Fk7
+// of Evaluators/MeanRatioEvaluator.cpp:127-134) with each bottom corner k and the top
+// corner k+4 above it in the two halves of paired FP32 operations.  With
+// A_k = p[k+1] - p[k], B_k = p[k+5] - p[k+4] (indices of the bottom / top
+// face mod 4) and V_k = p[k+4] - p[k], the corner determinants are
+// det(V_k, A_{k-1}, A_k) and det(V_k, B_{k-1}, B_k), the same values
+// mr_hex_fast takes with its signs, so the pair X_k = (A_k, B_k) feeds both
+// halves of a cross product X_{k-1} x X_k; the dot product with V_k, the
+// powers and the bookkeeping stay scalar.  An inverted corner (det <= 0) is
+// tracked without branches: r's bit pattern with det's sign bit set is a
+// negative integer, and the smallest such integer is the inverted corner of
+// smallest r, so one signed integer minimum finds both whether the element
+// is inverted and its quality -3 / r.  Returns false when some r is not
+// finite (a corner with det = +-0, or |F|^2 overflowing), where the caller
+// takes mr_hex_fast's exact rules for flat corners instead.
+__device__ __forceinline__ bool mr_hex_pair(const V3<float>* p, EQ<float>& q)
+{
+    Pair3 X[4];
+    V3<float> V[4];
+    float2 L[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        const int n = (k + 1) & 3;
+        X[k].x = make_float2(p[n].x - p[k].x, p[n + 4].x - p[k + 4].x);
+        X[k].y = make_float2(p[n].y - p[k].y, p[n + 4].y - p[k + 4].y);
+        X[k].z = make_float2(p[n].z - p[k].z, p[n + 4].z - p[k + 4].z);
+        V[k] = p[k + 4] - p[k];
+        L[k] = pdot(X[k], X[k]);
+    }
+    float2 rs2 = make_float2(0.f, 0.f);
+    int tmin = INT_MAX;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        const int j = (k + 3) & 3;
+        const Pair3 C = pcross(X[j], X[k]);
+        const float d0 = fmaf(V[k].z, C.z.x, fmaf(V[k].y, C.y.x, V[k].x * C.x.x));
+        const float d1 = fmaf(V[k].z, C.z.y, fmaf(V[k].y, C.y.y, V[k].x * C.x.y));
+        const float v2 = fmaf(V[k].z, V[k].z, fmaf(V[k].y, V[k].y, V[k].x * V[k].x));
+        const float2 F = padd(padd(L[j], L[k]), pdup(v2));  // |F|^2 of the two corners
+        float2 lg = make_float2(lg2_fast(fabsf(d0)), lg2_fast(fabsf(d1)));
+        lg = pmul(lg, pdup(-0.666666666666666667f));
+        const float2 r = pmul(F, make_float2(ex2_fast(lg.x), ex2_fast(lg.y)));  // 3 / q per corner
+        rs2 = padd(rs2, r);
+        tmin = min(tmin, __float_as_int(r.x) | (__float_as_int(d0) & (int)0x80000000));
+        tmin = min(tmin, __float_as_int(r.y) | (__float_as_int(d1) & (int)0x80000000));
+    }
+    const float rsum = rs2.x + rs2.y;
+    if (!(rsum < INFINITY)) return false;
+    if (tmin >= 0) q = EQ<float>{rsum * (1.f / 24.f), true};
+    else q = EQ<float>{-3.f * rcp_fast(__int_as_float(tmin & 0x7fffffff)), false};
+    return true;
+}
+
 // quality of a tet or hex from its connectivity; returns the bucket
 template <int VAR, int SET>
 __device__ __forceinline__ int eval_conn(const MeshView& m, const Crew& crew, const Conn<SET>& c, EvalAcc& acc)
@@ -183,7 +239,25 @@ __device__ __forceinline__ int eval_conn(const MeshView& m, const Crew& crew, co
         p[7] = to<float>(__ldg(&m.pos[GM_IX(m, c.b.w, m.nv, kBoundsPosition)]));
     }
     EQ<float> q;
-    if constexpr (SET == 9 && VAR == kVarMRFree) q = mr_hex_fast(p);
+    if constexpr (SET == 9 && VAR == kVarMRFree)
+    {
+        if (!mr_hex_pair(p, q))
+        {
+            // rare (a flat corner): gather again rather than keep the
+            // positions live across the paired evaluation
+            const Conn<SET> c2 = load_conn<SET>(m, c.i);
+            V3<float> s[8];
+            s[0] = to<float>(__ldg(&m.pos[GM_IX(m, c2.a.x, m.nv, kBoundsPosition)]));
+            s[1] = to<float>(__ldg(&m.pos[GM_IX(m, c2.a.y, m.nv, kBoundsPosition)]));
+            s[2] = to<float>(__ldg(&m.pos[GM_IX(m, c2.a.z, m.nv, kBoundsPosition)]));
+            s[3] = to<float>(__ldg(&m.pos[GM_IX(m, c2.a.w, m.nv, kBoundsPosition)]));
+            s[4] = to<float>(__ldg(&m.pos[GM_IX(m, c2.b.x, m.nv, kBoundsPosition)]));
+            s[5] = to<float>(__ldg(&m.pos[GM_IX(m, c2.b.y, m.nv, kBoundsPosition)]));
+            s[6] = to<float>(__ldg(&m.pos[GM_IX(m, c2.b.z, m.nv, kBoundsPosition)]));
+            s[7] = to<float>(__ldg(&m.pos[GM_IX(m, c2.b.w, m.nv, kBoundsPosition)]));
+            q = mr_hex_fast(s);
+        }
+    }
     else if constexpr (SET == 9) q = elem_quality<VAR, MAXK, float>(crew, kHex, p, elem_hint(kHex, c.i));
     else q = elem_quality<VAR, MAXK, float>(crew, kTet, p, elem_hint(kTet, c.i));
     return acc.add(q);
@@ -193,6 +267,13 @@ template <int VAR, int SET>
 __global__ void __launch_bounds__(kEvalThreads, kEvalMinBlocks<VAR, SET>) evaluate_kernel(MeshView m, Crew crew, EvalPartial* parts,
                                                                 Quality* out)
 {
+    // launched with programmatic stream serialisation (launch_eval_t), the
+    // blocks may become resident while the stream's previous kernel drains:
+    // wait for its completion and memory before the first global access, and
+    // let the stream's next kernel be scheduled as this one's blocks retire
+    // (a dependent launched the same way waits the same way)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     __shared__ EvalShared sh;
     eval_prologue(sh);
     EvalAcc acc;
@@ -323,8 +404,8 @@ int evaluate_blocks(uint32_t total, int sm_count)
 constexpr int kEvalMaxDevices = 64;
 
 template <int VAR, int SET>
-static void launch_eval_t(const MeshView& m, const Crew& crew, EvalPartial* parts, int nblocks, Quality* out,
-                          cudaStream_t s)
+static cudaError_t launch_eval_t(const MeshView& m, const Crew& crew, EvalPartial* parts, int nblocks, Quality* out,
+                                 cudaStream_t s)
 {
     static std::atomic<uint32_t> wave[kEvalMaxDevices];
     int dev = 0;
@@ -349,31 +430,53 @@ static void launch_eval_t(const MeshView& m, const Crew& crew, EvalPartial* part
     long grid = ((long)total + per_block - 1) / per_block;
     grid = grid < (long)per_sm * sms ? grid : (long)per_sm * sms;
     grid = grid < nblocks ? grid : nblocks;
-    evaluate_kernel<VAR, SET><<<(unsigned)(grid < 1 ? 1 : grid), kEvalThreads, 0, s>>>(m, crew, parts, out);
+    // programmatic dependent launch outside stream capture: the launch and
+    // block scheduling overlap the previous kernel's last blocks (1.6 us of a
+    // 28 us hex evaluation measured back to back); captured graphs keep plain
+    // edges
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(grid < 1 ? 1 : grid));
+    cfg.blockDim = dim3(kEvalThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const cudaError_t qe = cudaStreamIsCapturing(s, &cap);
+    if (qe == cudaSuccess && cap == cudaStreamCaptureStatusNone)
+    {
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    else if (qe != cudaSuccess)
+        cudaGetLastError();  // the query's own error (a capture elsewhere): launch with plain edges
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, evaluate_kernel<VAR, SET>, m, crew, parts, out);
     note_launch();
+    return e;
 }
 
 cudaError_t launch_evaluate(int variant, int maxk, const MeshView& m, const Crew& crew, EvalPartial* parts,
                             int nblocks, Quality* out, cudaStream_t s)
 {
+    cudaError_t e;
     switch (variant)
     {
     case kVarMRFree:
-        if (maxk == 4) launch_eval_t<kVarMRFree, 4>(m, crew, parts, nblocks, out, s);
-        else if (maxk == 9) launch_eval_t<kVarMRFree, 9>(m, crew, parts, nblocks, out, s);
-        else launch_eval_t<kVarMRFree, 8>(m, crew, parts, nblocks, out, s);
+        if (maxk == 4) e = launch_eval_t<kVarMRFree, 4>(m, crew, parts, nblocks, out, s);
+        else if (maxk == 9) e = launch_eval_t<kVarMRFree, 9>(m, crew, parts, nblocks, out, s);
+        else e = launch_eval_t<kVarMRFree, 8>(m, crew, parts, nblocks, out, s);
         break;
     case kVarMCDiag:
-        if (maxk == 4) launch_eval_t<kVarMCDiag, 4>(m, crew, parts, nblocks, out, s);
-        else launch_eval_t<kVarMCDiag, 8>(m, crew, parts, nblocks, out, s);
+        if (maxk == 4) e = launch_eval_t<kVarMCDiag, 4>(m, crew, parts, nblocks, out, s);
+        else e = launch_eval_t<kVarMCDiag, 8>(m, crew, parts, nblocks, out, s);
         break;
-    case kVarMRWise: launch_eval_t<kVarMRWise, 8>(m, crew, parts, nblocks, out, s); break;
+    case kVarMRWise: e = launch_eval_t<kVarMRWise, 8>(m, crew, parts, nblocks, out, s); break;
     default:
-        if (maxk == 4) launch_eval_t<kVarMC, 4>(m, crew, parts, nblocks, out, s);
-        else launch_eval_t<kVarMC, 8>(m, crew, parts, nblocks, out, s);
+        if (maxk == 4) e = launch_eval_t<kVarMC, 4>(m, crew, parts, nblocks, out, s);
+        else e = launch_eval_t<kVarMC, 8>(m, crew, parts, nblocks, out, s);
         break;
     }
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 __global__ void __launch_bounds__(256) ffma_probe_kernel(int iters, float* sink)

@@ -91,9 +91,14 @@ struct EvalAcc
         {
             ++nbad;
             bmin = fminf(bmin, q.v);
-            qv = q.v;
+            qv = 0.f;
         }
-        return qv > 0.f ? min((int)(qv * 20.f), 19) : 0;
+        // floor(20 q) without a float-to-int conversion (a quarter-rate
+        // instruction): 2^23 added with rounding toward zero leaves the
+        // integer part of x < 2^23 in the low mantissa bits; x >= 2^23 and
+        // infinity give more than 19, NaN gives bucket 0
+        const float x = fmaxf(qv * 20.f, 0.f);
+        return min(__float_as_int(__fadd_rz(x, 8388608.f)) - 0x4B000000, 19);
     }
     __device__ __forceinline__ float min_quality() const { return nbad ? bmin : fminf(1.0f, __frcp_rn(rmax)); }
 };

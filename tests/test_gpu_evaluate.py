@@ -96,6 +96,22 @@ def test_hex_only_fast_path_matches_mixed_path():
     compare(raw, MR)
 
 
+def test_hex_flat_corners_follow_the_exact_rules():
+    """An interior vertex moved onto its +x neighbour collapses an edge: the
+    corners at both ends of it have a determinant of exactly zero, which the
+    paired hex evaluation hands to the scalar rules (an inverted corner of
+    quality 0).  The minimum, the infinite 1/q sum and the buckets agree with
+    the oracle."""
+    n = 4
+    raw = meshgen.box_mesh(n, "hex", 0.0, 0)
+    W = n + 1
+    a, b = 2 + W * (2 + W * 2), 3 + W * (2 + W * 2)
+    raw.pos[a] = raw.pos[b]
+    g, o = compare(raw, MR)
+    assert o["inv_sum"] == float("inf") and g.minimumQuality() <= 0.0
+    assert g.nonPositiveCount() == 4 and g.buckets()[0] == 4 and g.sampleCount() == n ** 3
+
+
 def test_inverted_elements_zero_mean():
     raw = meshgen.box_mesh(8, "tet", 0.6, 7)  # heavy jitter folds some tets
     g, o = compare(raw, MR)
