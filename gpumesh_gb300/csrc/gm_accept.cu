@@ -19,6 +19,7 @@ template <int VAR, int MAXK>
 __global__ void __launch_bounds__(128) accept_kernel(MeshView m, Crew crew, Deferred def, uint32_t slot_base,
                                                      uint32_t cap, int maxe)
 {
+    GM_PDL_ENTRY();
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t w = blockIdx.x * (blockDim.x >> 5) + wib;
@@ -44,10 +45,10 @@ static cudaError_t launch_accept_t(const RelocLaunch& L)
         if (e != cudaSuccess) return e;
     }
     unsigned blocks = (L.count + L.warps_per_block - 1) / L.warps_per_block;
-    accept_kernel<VAR, MAXK><<<blocks, 32 * L.warps_per_block, smem, L.stream>>>(L.m, L.crew, L.def, L.slot_base,
-                                                                               L.count, L.maxe);
+    const cudaError_t e = launch_pdl(accept_kernel<VAR, MAXK>, dim3(blocks), dim3(32 * L.warps_per_block), smem,
+                                     L.stream, L.m, L.crew, L.def, L.slot_base, L.count, L.maxe);
     note_launch();
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_accept(const RelocLaunch& L)

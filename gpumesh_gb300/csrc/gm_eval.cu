@@ -267,13 +267,7 @@ template <int VAR, int SET>
 __global__ void __launch_bounds__(kEvalThreads, kEvalMinBlocks<VAR, SET>) evaluate_kernel(MeshView m, Crew crew, EvalPartial* parts,
                                                                 Quality* out)
 {
-    // launched with programmatic stream serialisation (launch_eval_t), the
-    // blocks may become resident while the stream's previous kernel drains:
-    // wait for its completion and memory before the first global access, and
-    // let the stream's next kernel be scheduled as this one's blocks retire
-    // (a dependent launched the same way waits the same way)
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    GM_PDL_ENTRY();
     __shared__ EvalShared sh;
     eval_prologue(sh);
     EvalAcc acc;
@@ -430,27 +424,10 @@ static cudaError_t launch_eval_t(const MeshView& m, const Crew& crew, EvalPartia
     long grid = ((long)total + per_block - 1) / per_block;
     grid = grid < (long)per_sm * sms ? grid : (long)per_sm * sms;
     grid = grid < nblocks ? grid : nblocks;
-    // programmatic dependent launch outside stream capture: the launch and
-    // block scheduling overlap the previous kernel's last blocks (1.6 us of a
-    // 28 us hex evaluation measured back to back); captured graphs keep plain
-    // edges
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(grid < 1 ? 1 : grid));
-    cfg.blockDim = dim3(kEvalThreads);
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    const cudaError_t qe = cudaStreamIsCapturing(s, &cap);
-    if (qe == cudaSuccess && cap == cudaStreamCaptureStatusNone)
-    {
-        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        attr[0].val.programmaticStreamSerializationAllowed = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-    }
-    else if (qe != cudaSuccess)
-        cudaGetLastError();  // the query's own error (a capture elsewhere): launch with plain edges
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, evaluate_kernel<VAR, SET>, m, crew, parts, out);
+    // programmatic dependent launch: 1.6 us of a 28 us hex evaluation
+    // measured back to back
+    const cudaError_t e = launch_pdl(evaluate_kernel<VAR, SET>, dim3((unsigned)(grid < 1 ? 1 : grid)),
+                                     dim3(kEvalThreads), 0, s, m, crew, parts, out);
     note_launch();
     return e;
 }
@@ -476,7 +453,7 @@ cudaError_t launch_evaluate(int variant, int maxk, const MeshView& m, const Crew
         else e = launch_eval_t<kVarMC, 8>(m, crew, parts, nblocks, out, s);
         break;
     }
-    return e != cudaSuccess ? e : cudaGetLastError();
+    return e;
 }
 
 __global__ void __launch_bounds__(256) ffma_probe_kernel(int iters, float* sink)

@@ -30,6 +30,7 @@ __device__ __forceinline__ void getme_one(const MeshView& m, const Crew& crew, f
 template <int VAR>
 __global__ void __launch_bounds__(256) getme_elements_kernel(MeshView m, Crew crew, float lambda, float4* corners)
 {
+    GM_PDL_ENTRY();
     const uint32_t total = m.nt + m.np + m.nh;
     float4* ctet = corners;
     float4* cpri = corners + 4 * (size_t)m.nt;
@@ -50,15 +51,17 @@ cudaError_t launch_getme_elements(int variant, const MeshView& m, const Crew& cr
     long need = ((long)total + 255) / 256;
     long cap = (long)sm_count * 8;
     int blocks = (int)(need < cap ? need : cap);
+    void (*k)(MeshView, Crew, float, float4*);
     switch (variant)
     {
-    case kVarMRFree: getme_elements_kernel<kVarMRFree><<<blocks, 256, 0, s>>>(m, crew, lambda, corners); break;
-    case kVarMRWise: getme_elements_kernel<kVarMRWise><<<blocks, 256, 0, s>>>(m, crew, lambda, corners); break;
-    case kVarMC: getme_elements_kernel<kVarMC><<<blocks, 256, 0, s>>>(m, crew, lambda, corners); break;
-    default: getme_elements_kernel<kVarMCWise><<<blocks, 256, 0, s>>>(m, crew, lambda, corners); break;
+    case kVarMRFree: k = getme_elements_kernel<kVarMRFree>; break;
+    case kVarMRWise: k = getme_elements_kernel<kVarMRWise>; break;
+    case kVarMC: k = getme_elements_kernel<kVarMC>; break;
+    default: k = getme_elements_kernel<kVarMCWise>; break;
     }
+    const cudaError_t e = launch_pdl(k, dim3(blocks), dim3(256), 0, s, m, crew, lambda, corners);
     note_launch();
-    return cudaGetLastError();
+    return e;
 }
 
 // weighted average of the vertex's transformed corners
@@ -97,6 +100,7 @@ __global__ void __launch_bounds__(128) getme_update_kernel(MeshView m, Crew crew
                                                            uint32_t count, int maxe, Counters* ctr, Deferred def,
                                                            uint32_t slot_base)
 {
+    GM_PDL_ENTRY();
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t w = blockIdx.x * (blockDim.x >> 5) + wib;
@@ -145,10 +149,11 @@ static cudaError_t launch_update_t(const RelocLaunch& L, const float4* corners)
         if (e != cudaSuccess) return e;
     }
     unsigned blocks = (L.count + L.warps_per_block - 1) / L.warps_per_block;
-    getme_update_kernel<VAR, MAXK><<<blocks, 32 * L.warps_per_block, smem, L.stream>>>(
-        L.m, L.crew, L.sp, corners, L.members, L.count, L.maxe, L.ctr, L.def, L.slot_base);
+    const cudaError_t e = launch_pdl(getme_update_kernel<VAR, MAXK>, dim3(blocks), dim3(32 * L.warps_per_block), smem,
+                                     L.stream, L.m, L.crew, L.sp, corners, L.members, L.count, L.maxe, L.ctr, L.def,
+                                     L.slot_base);
     note_launch();
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_getme_update(const RelocLaunch& L, const float4* corners)

@@ -63,6 +63,18 @@ __host__ __device__ inline EvalScratch eval_scratch(EvalPartial* base, int)
     return s;
 }
 
+// First statement of every kernel that launch_pdl (gm_launch.h) launches:
+// wait for the stream's previous kernel to complete and its memory to be
+// visible before any global access, then let the stream's next kernel be
+// scheduled as this one's blocks retire.  Launched without the programmatic
+// attribute (inside a capture, or by another launcher) both return at once.
+#define GM_PDL_ENTRY()                                                      \
+    do                                                                      \
+    {                                                                       \
+        asm volatile("griddepcontrol.wait;" ::: "memory");                  \
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");     \
+    } while (0)
+
 // Per-thread accumulation of evaluated elements (QualityHistogram::add,
 // DataStructures/QualityHistogram.cpp:63-76).  The minimum over valid
 // elements is the reciprocal of the maximum 1/q (a correctly rounded

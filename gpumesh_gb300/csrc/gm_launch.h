@@ -3,9 +3,42 @@
 
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "gm_kernels.cuh"
 
 namespace gm {
+
+// Launch a kernel that begins with GM_PDL_ENTRY with programmatic stream
+// serialisation (programmatic dependent launch) unless the stream is being
+// captured: its launch and block scheduling overlap the previous kernel's
+// last blocks, and its first instruction waits for that kernel's completion
+// and memory, so nothing is read early.  A captured launch keeps plain graph
+// edges.  Returns the launch's status and clears it from the last error.
+template <class... P, class... A>
+inline cudaError_t launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const cudaError_t qe = cudaStreamIsCapturing(s, &cap);
+    if (qe == cudaSuccess && cap == cudaStreamCaptureStatusNone)
+    {
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    else if (qe != cudaSuccess)
+        cudaGetLastError();  // the query's own error (a capture elsewhere): plain edges
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+    const cudaError_t last = cudaGetLastError();
+    return e != cudaSuccess ? e : last;
+}
 
 // Kernel launches made by this library, reported by gm_launch_count.  Every
 // launch site calls note_launch() after its launch.  Outside stream capture

@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(128, kRelocMinBlocks<SMOOTHER, VAR, MAXK>) rel
                                                        const uint32_t* members, uint32_t count, int maxe,
                                                        Counters* ctr, Deferred def, uint32_t slot_base)
 {
+    GM_PDL_ENTRY();
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t w = blockIdx.x * (blockDim.x >> 5) + wib;
@@ -103,6 +104,7 @@ __global__ void __launch_bounds__(kNMWarpsPerBlock * 32, 4)
     relocate_nm_lockstep_kernel(MeshView m, Crew crew, SmoothParams sp, const uint32_t* members, uint32_t count,
                                 uint32_t per_warp, int maxe, Counters* ctr, Deferred def, uint32_t slot_base)
 {
+    GM_PDL_ENTRY();
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t begin = (blockIdx.x * (blockDim.x >> 5) + wib) * per_warp;
@@ -128,10 +130,11 @@ static cudaError_t launch_nm_lockstep(const RelocLaunch& L)
     per_warp = per_warp > 4u * kNMGroups ? 4u * kNMGroups : per_warp;
     const uint64_t per_block = (uint64_t)per_warp * kNMWarpsPerBlock;
     const unsigned blocks = (unsigned)((L.count + per_block - 1) / per_block);
-    relocate_nm_lockstep_kernel<VAR><<<blocks, 32 * kNMWarpsPerBlock, smem, L.stream>>>(
-        L.m, L.crew, L.sp, L.members, L.count, per_warp, L.maxe, L.ctr, L.def, L.slot_base);
+    const cudaError_t e = launch_pdl(relocate_nm_lockstep_kernel<VAR>, dim3(blocks), dim3(32 * kNMWarpsPerBlock), smem,
+                                     L.stream, L.m, L.crew, L.sp, L.members, L.count, per_warp, L.maxe, L.ctr, L.def,
+                                     L.slot_base);
     note_launch();
-    return cudaGetLastError();
+    return e;
 }
 
 template <int SMOOTHER, int VAR, int MAXK>
@@ -149,10 +152,11 @@ static cudaError_t launch_relocate_t(const RelocLaunch& L)
             if (e != cudaSuccess) return e;
         }
         unsigned blocks = (L.count + L.warps_per_block - 1) / L.warps_per_block;
-        relocate_kernel<SMOOTHER, VAR, MAXK><<<blocks, 32 * L.warps_per_block, smem, L.stream>>>(
-            L.m, L.crew, L.sp, L.members, L.count, L.maxe, L.ctr, L.def, L.slot_base);
+        const cudaError_t e =
+            launch_pdl(relocate_kernel<SMOOTHER, VAR, MAXK>, dim3(blocks), dim3(32 * L.warps_per_block), smem, L.stream,
+                       L.m, L.crew, L.sp, L.members, L.count, L.maxe, L.ctr, L.def, L.slot_base);
         note_launch();
-        return cudaGetLastError();
+        return e;
     }
 }
 
