@@ -479,7 +479,8 @@ cudaError_t launch_ffma_probe(int blocks, int threads, int iters, float* sink, c
 
 size_t patch_smem_per_warp(int maxk, int maxe)
 {
-    return (size_t)patch_slots(maxk) * maxe * sizeof(float4) + (size_t)maxe * sizeof(int) +
+    return (size_t)patch_slots(maxk) * maxe * sizeof(float4) +
+           (size_t)patch_pair_slots(maxk) * pair_stride(maxe) * sizeof(float4) + (size_t)maxe * sizeof(int) +
            kMaxCand * sizeof(float4) + kMaxCand * sizeof(float);
 }
 

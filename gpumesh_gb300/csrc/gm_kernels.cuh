@@ -164,9 +164,19 @@ struct Counters
 // either the 4 corner positions or the 5-slot canonical form below.
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr int patch_slots(int maxk) { return maxk == 4 ? 5 : maxk; }
+// canonical tet patches also keep the 5 slots with the elements of each pair
+// (2j, 2j + 1) interleaved, for the paired FP32 evaluation (canonical_mc_pair)
+__host__ __device__ constexpr int patch_pair_slots(int maxk) { return maxk == 4 ? 5 : 0; }
+// element stride of the interleaved slots: maxe rounded up to a pair
+__host__ __device__ constexpr int pair_stride(int maxe) { return (maxe + 1) & ~1; }
 struct WarpPatch
 {
     float4* sp;    // patch_slots(maxk) * maxe
+    // patch_pair_slots(maxk) * pair_stride(maxe), or null: slot k of element
+    // pair j is pp[k * pair_stride + 2j] = (x0, x1, y0, y1) and
+    // pp[k * pair_stride + 2j + 1] = (z0, z1, w0, w1), elements 2j and 2j + 1
+    // side by side, so one 16-byte load yields two ready operand pairs
+    float4* pp;
     int* meta;     // maxe: type | local << 2
     float4* cand;  // kMaxCand candidate positions
     float* res;    // kMaxCand patch qualities
@@ -178,7 +188,8 @@ struct WarpPatch
 // maxk: corners of the largest element type (4 tets only, 8 otherwise)
 __device__ __forceinline__ size_t warp_patch_bytes(int maxk, int maxe)
 {
-    return (size_t)patch_slots(maxk) * maxe * sizeof(float4) + (size_t)maxe * sizeof(int) +
+    return (size_t)patch_slots(maxk) * maxe * sizeof(float4) +
+           (size_t)patch_pair_slots(maxk) * pair_stride(maxe) * sizeof(float4) + (size_t)maxe * sizeof(int) +
            kMaxCand * sizeof(float4) + kMaxCand * sizeof(float);
 }
 
@@ -187,6 +198,8 @@ __device__ __forceinline__ WarpPatch carve_patch(char* base, int maxk, int maxe)
     WarpPatch p;
     p.sp = reinterpret_cast<float4*>(base);
     base += (size_t)patch_slots(maxk) * maxe * sizeof(float4);
+    p.pp = patch_pair_slots(maxk) ? reinterpret_cast<float4*>(base) : nullptr;
+    base += (size_t)patch_pair_slots(maxk) * pair_stride(maxe) * sizeof(float4);
     p.cand = reinterpret_cast<float4*>(base);
     base += kMaxCand * sizeof(float4);
     p.res = reinterpret_cast<float*>(base);
@@ -279,13 +292,25 @@ __device__ __forceinline__ void stage_canonical_element(WarpPatch& P, int i, flo
 #pragma unroll
         for (int k = 0; k < 5; ++k) sincospif(4.f * X[k], &s[k], &c[k]);
     }
-    P.sp[0 * P.maxe + i] = make_float4(r0.x, r0.y, r0.z, s[0]);
-    P.sp[1 * P.maxe + i] = make_float4(q1.x, q1.y, q1.z, c[0]);
-    P.sp[2 * P.maxe + i] = make_float4(q2.x, q2.y, q2.z, s[1]);
-    if (VAR == kVarMCDiag)
+    const float4 v[5] = {make_float4(r0.x, r0.y, r0.z, s[0]), make_float4(q1.x, q1.y, q1.z, c[0]),
+                         make_float4(q2.x, q2.y, q2.z, s[1]), make_float4(c[1], s[2], c[2], s[3]),
+                         make_float4(c[3], s[4], c[4], 0.f)};
+    constexpr int nslot = VAR == kVarMCDiag ? 5 : 3;
+#pragma unroll
+    for (int k = 0; k < nslot; ++k) P.sp[k * P.maxe + i] = v[k];
+    if (VAR == kVarMCDiag && P.pp)
     {
-        P.sp[3 * P.maxe + i] = make_float4(c[1], s[2], c[2], s[3]);
-        P.sp[4 * P.maxe + i] = make_float4(c[3], s[4], c[4], 0.f);
+        // the interleaved copy: this element's half of its pair's two float4
+        const int h = i & 1, ps = pair_stride(P.maxe);
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+        {
+            float* f = reinterpret_cast<float*>(P.pp + k * ps + (i & ~1));
+            f[h] = v[k].x;
+            f[2 + h] = v[k].y;
+            f[4 + h] = v[k].z;
+            f[6 + h] = v[k].w;
+        }
     }
 }
 
@@ -478,32 +503,33 @@ __device__ __forceinline__ EQ<float> pair_corner_result(float det, float f2)
     return EQ<float>{det < 0.f ? -rcp_fast(r) : 0.f, false};
 }
 
-// metric conformity under a diagonal metric, canonical elements e0 and e1
-// (e1 may be a padding slot whose result the caller drops)
-__device__ __forceinline__ void canonical_mc_pair(const WarpPatch& P, int e0, int e1, const TetCand& t,
-                                                  const TetConst& k, bool sine, EQ<float>& q0, EQ<float>& q1)
+// metric conformity under a diagonal metric, canonical elements 2j and 2j + 1
+// from the interleaved slots (element 2j + 1 may be a padding slot whose
+// result the caller drops)
+__device__ __forceinline__ void canonical_mc_pair(const WarpPatch& P, int j, const TetCand& t, const TetConst& k,
+                                                  bool sine, EQ<float>& q0, EQ<float>& q1)
 {
-    const int mx = P.maxe;
-    const float4 A0 = P.sp[e0], B0 = P.sp[mx + e0], C0 = P.sp[2 * mx + e0];
-    const float4 A1 = P.sp[e1], B1 = P.sp[mx + e1], C1 = P.sp[2 * mx + e1];
+    const int ps = pair_stride(P.maxe);
+    const float4* pp = P.pp + 2 * j;
+    // slot s: lo = (x0, x1, y0, y1), hi = (z0, z1, w0, w1)
+    const float4 Alo = pp[0], Ahi = pp[1], Blo = pp[ps], Bhi = pp[ps + 1], Clo = pp[2 * ps], Chi = pp[2 * ps + 1];
     // corner-matrix columns c_j = k_j (c - o) - Q_j, as rows R_i = (c0_i, c1_i, c2_i)
-    const Pair3 R0 = {psub(pdup(t.k0.x), make_float2(A0.x, A1.x)), psub(pdup(t.k1.x), make_float2(B0.x, B1.x)),
-                      psub(pdup(t.k2.x), make_float2(C0.x, C1.x))};
-    const Pair3 R1 = {psub(pdup(t.k0.y), make_float2(A0.y, A1.y)), psub(pdup(t.k1.y), make_float2(B0.y, B1.y)),
-                      psub(pdup(t.k2.y), make_float2(C0.y, C1.y))};
-    const Pair3 R2 = {psub(pdup(t.k0.z), make_float2(A0.z, A1.z)), psub(pdup(t.k1.z), make_float2(B0.z, B1.z)),
-                      psub(pdup(t.k2.z), make_float2(C0.z, C1.z))};
+    const Pair3 R0 = {psub(pdup(t.k0.x), make_float2(Alo.x, Alo.y)), psub(pdup(t.k1.x), make_float2(Blo.x, Blo.y)),
+                      psub(pdup(t.k2.x), make_float2(Clo.x, Clo.y))};
+    const Pair3 R1 = {psub(pdup(t.k0.y), make_float2(Alo.z, Alo.w)), psub(pdup(t.k1.y), make_float2(Blo.z, Blo.w)),
+                      psub(pdup(t.k2.y), make_float2(Clo.z, Clo.w))};
+    const Pair3 R2 = {psub(pdup(t.k0.z), make_float2(Ahi.x, Ahi.y)), psub(pdup(t.k1.z), make_float2(Bhi.x, Bhi.y)),
+                      psub(pdup(t.k2.z), make_float2(Chi.x, Chi.y))};
     float2 mxx = pdup(k.my);
     if (sine)
     {
-        const float4 D0 = P.sp[3 * mx + e0], F0 = P.sp[4 * mx + e0];
-        const float4 D1 = P.sp[3 * mx + e1], F1 = P.sp[4 * mx + e1];
+        const float4 Dlo = pp[3 * ps], Dhi = pp[3 * ps + 1], Flo = pp[4 * ps], Fhi = pp[4 * ps + 1];
         // sin(4 pi x) at the 5 Keast points by angle addition
-        const float2 s0 = pfma(make_float2(A0.w, A1.w), pdup(t.ca), pmul(make_float2(B0.w, B1.w), pdup(t.sa)));
-        const float2 s1 = pfma(make_float2(C0.w, C1.w), pdup(t.cq), pmul(make_float2(D0.x, D1.x), pdup(t.sq)));
-        const float2 s2 = pfma(make_float2(D0.y, D1.y), pdup(t.cq), pmul(make_float2(D0.z, D1.z), pdup(t.sq)));
-        const float2 s3 = pfma(make_float2(D0.w, D1.w), pdup(t.cq), pmul(make_float2(F0.x, F1.x), pdup(t.sq)));
-        const float2 s4 = pfma(make_float2(F0.y, F1.y), pdup(t.ch), pmul(make_float2(F0.z, F1.z), pdup(t.sh)));
+        const float2 s0 = pfma(make_float2(Ahi.z, Ahi.w), pdup(t.ca), pmul(make_float2(Bhi.z, Bhi.w), pdup(t.sa)));
+        const float2 s1 = pfma(make_float2(Chi.z, Chi.w), pdup(t.cq), pmul(make_float2(Dlo.x, Dlo.y), pdup(t.sq)));
+        const float2 s2 = pfma(make_float2(Dlo.z, Dlo.w), pdup(t.cq), pmul(make_float2(Dhi.x, Dhi.y), pdup(t.sq)));
+        const float2 s3 = pfma(make_float2(Dhi.z, Dhi.w), pdup(t.cq), pmul(make_float2(Flo.x, Flo.y), pdup(t.sq)));
+        const float2 s4 = pfma(make_float2(Flo.z, Flo.w), pdup(t.ch), pmul(make_float2(Fhi.x, Fhi.y), pdup(t.sh)));
         const float2 one = pdup(1.f), nine = pdup(9.f), ks = pdup(k.s2);
         const float2 m0 = pmul(ks, pfma(nine, pmul(s0, s0), one)), m1 = pmul(ks, pfma(nine, pmul(s1, s1), one));
         const float2 m2 = pmul(ks, pfma(nine, pmul(s2, s2), one)), m3 = pmul(ks, pfma(nine, pmul(s3, s3), one));
@@ -671,7 +697,7 @@ __device__ __forceinline__ void patch_multi(const Crew& crew, WarpPatch& P, int 
                 for (int j = sub; 2 * j < P.E; j += S)
                 {
                     EQ<float> q0, q1;
-                    canonical_mc_pair(P, 2 * j, 2 * j + 1, t, k, sine, q0, q1);
+                    canonical_mc_pair(P, j, t, k, sine, q0, q1);
                     acc_add(a, q0);
                     if (2 * j + 1 < P.E) acc_add(a, q1);
                 }

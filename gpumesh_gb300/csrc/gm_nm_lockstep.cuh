@@ -111,6 +111,7 @@ __device__ __forceinline__ WarpPatch nm_group_patch(char* wsm, int gi, int maxe)
 {
     WarpPatch P;
     P.sp = reinterpret_cast<float4*>(wsm) + (size_t)gi * nm_slots<VAR>() * maxe;
+    P.pp = nullptr;  // one candidate at a time: no paired evaluation
     P.meta = nullptr;
     P.cand = nullptr;
     P.res = nullptr;
