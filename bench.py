@@ -53,19 +53,21 @@ L2_NOTE = "GPU arm: L2 flushed (256 MiB write) before every step"
 # 1, an FMA counts 2), counted by hand from gm_kernels.cuh / gm_device.cuh:
 #   mean ratio, canonical tet (canonical_quality): 9 column subtractions,
 #     det 14, |F|^2 17, power 3, 1/q 2, accumulate 1                     = 46
-#   metric conformity, canonical tet, sine-graded metric: 9 columns, 5
-#     Keast sines by angle addition 15, 5 metric values 20, quadrature 6,
-#     cofactors + det + F F^T + cofactor products 92, weights 6, tNc 30,
-#     |tNc|^2 17, two square roots + add 3, accumulate 1                    = 199
-#   the same under the uniform metric (no quadrature work)                 = 158
+#   metric conformity, canonical tet, sine-graded metric (the paired
+#     evaluation, canonical_mc_pair): 9 columns, 5 Keast sines by angle
+#     addition 15, 5 metric values with the quadrature weight folded in 15,
+#     quadrature sum 4, cofactors + det + F F^T + cofactor products 92,
+#     weights 5, tNc 27 (tNc_yz = tNc_zy), |tNc|^2 16, two square roots +
+#     add 3, accumulate 1                                                  = 187
+#   the same under the uniform metric (no quadrature work)                 = 153
 #   mean ratio, hex (mr_hex): 12 edges 36, 8 corners x 36, combination 9  = 333
 # Per-candidate work (the frame columns, 3 sincospi) is shared by all the
 # elements of a patch and not counted.
 FLOPS_PER_ELEM_EVAL = {
     ("mean_ratio", "tet"): 46,
     ("mean_ratio", "hex"): 333,
-    ("metric_conformity", "tet", "sine"): 199,
-    ("metric_conformity", "tet", "uniform"): 158,
+    ("metric_conformity", "tet", "sine"): 187,
+    ("metric_conformity", "tet", "uniform"): 153,
 }
 
 # DRAM traffic of the first spawn-search colour of the C2 sphere (61,699

@@ -355,6 +355,10 @@ struct TetCand
 struct TetConst
 {
     float s2, my, mz, iy, iz;
+    // the sine metric's x entry at a Keast point is s2 (1 + 9 s^2); the
+    // paired evaluation folds the quadrature weight into it: w s2 and 9 w s2
+    // for w = 0.45 (points 1-4) and w = -0.8 (the centroid)
+    float q1, q9, c1, c9;
 };
 
 template <int VAR>
@@ -370,6 +374,10 @@ __device__ __forceinline__ TetConst tet_const(const Crew& crew)
         k.mz = k.my;
         k.iy = rcp_fast(k.my);
         k.iz = k.iy;
+        k.q1 = 0.45f * s2;
+        k.q9 = 9.f * k.q1;
+        k.c1 = -0.8f * s2;
+        k.c9 = 9.f * k.c1;
     }
     return k;
 }
@@ -470,8 +478,10 @@ __device__ __forceinline__ EQ<float> canonical_quality(const WarpPatch& P, int e
 // partly idle, so evaluating elements e0 and e1 of a patch in the two halves
 // of every operation halves the instructions of the element algebra; the
 // per-element transcendentals (reciprocals, square roots) stay scalar.  Each
-// half computes the operations of mc_corner_diag_fast in a fixed contraction
-// (explicit fma), so its result is an FP32 evaluation of the same formula.
+// half computes the quantities of mc_corner_diag_fast in a fixed contraction
+// (explicit fma), with the quadrature weights folded into the metric
+// constants and the equal y / z metric entries used (tNc_yz = tNc_zy), so its
+// result is an FP32 evaluation of the same formula.
 // ---------------------------------------------------------------------------
 struct Pair3
 {
@@ -530,11 +540,13 @@ __device__ __forceinline__ void canonical_mc_pair(const WarpPatch& P, int j, con
         const float2 s2 = pfma(make_float2(Dlo.z, Dlo.w), pdup(t.cq), pmul(make_float2(Dhi.x, Dhi.y), pdup(t.sq)));
         const float2 s3 = pfma(make_float2(Dhi.z, Dhi.w), pdup(t.cq), pmul(make_float2(Flo.x, Flo.y), pdup(t.sq)));
         const float2 s4 = pfma(make_float2(Flo.z, Flo.w), pdup(t.ch), pmul(make_float2(Fhi.x, Fhi.y), pdup(t.sh)));
-        const float2 one = pdup(1.f), nine = pdup(9.f), ks = pdup(k.s2);
-        const float2 m0 = pmul(ks, pfma(nine, pmul(s0, s0), one)), m1 = pmul(ks, pfma(nine, pmul(s1, s1), one));
-        const float2 m2 = pmul(ks, pfma(nine, pmul(s2, s2), one)), m3 = pmul(ks, pfma(nine, pmul(s3, s3), one));
-        const float2 m4 = pmul(ks, pfma(nine, pmul(s4, s4), one));
-        mxx = pfma(m0, pdup(-0.8f), pmul(padd(padd(padd(m1, m2), m3), m4), pdup(0.45f)));
+        // the quadrature sum -0.8 m0 + 0.45 (m1 + m2 + m3 + m4), each weighted
+        // metric value one multiply and one fused multiply-add
+        const float2 q1 = pdup(k.q1), q9 = pdup(k.q9);
+        const float2 m0 = pfma(s0, pmul(s0, pdup(k.c9)), pdup(k.c1));
+        const float2 m1 = pfma(s1, pmul(s1, q9), q1), m2 = pfma(s2, pmul(s2, q9), q1);
+        const float2 m3 = pfma(s3, pmul(s3, q9), q1), m4 = pfma(s4, pmul(s4, q9), q1);
+        mxx = padd(padd(padd(padd(m0, m1), m2), m3), m4);
     }
     // cofactor rows, det, F F^T and the cofactor products (mc_corner_diag_fast)
     const Pair3 N0 = pcross(R1, R2), N1 = pcross(R2, R0), N2 = pcross(R0, R1);
@@ -546,14 +558,16 @@ __device__ __forceinline__ void canonical_mc_pair(const WarpPatch& P, int j, con
     const float2 d2 = pmul(det, det);
     const float2 id2 = make_float2(rcp_fast(d2.x), rcp_fast(d2.y));
     const float2 wx = pmul(id2, make_float2(rcp_fast(mxx.x), rcp_fast(mxx.y)));
-    const float2 wy = pmul(id2, pdup(k.iy)), wz = pmul(id2, pdup(k.iz));
-    const float2 my = pdup(k.my), mz = pdup(k.mz), two = pdup(-2.f);
-    const float2 txx = padd(pfma(Nxx, wx, pmul(Axx, mxx)), two);
-    const float2 tyy = padd(pfma(Nyy, wy, pmul(Ayy, my)), two);
-    const float2 tzz = padd(pfma(Nzz, wz, pmul(Azz, mz)), two);
+    // the diagonal metrics here have equal y and z entries (my = mz, so
+    // wy = wz), which makes tNc_yz = tNc_zy
+    const float2 wy = pmul(id2, pdup(k.iy));
+    const float2 my = pdup(k.my), two = pdup(-2.f);
+    const float2 txx = pfma(Nxx, wx, pfma(Axx, mxx, two));
+    const float2 tyy = pfma(Nyy, wy, pfma(Ayy, my, two));
+    const float2 tzz = pfma(Nzz, wy, pfma(Azz, my, two));
     const float2 txy = pfma(Nxy, wx, pmul(Axy, my)), tyx = pfma(Nxy, wy, pmul(Axy, mxx));
-    const float2 txz = pfma(Nxz, wx, pmul(Axz, mz)), tzx = pfma(Nxz, wz, pmul(Axz, mxx));
-    const float2 tyz = pfma(Nyz, wy, pmul(Ayz, mz)), tzy = pfma(Nyz, wz, pmul(Ayz, my));
+    const float2 txz = pfma(Nxz, wx, pmul(Axz, my)), tzx = pfma(Nxz, wy, pmul(Axz, mxx));
+    const float2 tyz = pfma(Nyz, wy, pmul(Ayz, my));
     float2 f2 = pmul(txx, txx);
     f2 = pfma(tyy, tyy, f2);
     f2 = pfma(tzz, tzz, f2);
@@ -561,8 +575,7 @@ __device__ __forceinline__ void canonical_mc_pair(const WarpPatch& P, int j, con
     f2 = pfma(tyx, tyx, f2);
     f2 = pfma(txz, txz, f2);
     f2 = pfma(tzx, tzx, f2);
-    f2 = pfma(tyz, tyz, f2);
-    f2 = pfma(tzy, tzy, f2);
+    f2 = pfma(padd(tyz, tyz), tyz, f2);
     q0 = pair_corner_result(det.x, f2.x);
     q1 = pair_corner_result(det.y, f2.y);
 }
