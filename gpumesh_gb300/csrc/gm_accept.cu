@@ -1,9 +1,10 @@
 // FP64 acceptance test for near-degenerate patches.
 //
 // The FP32 relocation kernels hand over every vertex whose old or new patch
-// quality is below the acceptance threshold (1e-3 by default).  Here, one
-// warp per such vertex evaluates both patch qualities in FP64 and keeps the
-// move only if the new quality is not lower -- the rule of
+// quality is below the acceptance threshold (1e-3 by default).  Here a warp
+// per such vertex (a grid-stride loop over them) evaluates both patch
+// qualities in FP64 and keeps the move only if the new quality is not lower
+// -- the rule of
 // AbstractElementWiseSmoother::updateVertexPositions
 // (Smoothers/ElementWise/AbstractElementWiseSmoother.cpp:433-441).  The
 // vertex-wise smoothers always include the old position among their
@@ -22,16 +23,21 @@ __global__ void __launch_bounds__(128) accept_kernel(MeshView m, Crew crew, Defe
     GM_PDL_ENTRY();
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint32_t w = blockIdx.x * (blockDim.x >> 5) + wib;
-    const uint32_t n = *def.count;
-    if (w >= n || w >= cap) return;
+    const uint32_t n = min(*def.count, cap);
+    const uint32_t stride = gridDim.x * (blockDim.x >> 5);
     WarpPatch P = carve_patch(smem + wib * warp_patch_bytes(MAXK, maxe), MAXK, maxe);
-    const uint32_t v = GM_IX(m, def.v[slot_base + w], m.nv, kBoundsPosition);
-    stage_patch(m, v, P, lane);
-    const float4 oldp = def.oldp[slot_base + w], newp = def.newp[slot_base + w];
-    const double q0 = patch_uniform<VAR, MAXK, double>(crew, P, to<double>(oldp), lane);
-    const double q1 = patch_uniform<VAR, MAXK, double>(crew, P, to<double>(newp), lane);
-    if (lane == 0 && !(q1 < q0)) m.pos[v] = newp;
+    // the deferred vertices of one colour: an independent set, so the order
+    // in which the warps take them does not matter
+    for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + wib; w < n; w += stride)
+    {
+        const uint32_t v = GM_IX(m, def.v[slot_base + w], m.nv, kBoundsPosition);
+        stage_patch(m, v, P, lane);
+        const float4 oldp = def.oldp[slot_base + w], newp = def.newp[slot_base + w];
+        const double q0 = patch_uniform<VAR, MAXK, double>(crew, P, to<double>(oldp), lane);
+        const double q1 = patch_uniform<VAR, MAXK, double>(crew, P, to<double>(newp), lane);
+        if (lane == 0 && !(q1 < q0)) m.pos[v] = newp;
+        __syncwarp();  // the patch is staged again for the next vertex
+    }
 }
 
 template <int VAR, int MAXK>
@@ -44,7 +50,13 @@ static cudaError_t launch_accept_t(const RelocLaunch& L)
                                              (int)smem);
         if (e != cudaSuccess) return e;
     }
+    // the deferred count is on the device: a grid of a few blocks per SM loops
+    // over however many there are (usually a few dozen of a colour's
+    // thousands of vertices, so a grid sized to the colour was mostly warps
+    // that read the count and left)
     unsigned blocks = (L.count + L.warps_per_block - 1) / L.warps_per_block;
+    const unsigned cap_blocks = (unsigned)(L.sm_count > 0 ? L.sm_count : 152) * 4u;
+    blocks = blocks < cap_blocks ? blocks : cap_blocks;
     const cudaError_t e = launch_pdl(accept_kernel<VAR, MAXK>, dim3(blocks), dim3(32 * L.warps_per_block), smem,
                                      L.stream, L.m, L.crew, L.def, L.slot_base, L.count, L.maxe);
     note_launch();
