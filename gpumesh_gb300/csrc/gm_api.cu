@@ -114,6 +114,7 @@ void update_patch_shape(gm_mesh* m, const uint32_t* ve_off_host)
     uint32_t mx = 0;
     for (uint32_t v = 0; v < m->nv; ++v) mx = std::max(mx, ve_off_host[v + 1] - ve_off_host[v]);
     m->maxe = std::max<int>(32, (int)((mx + 31) / 32 * 32));
+    m->max_incident = (int)mx;
     m->ks = (m->nh || m->np) ? 8 : 4;
     size_t per = patch_smem_per_warp(m->ks, m->maxe);
     int wpb = 4;
@@ -240,6 +241,7 @@ void relocate_group(gm_mesh* m, int smoother, const SmoothParams& sp, uint32_t b
     L.members = m->members.p + base;
     L.count = count;
     L.maxe = m->maxe;
+    L.max_incident = m->max_incident;
     L.warps_per_block = m->warps_per_block;
     L.sm_count = m->sm_count;
     L.ctr = m->ctr.p;
@@ -872,6 +874,7 @@ gm_status gm_mesh_clone(gm_mesh* dst, const gm_mesh* src)
         if (dst->crew.sampler >= GM_SAMPLER_LOCAL) dst->crew.local = assemble_field(dst);
         dst->ks = src->ks;
         dst->maxe = src->maxe;
+        dst->max_incident = src->max_incident;
         dst->warps_per_block = src->warps_per_block;
         GM_CUDA(cudaStreamSynchronize(s));
     });

@@ -286,7 +286,12 @@ __global__ void __launch_bounds__(kGetmeGroupWarps * 32) getme_update_groups_ker
 template <int VAR>
 static cudaError_t launch_update_groups_t(const RelocLaunch& L, const float4* corners)
 {
-    const size_t smem = getme_group_bytes(L.maxe) * kGetmeGroups * kGetmeGroupWarps;
+    // a group's patch is sized by the mesh's largest vertex valence (8 on a
+    // hex mesh), not by the 32-padded maxe of the warp-per-vertex kernels:
+    // the shared memory then allows the 5 resident blocks per SM the
+    // registers do, instead of 3
+    const int maxe = L.max_incident > 0 ? L.max_incident : L.maxe;
+    const size_t smem = getme_group_bytes(maxe) * kGetmeGroups * kGetmeGroupWarps;
     if (smem > 48 * 1024)
     {
         cudaError_t e = cudaFuncSetAttribute(getme_update_groups_kernel<VAR>,
@@ -296,7 +301,7 @@ static cudaError_t launch_update_groups_t(const RelocLaunch& L, const float4* co
     const uint32_t per_block = kGetmeGroups * kGetmeGroupWarps;
     const unsigned blocks = (L.count + per_block - 1) / per_block;
     const cudaError_t e = launch_pdl(getme_update_groups_kernel<VAR>, dim3(blocks), dim3(32 * kGetmeGroupWarps), smem,
-                                     L.stream, L.m, L.crew, L.sp, corners, L.members, L.count, L.maxe, L.ctr, L.def,
+                                     L.stream, L.m, L.crew, L.sp, corners, L.members, L.count, maxe, L.ctr, L.def,
                                      L.slot_base);
     note_launch();
     return e;

@@ -227,6 +227,7 @@ struct gm_mesh
     Crew crew{};
     int ks = 4;
     int maxe = 32;
+    int max_incident = 0;  // the largest number of elements around a vertex (maxe is it padded to 32)
     int warps_per_block = 4;
     std::vector<float4> staging;  // host conversion buffer
     // device-resident job (gm_job_*): a CUDA graph running a whole stop-rule

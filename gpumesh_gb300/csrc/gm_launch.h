@@ -74,6 +74,7 @@ struct RelocLaunch
     const uint32_t* members;
     uint32_t count;
     int maxe;
+    int max_incident;  // the largest number of elements around a vertex (maxe is it padded)
     int warps_per_block;
     int sm_count;
     Counters* ctr;
