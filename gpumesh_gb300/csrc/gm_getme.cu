@@ -24,7 +24,10 @@ __device__ __forceinline__ void getme_one(const MeshView& m, const Crew& crew, f
     for (int k = 0; k < N; ++k) vp[k] = to<float>(m.pos[vi[k]]);  // vi checked by elem_vertices
     float w = getme_transform<VAR, float, N>(m, crew, lambda, type, vi, vp, vpp, elem_hint(type, id));
 #pragma unroll
-    for (int k = 0; k < N; ++k) out[(size_t)id * N + k] = make_float4(vpp[k].x, vpp[k].y, vpp[k].z, w);
+    // streaming stores: each corner is read once, by its vertex's update, and
+    // the corner buffer (16 B per element corner) is larger than the L2, so it
+    // should not push out the positions and connectivity the updates stage
+    for (int k = 0; k < N; ++k) __stcs(&out[(size_t)id * N + k], make_float4(vpp[k].x, vpp[k].y, vpp[k].z, w));
 }
 
 template <int VAR>
@@ -76,7 +79,7 @@ __device__ __forceinline__ bool getme_average(const MeshView& m, const float4* c
         uint32_t r = m.ve[GM_IX(m, i, m.ve_len, kBoundsNeighbourElem)];
         int type = ref_type(r);
         const size_t ci = base[type] + (size_t)ref_id(r) * type_size(type) + ref_local(r);
-        float4 c = corners[GM_IX(m, ci, 4 * m.nt + 6 * m.np + 8 * m.nh, kBoundsCorner)];
+        float4 c = __ldcs(&corners[GM_IX(m, ci, 4 * m.nt + 6 * m.np + 8 * m.nh, kBoundsCorner)]);  // read once
         sx += c.x * c.w;
         sy += c.y * c.w;
         sz += c.z * c.w;
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(kGetmeGroupWarps * 32) getme_update_groups_ker
             const uint32_t r = m.ve[GM_IX(m, i, m.ve_len, kBoundsNeighbourElem)];
             const int type = ref_type(r);
             const size_t ci = base[type] + (size_t)ref_id(r) * type_size(type) + ref_local(r);
-            const float4 c = corners[GM_IX(m, ci, 4 * m.nt + 6 * m.np + 8 * m.nh, kBoundsCorner)];
+            const float4 c = __ldcs(&corners[GM_IX(m, ci, 4 * m.nt + 6 * m.np + 8 * m.nh, kBoundsCorner)]);  // read once
             acc[k].x += c.x * c.w;
             acc[k].y += c.y * c.w;
             acc[k].z += c.z * c.w;
